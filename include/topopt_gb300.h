@@ -1,0 +1,164 @@
+/*
+ * libtopopt_gb300 -- GB300-native SIMP compliance minimisation with a
+ * matrix-free, multigrid-preconditioned CG state solve.
+ *
+ * Handle API (this header). The reference-signature drop-in entry points
+ * (top3dmgcg, applyStateOperator_stencil, ...) are declared in
+ * topopt_ref_api.h and are thin wrappers over this API.
+ *
+ * Conventions
+ *  - Every entry point returns tp_status (0 = TP_OK) except the plain getters.
+ *  - Arrays are double unless the name ends in _f32, and use the canonical
+ *    unpadded layout: level l has (nelx>>l)+1 x (nely>>l)+1 x (nelz>>l)+1
+ *    nodes, node (i,k,j) at n = (i*nz + k)*ny + j with DOFs 3n+0..2 (x,y,z);
+ *    fine element (i,k,j) at (i*nelz + k)*nely + j. This is the reference's
+ *    ordering (stencil_utility.h:19-52) without its halo and y-padding.
+ *  - "_dev" arguments are device pointers on the context's device; other
+ *    array arguments are host pointers. Work is stream-ordered on the
+ *    context's stream; tp_sync() waits for it.
+ *  - A context is used by one host thread at a time.
+ */
+#ifndef TOPOPT_GB300_H
+#define TOPOPT_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  TP_OK = 0,
+  TP_ERR_ARG = 1,           /* invalid argument or size */
+  TP_ERR_CUDA = 2,          /* a CUDA call or launch failed */
+  TP_ERR_ALLOC = 3,         /* device or host allocation failed */
+  TP_ERR_NOT_SPD = 4,       /* coarse Cholesky met a non-positive pivot */
+  TP_ERR_NOT_CONVERGED = 5, /* CG reached cgmax without relres < cgtol */
+  TP_ERR_NONFINITE = 6,     /* NaN/Inf in a residual or reduction */
+  TP_ERR_TIMEOUT = 7,       /* a bounded device wait gave up */
+  TP_ERR_STATE = 8          /* call out of order (e.g. operators not assembled) */
+} tp_status;
+
+typedef enum {
+  TP_FP64 = 0, /* everything FP64: the drop-in form of the reference's path */
+  TP_MIXED = 1 /* FP32 V-cycle and smoother; FP64 CG, dots, update, coarse Cholesky */
+} tp_precision;
+
+typedef struct tp_ctx tp_ctx;
+
+typedef struct {
+  int nelx, nely, nelz; /* fine elements; each divisible by 2^(nl-1) */
+  int nl;               /* multigrid levels, >= 3 (stencil_optimization.c:13) */
+  double volfrac;       /* volume fraction (the reference's main() holds it as float) */
+  double rmin;          /* density-filter radius in elements */
+  double cgtol;         /* relative residual tolerance (top3d.c:82) */
+  int cgmax;            /* CG iteration cap; the reference hard-codes 1000 (stencil_solvers.c:334) */
+  int nswp;             /* Jacobi sweeps per smoothing (stencil_optimization.c:154) */
+  double omega;         /* Jacobi damping (stencil_solvers.c:332) */
+  int precision;        /* tp_precision */
+  int nrhs;             /* load cases solved together (1 = the reference's single load) */
+  int device;           /* CUDA device ordinal */
+} tp_params;
+
+typedef struct {
+  int loop;        /* 1-based design iteration */
+  double c;        /* compliance (summed over load cases) */
+  double vol;      /* volume fraction of xPhys */
+  double change;   /* max |x - xnew|, rounded through float as the reference does */
+  int cgiters;     /* last CG iteration index, as the reference reports it */
+  double relres;   /* final relative residual, rounded through float */
+  double ms;       /* device milliseconds of this design iteration */
+} tp_iter_info;
+
+typedef enum {
+  TP_FIELD_X = 0,     /* design variables x (fine elements) */
+  TP_FIELD_XPHYS = 1, /* filtered densities xPhys */
+  TP_FIELD_XNEW = 2,
+  TP_FIELD_DC = 3,    /* compliance sensitivity (after the filter adjoint in the loop) */
+  TP_FIELD_DV = 4,    /* volume sensitivity, filter adjoint of ones */
+  TP_FIELD_F = 5,     /* load vectors, nrhs * ndof(0) */
+  TP_FIELD_U = 6      /* displacements, nrhs * ndof(0) */
+} tp_field;
+
+/* Reference defaults: 12x6x6 coarse elements at nl=4 (top3d.c:16-24),
+ * volfrac (float)0.2, rmin 1.5, cgtol (float)1e-5, cgmax 1000, nswp 4,
+ * omega 0.6, FP64, one load case, device 0. */
+void tp_default_params(tp_params* p);
+
+tp_status tp_create(const tp_params* p, tp_ctx** out);
+void tp_destroy(tp_ctx* c);
+const char* tp_status_string(tp_status s);
+const char* tp_error_message(const tp_ctx* c);
+tp_status tp_sync(tp_ctx* c);
+
+long tp_ndof(const tp_ctx* c, int level);   /* 3 * nodes of level */
+long tp_nelem(const tp_ctx* c);             /* fine elements */
+long tp_device_bytes(const tp_ctx* c);      /* device memory the context holds */
+double* tp_field_ptr(tp_ctx* c, tp_field f); /* device pointer to a context field */
+
+/* Host <-> device copies of context fields (count = elements of the field). */
+tp_status tp_upload(tp_ctx* c, tp_field f, const double* host, long count);
+tp_status tp_download(tp_ctx* c, tp_field f, double* host, long count);
+
+/* Set-up data, for checks: element stiffness tables of level l
+ * (576 * 8^l doubles, local_matrix.c:251-319) and the fixed DOFs of level l
+ * (stencil_grid_utility.c:7-65). *count receives the number written. */
+tp_status tp_element_matrices(const tp_ctx* c, int level, double* out_host);
+/* The same tables without a context (host only): nu = Poisson's ratio. */
+tp_status tp_element_matrix_tables(int level, double nu, double* out_host);
+/* The reference's cantilever load for a fine grid, host only
+ * (stencil_optimization.c:37-95): 3*(nelx+1)*(nely+1)*(nelz+1) doubles. */
+tp_status tp_reference_load(int nelx, int nely, int nelz, double* F_host);
+tp_status tp_fixed_dofs(const tp_ctx* c, int level, long* out_host, long* count);
+
+/* Builds every level's operator for the current xPhys: E(xPhys), inverse
+ * Jacobi diagonals, assembled stencils of levels >= 1, and the FP64 band
+ * Cholesky factor of the coarsest level (stencil_solvers.c:283-302). */
+tp_status tp_assemble(tp_ctx* c);
+
+/* Operators on device vectors of level `level`.
+ * level 0: the matrix-free hex8 stencil (stencil_methods.c:7-428);
+ * level 1: the subspace operator (stencil_methods.c:436-519);
+ * level >= 2: the assembled operator with fixed rows and columns zeroed
+ * (stencil_assembly.c:126-364). Fixed rows return the input. */
+tp_status tp_apply(tp_ctx* c, int level, const double* in_dev, double* out_dev);
+tp_status tp_apply_f32(tp_ctx* c, int level, const float* in_dev, float* out_dev);
+tp_status tp_inv_diag(tp_ctx* c, int level, double* out_dev);            /* stencil_methods.c:693-773 */
+tp_status tp_restrict(tp_ctx* c, int level, const double* fine_dev, double* coarse_dev);  /* :595-688 */
+tp_status tp_prolong(tp_ctx* c, int level, const double* coarse_dev, double* fine_dev);   /* :521-590 */
+tp_status tp_smooth(tp_ctx* c, int level, int nswp, double omega, const double* b_dev,
+                    double* u_dev);                                       /* stencil_solvers.c:11-122 */
+tp_status tp_coarse_solve(tp_ctx* c, const double* rhs_dev, double* x_dev); /* stencil_assembly.c:439-503 */
+tp_status tp_vcycle(tp_ctx* c, const double* r_dev, double* z_dev);       /* stencil_solvers.c:129-252 */
+
+/* PCG solve of K(xPhys) U = F, warm-started from U (stencil_solvers.c:259-397).
+ * Assembles the operators first. */
+tp_status tp_solve(tp_ctx* c, int* iters, double* relres);
+/* The same solve for an arbitrary right-hand side (an adjoint solve). */
+tp_status tp_solve_rhs(tp_ctx* c, const double* rhs_dev, double* sol_dev, int* iters, double* relres);
+
+/* Compliance c = sum E(xPhys_e) u_e^T KE u_e and dc/dxPhys
+ * (stencil_methods.c:808-862) for the context's U, into TP_FIELD_DC. */
+tp_status tp_compliance(tp_ctx* c, double* c_out);
+/* General adjoint sensitivity: out_e = -3 (E0-Emin) xPhys_e^2 w_e^T KE u_e. */
+tp_status tp_element_sensitivity(tp_ctx* c, const double* u_dev, const double* w_dev, double* out_dev);
+
+/* Density filter xPhys = (H x)/Hs and its adjoint v <- H (v/Hs)
+ * (stencil_optimization.c:228-395). */
+tp_status tp_filter(tp_ctx* c, const double* in_dev, double* out_dev);
+tp_status tp_filter_T(tp_ctx* c, double* v_dev);
+tp_status tp_volume(tp_ctx* c, double* vol);   /* sum of xPhys / nelem (gpu_definitions.c:94-108) */
+/* OC bisection update from x, dc, dv with constraint value g
+ * (gpu_definitions.c:127-157), then change = max|x - xnew| and x <- xnew
+ * (:110-125). */
+tp_status tp_oc_update(tp_ctx* c, double g, double* change);
+
+/* One design iteration of the loop at stencil_optimization.c:148-189, and the
+ * whole loop from x = xPhys = volfrac (:97-189). The loop stops when
+ * change <= 1e-2 or after max_iterations. hist may be NULL. */
+tp_status tp_init_design(tp_ctx* c);
+tp_status tp_design_iteration(tp_ctx* c, tp_iter_info* info);
+tp_status tp_run(tp_ctx* c, int max_iterations, tp_iter_info* hist, int* loops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -72,6 +72,8 @@ class Oracle:
             L.or_restrict.argtypes = [V, ctypes.c_int, _D, _D]
             L.or_prolong.argtypes = [V, ctypes.c_int, _D, _D]
             L.or_smooth.argtypes = [V, ctypes.c_int, _D, ctypes.c_int, ctypes.c_double, _D, _D, _D, _D]
+            L.or_coarse_direct.restype = ctypes.c_int
+            L.or_coarse_direct.argtypes = [V, ctypes.c_int, _D, _D, _D]
             L.or_solve.restype = ctypes.c_int
             L.or_solve.argtypes = [V, _D, _D, _D, ctypes.c_int, ctypes.c_double, _I, _D]
             L.or_compliance.restype = ctypes.c_double
@@ -154,6 +156,12 @@ class Oracle:
         self.L.or_smooth(self.h, l, _p(np.ascontiguousarray(x, np.float64)), nswp, omega, _p(invD),
                          _p(np.ascontiguousarray(b, np.float64)), _p(u), _p(tmp))
         return u
+
+    def coarse_direct(self, l, x, rhs):
+        sol = np.zeros(self.ndof(l))
+        st = self.L.or_coarse_direct(self.h, l, _p(np.ascontiguousarray(x, np.float64)),
+                                     _p(np.ascontiguousarray(rhs, np.float64)), _p(sol))
+        return sol, st
 
     def solve(self, x, b, u0=None, nswp=4, tol=float(np.float32(1e-5))):
         u = np.zeros(self.ndof()) if u0 is None else np.array(u0, np.float64)

@@ -487,6 +487,15 @@ void or_coarse_free(OrCoarse *cs) {
   cs->band = NULL;
 }
 
+/* factor + solve in one call, for checks of the coarse direct solve */
+int or_coarse_direct(const OrGrid *g, int l, const double *x, const double *rhs, double *sol) {
+  OrCoarse cs;
+  const int st = or_coarse_factor(g, l, x, &cs);
+  or_coarse_solve(&cs, rhs, sol);
+  or_coarse_free(&cs);
+  return st;
+}
+
 /* ------------------------------------------------------------------------ */
 /* V-cycle (stencil_solvers.c:129-252) and PCG (:259-397) */
 typedef struct {

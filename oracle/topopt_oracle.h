@@ -67,6 +67,7 @@ typedef struct {
 int or_coarse_factor(const OrGrid *g, int l, const double *x, OrCoarse *cs);
 void or_coarse_solve(const OrCoarse *cs, const double *rhs, double *sol);
 void or_coarse_free(OrCoarse *cs);
+int or_coarse_direct(const OrGrid *g, int l, const double *x, const double *rhs, double *sol);
 
 int or_solve(const OrGrid *g, const double *x, const double *b, double *u,
              int nswp, double tol, int *iters, double *relres);

@@ -1,0 +1,173 @@
+// Internal declarations of libtopopt_gb300 (not part of the public C ABI).
+//
+// Device layout (every vector, every level): canonical, unpadded, AoS.
+//   level l: ex = nelx >> l elements in x (ey, ez likewise), nx = ex + 1 nodes;
+//   node (i, k, j) -> n = (i*nz + k)*ny + j, DOFs 3n + {0,1,2} (x, y, z);
+//   fine element (i, k, j) -> (i*nelz + k)*nely + j.
+// This is the reference's ordering (stencil_utility.h:19-52) with its halo
+// and its y-padding to multiples of 128 (gpu_definitions.c:67-92) removed;
+// the reference-layout entry points convert at the boundary.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+
+#include "topopt_gb300.h"
+
+#define TP_MAXL 8
+
+namespace tp {
+
+struct Level {
+  int ex, ey, ez;     // elements
+  int nx, ny, nz;     // nodes
+  long nnodes, ndof;
+  int lim;            // fixed strip width: nodes j < lim or j >= ny - lim on the x=0 face
+  long nfixed;        // fixed DOFs
+};
+
+Level make_level(int nelx, int nely, int nelz, int l);
+
+// Host set-up (tp_setup.cpp)
+void element_matrix_tables(double nu, int l, double* KE);   // 576 * ncell^3
+void cantilever_load(const Level& L0, double* F);            // 3*nnodes
+
+// Reduction scratch: partial sums of one pass, one slot per block.
+constexpr int kRedSlots = 4096;
+
+// Scalars the CG keeps on the device (indices into ctx->d_scal).
+enum Scalar {
+  S_RHO = 0, S_RHOOLD, S_ALPHA, S_BETA, S_DPR, S_RNORM2, S_BNORM2, S_RELRES,
+  S_C, S_VOL, S_CHANGE, S_L1, S_L2, S_LMID, S_GT, S_OCDONE, S_TMP0, S_TMP1,
+  S_COUNT
+};
+
+// The coarsest-level direct solver: band Cholesky in FP64 (tp_cholesky.cu).
+struct Coarse {
+  long n = 0, bw = 0;           // order, half bandwidth
+  double* band = nullptr;       // L(r,c) at c*bw + r, 0 <= r - c <= bw (column-major, ld = bw)
+  size_t band_elems = 0;
+  int nbs = 0, nblk = 0;        // solve block size and count
+  double* dinv = nullptr;       // inverse of each diagonal block of L, nbs*nbs per block (column-major)
+  double* vec = nullptr;        // work vector (n)
+  int* info = nullptr;          // device status: first non-positive pivot + 1, 0 if none
+};
+
+}  // namespace tp
+
+struct tp_ctx {
+  tp_params p;
+  int nl;
+  tp::Level L[TP_MAXL];
+  cudaStream_t s = nullptr;
+  int device = 0;
+  std::string err;
+
+  // element stiffness tables per level (576 * ncell^3), FP64 and FP32 copies
+  double* d_ke[TP_MAXL] = {};
+  float* d_kef[TP_MAXL] = {};
+
+  // design fields (fine elements), FP64
+  double *d_x = nullptr, *d_xphys = nullptr, *d_xnew = nullptr, *d_dc = nullptr,
+         *d_dv = nullptr, *d_hs = nullptr;
+  double* d_E = nullptr;  // E(xPhys) per fine element
+  float* d_Ef = nullptr;
+
+  // state: load and displacement (FP64), nrhs columns, column-contiguous
+  double *d_F = nullptr, *d_U = nullptr;
+
+  // CG vectors (FP64)
+  double *d_r = nullptr, *d_z = nullptr, *d_p = nullptr, *d_q = nullptr;
+
+  // multigrid vectors per level, in the V-cycle precision
+  // (FP64 form: the double set; mixed form: the float set)
+  double *mg_r[TP_MAXL] = {}, *mg_z[TP_MAXL] = {}, *mg_d[TP_MAXL] = {}, *mg_t[TP_MAXL] = {};
+  float *mgf_r[TP_MAXL] = {}, *mgf_z[TP_MAXL] = {}, *mgf_d[TP_MAXL] = {}, *mgf_t[TP_MAXL] = {};
+  double* invD[TP_MAXL] = {};
+  float* invDf[TP_MAXL] = {};
+
+  // assembled 27-point block stencils of levels 1 .. nl-1 (243 coefficients
+  // per node, coefficient-major: A[(nb*9 + c*3 + d)*nnodes + n])
+  double* st[TP_MAXL] = {};
+  float* stf[TP_MAXL] = {};
+
+  tp::Coarse coarse;
+
+  // reductions
+  double* d_red = nullptr;   // kRedSlots partials
+  double* d_scal = nullptr;  // S_COUNT scalars
+  double* h_scal = nullptr;  // pinned mirror
+  int* d_flag = nullptr;     // device error flag (bounded waits)
+
+  bool assembled = false;    // operators built for the current xPhys
+  long mem_bytes = 0;
+};
+
+namespace tp {
+
+// kernels (tp_kernels_*.cu); every launcher enqueues on ctx->s
+void set_fine_ke(const double* ke0_host);  // __constant__ copies (FP64 + FP32)
+
+void compute_E(tp_ctx* c);  // d_E, d_Ef from d_xphys
+int fine_blocks(const tp_ctx* c);
+
+// level 0 (matrix-free hex8 stencil)
+template <typename T> void fine_apply(tp_ctx* c, const T* E, const T* in, T* out);
+template <typename T> void fine_apply_dot(tp_ctx* c, const T* E, const T* in, T* out);  // + <in,out> partials
+template <typename T> void fine_jacobi(tp_ctx* c, const T* E, const T* invD, const T* b, const T* u, T* unew, T omega);
+template <typename T> void fine_resid(tp_ctx* c, const T* E, const T* b, const T* u, T* d);
+void fine_inv_diag(tp_ctx* c, double* invD);
+
+// levels >= 1 (assembled block stencils)
+template <typename T> void assemble_stencil(tp_ctx* c, int l, const T* E, const T* ke, T* st, double* invD);
+template <typename T> void stencil_apply(tp_ctx* c, int l, const T* st, const T* in, T* out);
+template <typename T> void stencil_jacobi(tp_ctx* c, int l, const T* st, const T* invD, const T* b, const T* u, T* unew, T omega);
+template <typename T> void stencil_resid(tp_ctx* c, int l, const T* st, const T* b, const T* u, T* d);
+
+// grid transfer
+template <typename T> void restrict_fw(tp_ctx* c, int l, const T* fine, T* coarse);
+template <typename T> void prolong_add(tp_ctx* c, int l, const T* coarse, T* fine);
+template <typename T> void prolong_set(tp_ctx* c, int l, const T* coarse, T* fine);
+
+// vectors
+template <typename T> void vscale(tp_ctx* c, long n, const T* a, const T* b, T* out, T omega);  // out = omega*a*b
+void dot_partials(tp_ctx* c, long n, const double* a, const double* b, int* nblocks);
+void finish_sum(tp_ctx* c, int nblocks, int slot, int op);  // sum partials into d_scal[slot]
+void cast_d2f(tp_ctx* c, long n, const double* a, float* b);
+void cast_f2d(tp_ctx* c, long n, const float* a, double* b);
+void cg_pupdate(tp_ctx* c, long n, const double* z, double* p, int first);
+void cg_xr_update(tp_ctx* c, long n, double* u, double* r, const double* p, const double* q, int* nblocks);
+void cg_scalars(tp_ctx* c, int what);
+
+// coarsest level (tp_cholesky.cu)
+void coarse_alloc(tp_ctx* c);
+void coarse_free(tp_ctx* c);
+void coarse_assemble(tp_ctx* c);  // from the FP64 stencil of level nl-1
+void coarse_factor(tp_ctx* c);
+void coarse_solve(tp_ctx* c, const double* rhs, double* x);
+
+// design-variable ops (tp_kernels_design.cu)
+void compliance(tp_ctx* c, const double* u, double* dc, int* nblocks);
+void filter_hs(tp_ctx* c, double* hs);
+void filter_fwd(tp_ctx* c, const double* x, double* out);
+void filter_adj(tp_ctx* c, double* v, double* tmp);
+void volume_partials(tp_ctx* c, const double* xphys, int* nblocks);
+int oc_update(tp_ctx* c, double g);   // bisection; leaves xnew, change and x <- xnew
+void element_sens(tp_ctx* c, const double* u, const double* w, double* out);
+int filter_fwd_blocks(const tp_ctx* c);
+void set_design_ke(const double* ke0_host);
+
+// error helpers
+bool cuda_ok(tp_ctx* c, cudaError_t e, const char* what);
+int grid_for(long n, int threads);
+
+}  // namespace tp
+
+#define TP_CHECK_LAUNCH(c, what)                                   \
+  do {                                                             \
+    cudaError_t _e = cudaGetLastError();                           \
+    if (_e != cudaSuccess) {                                       \
+      (c)->err = std::string(what) + ": " + cudaGetErrorString(_e); \
+    }                                                              \
+  } while (0)

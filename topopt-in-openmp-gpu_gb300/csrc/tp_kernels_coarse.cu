@@ -1,0 +1,265 @@
+// Levels >= 1: assembled 27-point block stencils, and the grid transfers.
+//
+// The reference applies level 1 matrix-free, summing for every coarse
+// element the E(rho)-weighted stiffness of its ncell^3 fine sub-cells
+// (stencil_methods.c:436-519), and assembles levels >= 2 into CSR on the
+// host (stencil_assembly.c:126-260). Here every level >= 1 is assembled once
+// per design iteration on the GPU into a block stencil: for each node, the
+// 3x3 coupling blocks to its 27 neighbours. The operator semantics of the
+// reference are kept exactly:
+//   level 1      : free rows couple to every neighbour, fixed rows = identity
+//                  (the matrix-free subspace operator);
+//   level >= 2   : additionally the columns of fixed DOFs are zeroed (the CSR
+//                  with BC rows/columns zeroed and a unit diagonal).
+// The Jacobi diagonal comes from the unmodified sum, 1 at fixed DOFs, as
+// assembleInvertedMatrixDiagonalSubspace_halo does for every level.
+#include "tp_internal.h"
+
+namespace tp {
+
+__host__ __device__ constexpr int cloc(int dx, int dy, int dz) {
+  return dz * 4 + (dy ? (dx ? 1 : 0) : (dx ? 2 : 3));
+}
+
+struct CGeom {
+  int nx, ny, nz, ex, ey, ez, lim;
+  int ncell, lg2;  // fine sub-cells per coarse element edge
+  int fex, fey, fez;  // fine elements
+  long nnodes;
+};
+
+static CGeom cgeom(const tp_ctx* c, int l) {
+  const Level& L = c->L[l];
+  const Level& F = c->L[0];
+  return CGeom{L.nx, L.ny, L.nz, L.ex, L.ey, L.ez, L.lim, 1 << l, l, F.ex, F.ey, F.ez, L.nnodes};
+}
+
+__device__ __forceinline__ bool is_fixed(const CGeom& g, int i, int j) {
+  return i == 0 && (j < g.lim || j >= g.ny - g.lim);
+}
+
+// G lanes cooperate on one node; each lane sums a strided share of the
+// ncell^3 sub-cells, then the lanes reduce by shuffles.
+template <typename T, int G>
+__global__ void assemble_kernel(CGeom g, const T* __restrict__ E, const T* __restrict__ ke,
+                                T* __restrict__ st, double* __restrict__ invD, int masked) {
+  const long tid = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long n = tid / G;
+  const int lane = threadIdx.x % G;
+  if (n >= g.nnodes) return;  // G divides the block size: whole groups leave together
+  const int j = n % g.ny;
+  const int k = (n / g.ny) % g.nz;
+  const int i = n / ((long)g.ny * g.nz);
+  const int nc = g.ncell, nsub = nc * nc * nc;
+  const bool nfix = is_fixed(g, i, j);
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) / G * G));
+
+  for (int m = 0; m < 27; m++) {
+    const int mx = m / 9 - 1, mz = (m / 3) % 3 - 1, my = m % 3 - 1;
+    T acc[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) acc[q] = T(0);
+    const int mi = i + mx, mk = k + mz, mj = j + my;
+    const bool minside = mi >= 0 && mi < g.nx && mk >= 0 && mk < g.nz && mj >= 0 && mj < g.ny;
+    if (minside) {
+#pragma unroll
+      for (int e = 0; e < 8; e++) {
+        const int ex = -(e & 1), ez = -((e >> 1) & 1), ey = -((e >> 2) & 1);
+        const int rx = mx - ex, ry = my - ey, rz = mz - ez;
+        if (rx < 0 || rx > 1 || ry < 0 || ry > 1 || rz < 0 || rz > 1) continue;
+        const int ci = i + ex, ck = k + ez, cj = j + ey;
+        if (ci < 0 || ci >= g.ex || ck < 0 || ck >= g.ez || cj < 0 || cj >= g.ey) continue;
+        const int qn = cloc(-ex, -ey, -ez), qm = cloc(rx, ry, rz);
+        for (int s = lane; s < nsub; s += G) {
+          const int ii = s >> (2 * g.lg2), kk = (s >> g.lg2) & (nc - 1), jj = s & (nc - 1);
+          const long fe = ((long)(ci * nc + ii) * g.fez + (ck * nc + kk)) * g.fey + (cj * nc + jj);
+          const T Es = E[fe];
+          const T* K = ke + (long)s * 576 + (3 * qn) * 24 + 3 * qm;
+#pragma unroll
+          for (int c = 0; c < 3; c++)
+#pragma unroll
+            for (int d = 0; d < 3; d++) acc[3 * c + d] += Es * K[24 * c + d];
+        }
+      }
+    }
+    if (G > 1) {
+#pragma unroll
+      for (int q = 0; q < 9; q++)
+        for (int o = G / 2; o > 0; o >>= 1) acc[q] += __shfl_down_sync(gmask, acc[q], o, G);
+    }
+    if (lane == 0) {
+      if (m == 13) {  // the node itself: Jacobi diagonal before BCs
+        for (int c = 0; c < 3; c++) invD[3 * n + c] = nfix ? 1.0 : 1.0 / (double)acc[4 * c];
+      }
+      bool zero = !minside;
+      if (nfix) zero = true;
+      if (masked && minside && is_fixed(g, mi, mj)) zero = true;
+#pragma unroll
+      for (int q = 0; q < 9; q++) {
+        T v = zero ? T(0) : acc[q];
+        if (nfix && m == 13 && (q % 4 == 0)) v = T(1);
+        st[(long)(m * 9 + q) * g.nnodes + n] = v;
+      }
+    }
+  }
+}
+
+template <typename T>
+void assemble_stencil(tp_ctx* c, int l, const T* E, const T* ke, T* st, double* invD) {
+  const CGeom g = cgeom(c, l);
+  const int masked = l >= 2;
+  const int nsub = g.ncell * g.ncell * g.ncell;
+  const int threads = 256;
+  if (nsub >= 32) {
+    assemble_kernel<T, 32><<<grid_for(g.nnodes * 32, threads), threads, 0, c->s>>>(g, E, ke, st, invD, masked);
+  } else if (nsub >= 8) {
+    assemble_kernel<T, 8><<<grid_for(g.nnodes * 8, threads), threads, 0, c->s>>>(g, E, ke, st, invD, masked);
+  } else {
+    assemble_kernel<T, 1><<<grid_for(g.nnodes, threads), threads, 0, c->s>>>(g, E, ke, st, invD, masked);
+  }
+  TP_CHECK_LAUNCH(c, "assemble_stencil");
+}
+template void assemble_stencil<double>(tp_ctx*, int, const double*, const double*, double*, double*);
+template void assemble_stencil<float>(tp_ctx*, int, const float*, const float*, float*, double*);
+
+enum { S_APPLY = 0, S_JACOBI = 1, S_RESID = 2 };
+
+template <typename T, int MODE>
+__global__ void stencil_kernel(CGeom g, const T* __restrict__ st, const T* __restrict__ in,
+                               T* __restrict__ out, const T* __restrict__ b,
+                               const T* __restrict__ invD, T omega) {
+  const long n = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (n >= g.nnodes) return;
+  const int j = n % g.ny;
+  const int k = (n / g.ny) % g.nz;
+  const int i = n / ((long)g.ny * g.nz);
+  T y[3] = {T(0), T(0), T(0)};
+#pragma unroll
+  for (int m = 0; m < 27; m++) {
+    const int mx = m / 9 - 1, mz = (m / 3) % 3 - 1, my = m % 3 - 1;
+    const int mi = i + mx, mk = k + mz, mj = j + my;
+    if (mi < 0 || mi >= g.nx || mk < 0 || mk >= g.nz || mj < 0 || mj >= g.ny) continue;
+    const long nm = ((long)mi * g.nz + mk) * g.ny + mj;
+    const T u0 = in[3 * nm], u1 = in[3 * nm + 1], u2 = in[3 * nm + 2];
+    const T* A = st + (long)m * 9 * g.nnodes + n;
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+      y[c] += A[(3 * c) * g.nnodes] * u0 + A[(3 * c + 1) * g.nnodes] * u1 + A[(3 * c + 2) * g.nnodes] * u2;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    if (MODE == S_APPLY) out[3 * n + c] = y[c];
+    if (MODE == S_JACOBI) out[3 * n + c] = in[3 * n + c] + omega * invD[3 * n + c] * (b[3 * n + c] - y[c]);
+    if (MODE == S_RESID) out[3 * n + c] = b[3 * n + c] - y[c];
+  }
+}
+
+template <typename T>
+void stencil_apply(tp_ctx* c, int l, const T* st, const T* in, T* out) {
+  const CGeom g = cgeom(c, l);
+  stencil_kernel<T, S_APPLY><<<grid_for(g.nnodes, 128), 128, 0, c->s>>>(g, st, in, out, nullptr, nullptr, T(0));
+  TP_CHECK_LAUNCH(c, "stencil_apply");
+}
+template <typename T>
+void stencil_jacobi(tp_ctx* c, int l, const T* st, const T* invD, const T* b, const T* u, T* unew, T omega) {
+  const CGeom g = cgeom(c, l);
+  stencil_kernel<T, S_JACOBI><<<grid_for(g.nnodes, 128), 128, 0, c->s>>>(g, st, u, unew, b, invD, omega);
+  TP_CHECK_LAUNCH(c, "stencil_jacobi");
+}
+template <typename T>
+void stencil_resid(tp_ctx* c, int l, const T* st, const T* b, const T* u, T* d) {
+  const CGeom g = cgeom(c, l);
+  stencil_kernel<T, S_RESID><<<grid_for(g.nnodes, 128), 128, 0, c->s>>>(g, st, u, d, b, nullptr, T(0));
+  TP_CHECK_LAUNCH(c, "stencil_resid");
+}
+template void stencil_apply<double>(tp_ctx*, int, const double*, const double*, double*);
+template void stencil_apply<float>(tp_ctx*, int, const float*, const float*, float*);
+template void stencil_jacobi<double>(tp_ctx*, int, const double*, const double*, const double*, const double*, double*, double);
+template void stencil_jacobi<float>(tp_ctx*, int, const float*, const float*, const float*, const float*, float*, float);
+template void stencil_resid<double>(tp_ctx*, int, const double*, const double*, const double*, double*);
+template void stencil_resid<float>(tp_ctx*, int, const float*, const float*, const float*, float*);
+
+// ---------------------------------------------------------------------------
+// Full-weighting restriction, level l+1 <- level l (stencil_methods.c:595-688):
+// the coarse node at fine (2i, 2j, 2k) gathers its 27 fine neighbours with
+// weights 1, 1/2, 1/4, 1/8 by squared distance, in the reference's x, z, y
+// loop order.
+template <typename T>
+__global__ void restrict_kernel(CGeom f, CGeom cg, const T* __restrict__ fine, T* __restrict__ coarse) {
+  const long n = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (n >= cg.nnodes) return;
+  const int jc = n % cg.ny;
+  const int kc = (n / cg.ny) % cg.nz;
+  const int ic = n / ((long)cg.ny * cg.nz);
+  const int i1 = 2 * ic, j1 = 2 * jc, k1 = 2 * kc;
+  T acc[3] = {T(0), T(0), T(0)};
+  for (int i = i1 - 1; i < i1 + 2; i++)
+    for (int k = k1 - 1; k < k1 + 2; k++)
+      for (int j = j1 - 1; j < j1 + 2; j++) {
+        if (i < 0 || i >= f.nx || j < 0 || j >= f.ny || k < 0 || k >= f.nz) continue;
+        const int d2 = (i1 - i) * (i1 - i) + (j1 - j) * (j1 - j) + (k1 - k) * (k1 - k);
+        const T w = d2 == 0 ? T(1.0) : d2 == 1 ? T(0.5) : d2 == 2 ? T(0.25) : T(0.125);
+        const long nf = ((long)i * f.nz + k) * f.ny + j;
+        acc[0] += w * fine[3 * nf];
+        acc[1] += w * fine[3 * nf + 1];
+        acc[2] += w * fine[3 * nf + 2];
+      }
+  coarse[3 * n] = acc[0];
+  coarse[3 * n + 1] = acc[1];
+  coarse[3 * n + 2] = acc[2];
+}
+
+// Trilinear prolongation, level l <- level l+1 (stencil_methods.c:521-590):
+// each fine node averages the (possibly repeated) 8 coarse nodes
+// (i>>1 | (i+1)>>1) x (j>>1 | (j+1)>>1) x (k>>1 | (k+1)>>1) with weight 1/8,
+// summed in the reference's order. ADD adds the result to the fine vector.
+template <typename T, bool ADD>
+__global__ void prolong_kernel(CGeom f, CGeom cg, const T* __restrict__ coarse, T* __restrict__ fine) {
+  const long n = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (n >= f.nnodes) return;
+  const int j = n % f.ny;
+  const int k = (n / f.ny) % f.nz;
+  const int i = n / ((long)f.ny * f.nz);
+  const int i1 = i >> 1, i2 = (i + 1) >> 1, j1 = j >> 1, j2 = (j + 1) >> 1, k1 = k >> 1, k2 = (k + 1) >> 1;
+  auto cn = [&](int a, int b, int d) { return ((long)a * cg.nz + b) * cg.ny + d; };
+  const long c1 = cn(i1, k1, j2), c2 = cn(i2, k1, j2), c3 = cn(i2, k1, j1), c4 = cn(i1, k1, j1),
+             c5 = cn(i1, k2, j2), c6 = cn(i2, k2, j2), c7 = cn(i2, k2, j1), c8 = cn(i1, k2, j1);
+  const T h = T(0.125);
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const T v = h * coarse[3 * c1 + c] + h * coarse[3 * c2 + c] + h * coarse[3 * c3 + c] +
+                h * coarse[3 * c4 + c] + h * coarse[3 * c5 + c] + h * coarse[3 * c6 + c] +
+                h * coarse[3 * c7 + c] + h * coarse[3 * c8 + c];
+    if (ADD)
+      fine[3 * n + c] += v;
+    else
+      fine[3 * n + c] = v;
+  }
+}
+
+template <typename T>
+void restrict_fw(tp_ctx* c, int l, const T* fine, T* coarse) {
+  const CGeom f = cgeom(c, l), cg = cgeom(c, l + 1);
+  restrict_kernel<T><<<grid_for(cg.nnodes, 128), 128, 0, c->s>>>(f, cg, fine, coarse);
+  TP_CHECK_LAUNCH(c, "restrict");
+}
+template <typename T>
+void prolong_add(tp_ctx* c, int l, const T* coarse, T* fine) {
+  const CGeom f = cgeom(c, l), cg = cgeom(c, l + 1);
+  prolong_kernel<T, true><<<grid_for(f.nnodes, 128), 128, 0, c->s>>>(f, cg, coarse, fine);
+  TP_CHECK_LAUNCH(c, "prolong_add");
+}
+template <typename T>
+void prolong_set(tp_ctx* c, int l, const T* coarse, T* fine) {
+  const CGeom f = cgeom(c, l), cg = cgeom(c, l + 1);
+  prolong_kernel<T, false><<<grid_for(f.nnodes, 128), 128, 0, c->s>>>(f, cg, coarse, fine);
+  TP_CHECK_LAUNCH(c, "prolong_set");
+}
+template void restrict_fw<double>(tp_ctx*, int, const double*, double*);
+template void restrict_fw<float>(tp_ctx*, int, const float*, float*);
+template void prolong_add<double>(tp_ctx*, int, const double*, double*);
+template void prolong_add<float>(tp_ctx*, int, const float*, float*);
+template void prolong_set<double>(tp_ctx*, int, const double*, double*);
+template void prolong_set<float>(tp_ctx*, int, const float*, float*);
+
+}  // namespace tp

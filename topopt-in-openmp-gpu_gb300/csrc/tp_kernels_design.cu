@@ -1,0 +1,326 @@
+// Design-variable operations of the loop at stencil_optimization.c:148-189:
+// compliance and sensitivity (stencil_methods.c:808-862), the density filter
+// and its adjoint (stencil_optimization.c:228-395), the volume
+// (gpu_definitions.c:94-108) and the OC bisection with the change measure
+// (gpu_definitions.c:110-157). All FP64, all reductions two-pass and
+// order-fixed.
+#include <cmath>
+
+#include "tp_internal.h"
+
+namespace tp {
+
+__constant__ double c_ke0_design[576];
+
+void set_design_ke(const double* ke0) { cudaMemcpyToSymbol(c_ke0_design, ke0, sizeof(double) * 576); }
+
+__host__ __device__ constexpr int dloc_dx(int q) { return (q == 1 || q == 2 || q == 5 || q == 6) ? 1 : 0; }
+__host__ __device__ constexpr int dloc_dy(int q) { return (q == 0 || q == 1 || q == 4 || q == 5) ? 1 : 0; }
+__host__ __device__ constexpr int dloc_dz(int q) { return q >= 4 ? 1 : 0; }
+
+__device__ __forceinline__ double bsum256(double v) {
+  __shared__ double sh[8];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < 8; w++) s += sh[w];
+  __syncthreads();
+  return s;
+}
+__device__ __forceinline__ double bmax256(double v) {
+  __shared__ double sh[8];
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < 8; w++) s = fmax(s, sh[w]);
+  __syncthreads();
+  return s;
+}
+
+struct DGeom {
+  int ex, ey, ez, nx, ny, nz;
+};
+static DGeom dgeom(const tp_ctx* c) {
+  const Level& L = c->L[0];
+  return DGeom{L.ex, L.ey, L.ez, L.nx, L.ny, L.nz};
+}
+
+constexpr int kMaxBlocks = 4096;
+
+// out_e = -3 (E0-Emin) x_e^2 w_e^T KE u_e (penalty 3, stencil_methods.c:855-858);
+// with w = u, also the compliance partials sum_e E_e u_e^T KE u_e.
+template <bool COMPLIANCE>
+__global__ void sens_kernel(DGeom g, const double* __restrict__ x, const double* __restrict__ u,
+                            const double* __restrict__ w, double* __restrict__ out,
+                            double* __restrict__ partials) {
+  const long ne = (long)g.ex * g.ey * g.ez;
+  const double Ed = 1.0 - 1e-6;
+  double csum = 0.0;
+  for (long e = blockIdx.x * 256L + threadIdx.x; e < ne; e += (long)gridDim.x * 256) {
+    const int j = e % g.ey;
+    const int k = (e / g.ey) % g.ez;
+    const int i = e / ((long)g.ey * g.ez);
+    double ue[24], we[24];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const long n = ((long)(i + dloc_dx(q)) * g.nz + (k + dloc_dz(q))) * g.ny + (j + dloc_dy(q));
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        ue[3 * q + c] = u[3 * n + c];
+        we[3 * q + c] = COMPLIANCE ? ue[3 * q + c] : w[3 * n + c];
+      }
+    }
+    const double xe = x[e];
+    double d = 0.0;
+#pragma unroll
+    for (int ii = 0; ii < 8; ii++) {
+      double cl = 0.0;
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        double t = 0.0;
+#pragma unroll
+        for (int b = 0; b < 24; b++) t += c_ke0_design[(ii * 3 + a) * 24 + b] * ue[b];
+        cl += we[3 * ii + a] * t;
+      }
+      if (COMPLIANCE) csum += cl * (1e-6 + xe * xe * xe * Ed);
+      d += cl * (-3.0 * Ed * xe * xe);
+    }
+    out[e] = d;
+  }
+  if (COMPLIANCE) {
+    const double s = bsum256(csum);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+  }
+}
+
+static int blocks_for(long n) {
+  long b = (n + 255) / 256;
+  if (b > kMaxBlocks) b = kMaxBlocks;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+void compliance(tp_ctx* c, const double* u, double* dc, int* nblocks) {
+  const DGeom g = dgeom(c);
+  const long ne = (long)g.ex * g.ey * g.ez;
+  const int nb = blocks_for(ne);
+  sens_kernel<true><<<nb, 256, 0, c->s>>>(g, c->d_xphys, u, nullptr, dc, c->d_red);
+  TP_CHECK_LAUNCH(c, "compliance");
+  *nblocks = nb;
+}
+
+void element_sens(tp_ctx* c, const double* u, const double* w, double* out) {
+  const DGeom g = dgeom(c);
+  const long ne = (long)g.ex * g.ey * g.ez;
+  sens_kernel<false><<<blocks_for(ne), 256, 0, c->s>>>(g, c->d_xphys, u, w, out, nullptr);
+  TP_CHECK_LAUNCH(c, "element_sens");
+}
+
+// ----------------------------------------------------------------------------
+// Filter neighbourhood: [i-(ceil(rmin)-1), i+ceil(rmin)] clipped to the grid
+// (stencil_optimization.c:254-269), weights max(0, rmin - |d|), loops in the
+// reference's x, z, y order.
+struct FBox {
+  int cr;       // ceil(rmin)
+  double rmin;
+};
+
+__device__ __forceinline__ void box(int i, int n, int cr, int& lo, int& hi) {
+  lo = max(i - (cr - 1), 0);
+  hi = min(i + cr + 1, n);
+}
+
+template <int MODE>  // 0: Hs, 1: forward H x / Hs, 2: adjoint H (v) with v already / Hs
+__global__ void filter_kernel(DGeom g, FBox fb, const double* __restrict__ in, const double* __restrict__ hs,
+                              double* __restrict__ out, double* __restrict__ partials) {
+  const long ne = (long)g.ex * g.ey * g.ez;
+  double vsum = 0.0;
+  for (long e = blockIdx.x * 256L + threadIdx.x; e < ne; e += (long)gridDim.x * 256) {
+    const int j = e % g.ey;
+    const int k = (e / g.ey) % g.ez;
+    const int i = e / ((long)g.ey * g.ez);
+    int i0, i1, k0, k1, j0, j1;
+    box(i, g.ex, fb.cr, i0, i1);
+    box(k, g.ez, fb.cr, k0, k1);
+    box(j, g.ey, fb.cr, j0, j1);
+    double o = 0.0, h = 0.0;
+    for (int i2 = i0; i2 < i1; i2++)
+      for (int k2 = k0; k2 < k1; k2++)
+        for (int j2 = j0; j2 < j1; j2++) {
+          const unsigned d2 = (unsigned)((i - i2) * (i - i2) + (j - j2) * (j - j2) + (k - k2) * (k - k2));
+          const double wgt = fmax(0.0, fb.rmin - sqrt((double)d2));
+          if (MODE == 0) h += wgt;
+          if (MODE != 0) o += wgt * in[((long)i2 * g.ez + k2) * g.ey + j2];
+        }
+    if (MODE == 0) out[e] = h;
+    if (MODE == 1) {
+      const double v = o / hs[e];
+      out[e] = v;
+      vsum += v;
+    }
+    if (MODE == 2) out[e] = o;
+  }
+  if (MODE == 1) {
+    const double s = bsum256(vsum);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+  }
+}
+
+__global__ void div_kernel(long n, const double* __restrict__ v, const double* __restrict__ hs, double* __restrict__ t) {
+  const long e = blockIdx.x * 256L + threadIdx.x;
+  if (e < n) t[e] = v[e] / hs[e];
+}
+
+static FBox fbox(const tp_ctx* c) { return FBox{(int)std::ceil(c->p.rmin), c->p.rmin}; }
+
+void filter_hs(tp_ctx* c, double* hs) {
+  const DGeom g = dgeom(c);
+  filter_kernel<0><<<blocks_for((long)g.ex * g.ey * g.ez), 256, 0, c->s>>>(g, fbox(c), nullptr, nullptr, hs, nullptr);
+  TP_CHECK_LAUNCH(c, "filter_hs");
+}
+
+// forward filter; leaves sum(out) partials for the volume in d_red
+int filter_fwd_blocks(const tp_ctx* c) {
+  const DGeom g = dgeom(c);
+  return blocks_for((long)g.ex * g.ey * g.ez);
+}
+void filter_fwd(tp_ctx* c, const double* x, double* out) {
+  const DGeom g = dgeom(c);
+  filter_kernel<1><<<filter_fwd_blocks(c), 256, 0, c->s>>>(g, fbox(c), x, c->d_hs, out, c->d_red);
+  TP_CHECK_LAUNCH(c, "filter_fwd");
+}
+
+void filter_adj(tp_ctx* c, double* v, double* tmp) {
+  const DGeom g = dgeom(c);
+  const long ne = (long)g.ex * g.ey * g.ez;
+  div_kernel<<<grid_for(ne, 256), 256, 0, c->s>>>(ne, v, c->d_hs, tmp);
+  filter_kernel<2><<<blocks_for(ne), 256, 0, c->s>>>(g, fbox(c), tmp, nullptr, v, nullptr);
+  TP_CHECK_LAUNCH(c, "filter_adj");
+}
+
+__global__ void sum_kernel(long n, const double* __restrict__ v, double* __restrict__ partials) {
+  double s = 0.0;
+  for (long e = blockIdx.x * 256L + threadIdx.x; e < n; e += (long)gridDim.x * 256) s += v[e];
+  s = bsum256(s);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+void volume_partials(tp_ctx* c, const double* xphys, int* nblocks) {
+  const long ne = (long)c->L[0].ex * c->L[0].ey * c->L[0].ez;
+  const int nb = blocks_for(ne);
+  sum_kernel<<<nb, 256, 0, c->s>>>(ne, xphys, c->d_red);
+  TP_CHECK_LAUNCH(c, "volume");
+  *nblocks = nb;
+}
+
+// ----------------------------------------------------------------------------
+// OC: xnew = max(0, max(x - move, min(1, min(x + move, x*sqrt(-dc/(dv*lmid))))))
+// with the reference's MAX/MIN macros (a > b ? a : b), move = 0.2.
+__device__ __forceinline__ double oc_xnew(double x, double dc, double dv, double lmid) {
+  const double move = 0.2;
+  const double xs = x * sqrt(-dc / (dv * lmid));
+  const double a = (x + move > xs) ? xs : x + move;  // MIN(x + move, xs)
+  const double b = (1.0 > a) ? a : 1.0;              // MIN(1.0, a)
+  const double cc = (x - move > b) ? x - move : b;   // MAX(x - move, b)
+  return (0.0 > cc) ? 0.0 : cc;                      // MAX(0.0, cc)
+}
+
+// one bisection step: partial sums of dv*(xnew - x) at lmid = (l1 + l2)/2
+__global__ void oc_step_kernel(long n, const double* __restrict__ x, const double* __restrict__ dc,
+                               const double* __restrict__ dv, double* __restrict__ scal,
+                               double* __restrict__ partials) {
+  if (scal[S_OCDONE] != 0.0) return;
+  const double lmid = 0.5 * (scal[S_L2] + scal[S_L1]);
+  double s = 0.0;
+  for (long e = blockIdx.x * 256L + threadIdx.x; e < n; e += (long)gridDim.x * 256) {
+    const double xn = oc_xnew(x[e], dc[e], dv[e], lmid);
+    s += dv[e] * (xn - x[e]);
+  }
+  s = bsum256(s);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+// gt = sum + g; l1 or l2 <- lmid; done when (l2-l1)/(l1+l2) <= 1e-6
+__global__ void oc_finish_kernel(const double* __restrict__ partials, int nb, double* __restrict__ scal, double g) {
+  if (scal[S_OCDONE] != 0.0) return;
+  __shared__ double sh[256];
+  const int per = (nb + 255) / 256;
+  const int b0 = threadIdx.x * per;
+  double s = 0.0;
+  for (int i = b0; i < b0 + per && i < nb; i++) s += partials[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = sh[0];
+    for (int i = 1; i < 256; i++) t += sh[i];
+    const double l1 = scal[S_L1], l2 = scal[S_L2];
+    const double lmid = 0.5 * (l2 + l1);
+    const double gt = t + g;
+    double nl1 = l1, nl2 = l2;
+    if (gt > 0)
+      nl1 = lmid;
+    else
+      nl2 = lmid;
+    scal[S_L1] = nl1;
+    scal[S_L2] = nl2;
+    scal[S_LMID] = lmid;
+    scal[S_GT] = gt;
+    scal[S_OCDONE] = ((nl2 - nl1) / (nl1 + nl2) > 1e-6) ? 0.0 : 1.0;
+    scal[S_TMP0] += 1.0;  // steps taken
+  }
+}
+
+// final pass at the last lmid: xnew, max |x - xnew| partials, x <- xnew
+__global__ void oc_apply_kernel(long n, double* __restrict__ x, double* __restrict__ xnew,
+                                const double* __restrict__ dc, const double* __restrict__ dv,
+                                const double* __restrict__ scal, double* __restrict__ partials) {
+  const double lmid = scal[S_LMID];
+  double m = 0.0;
+  for (long e = blockIdx.x * 256L + threadIdx.x; e < n; e += (long)gridDim.x * 256) {
+    const double xo = x[e];
+    const double xn = oc_xnew(xo, dc[e], dv[e], lmid);
+    xnew[e] = xn;
+    m = fmax(m, fabs(xo - xn));
+    x[e] = xn;
+  }
+  m = bmax256(m);
+  if (threadIdx.x == 0) partials[blockIdx.x] = m;
+}
+
+__global__ void oc_init_kernel(double* scal) {
+  scal[S_L1] = 0.0;
+  scal[S_L2] = 1e9;
+  scal[S_OCDONE] = ((1e9 - 0.0) / (0.0 + 1e9) > 1e-6) ? 0.0 : 1.0;
+  scal[S_TMP0] = 0.0;
+  scal[S_LMID] = 0.0;
+}
+
+// returns 0 on success; -1 if the bisection did not finish within its cap
+int oc_update(tp_ctx* c, double g) {
+  const long ne = (long)c->L[0].ex * c->L[0].ey * c->L[0].ez;
+  const int nb = blocks_for(ne);
+  oc_init_kernel<<<1, 1, 0, c->s>>>(c->d_scal);
+  const int kBatch = 24, kMaxSteps = 240;
+  int taken = 0;
+  for (;;) {
+    for (int q = 0; q < kBatch; q++) {
+      oc_step_kernel<<<nb, 256, 0, c->s>>>(ne, c->d_x, c->d_dc, c->d_dv, c->d_scal, c->d_red);
+      oc_finish_kernel<<<1, 256, 0, c->s>>>(c->d_red, nb, c->d_scal, g);
+    }
+    taken += kBatch;
+    cudaMemcpyAsync(c->h_scal + S_OCDONE, c->d_scal + S_OCDONE, sizeof(double), cudaMemcpyDeviceToHost, c->s);
+    cudaStreamSynchronize(c->s);
+    if (c->h_scal[S_OCDONE] != 0.0) break;
+    if (taken >= kMaxSteps) return -1;
+  }
+  oc_apply_kernel<<<nb, 256, 0, c->s>>>(ne, c->d_x, c->d_xnew, c->d_dc, c->d_dv, c->d_scal, c->d_red);
+  finish_sum(c, nb, S_CHANGE, 1);
+  TP_CHECK_LAUNCH(c, "oc_update");
+  return 0;
+}
+
+}  // namespace tp

@@ -1,0 +1,290 @@
+"""ctypes binding of libtopopt_gb300 (the C ABI in include/topopt_gb300.h).
+
+This is the host-side harness used by the tests and bench.py. Device arrays
+are torch CUDA tensors (float64 unless a method says otherwise); torch only
+provides the memory. Every call goes through the C ABI into the CUDA
+kernels; if the shared library is missing the constructor raises, there is
+no CPU fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libtopopt_gb300.so")
+
+TP_FP64, TP_MIXED = 0, 1
+FIELDS = {"x": 0, "xphys": 1, "xnew": 2, "dc": 3, "dv": 4, "F": 5, "U": 6}
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "allocation failed",
+          4: "coarse matrix not positive definite", 5: "CG did not converge",
+          6: "non-finite value", 7: "device wait timed out", 8: "call out of order"}
+
+
+class TpParams(ctypes.Structure):
+    _fields_ = [("nelx", ctypes.c_int), ("nely", ctypes.c_int), ("nelz", ctypes.c_int),
+                ("nl", ctypes.c_int), ("volfrac", ctypes.c_double), ("rmin", ctypes.c_double),
+                ("cgtol", ctypes.c_double), ("cgmax", ctypes.c_int), ("nswp", ctypes.c_int),
+                ("omega", ctypes.c_double), ("precision", ctypes.c_int), ("nrhs", ctypes.c_int),
+                ("device", ctypes.c_int)]
+
+
+class TpIterInfo(ctypes.Structure):
+    _fields_ = [("loop", ctypes.c_int), ("c", ctypes.c_double), ("vol", ctypes.c_double),
+                ("change", ctypes.c_double), ("cgiters", ctypes.c_int), ("relres", ctypes.c_double),
+                ("ms", ctypes.c_double)]
+
+
+class TopOptError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s (%d): %s" % (STATUS.get(status, "?"), status, msg))
+        self.status = status
+
+
+_lib = None
+
+
+def load():
+    """Loads the shared library (building it first if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("tp_build", os.path.join(PKG, "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+    L = ctypes.CDLL(LIB_PATH)
+    V, P, I, D = ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    L.tp_default_params.argtypes = [ctypes.POINTER(TpParams)]
+    L.tp_create.argtypes = [ctypes.POINTER(TpParams), ctypes.POINTER(V)]
+    L.tp_destroy.argtypes = [V]
+    L.tp_status_string.restype = ctypes.c_char_p
+    L.tp_status_string.argtypes = [I]
+    L.tp_error_message.restype = ctypes.c_char_p
+    L.tp_error_message.argtypes = [V]
+    L.tp_sync.argtypes = [V]
+    L.tp_ndof.restype = ctypes.c_long
+    L.tp_ndof.argtypes = [V, I]
+    L.tp_nelem.restype = ctypes.c_long
+    L.tp_nelem.argtypes = [V]
+    L.tp_device_bytes.restype = ctypes.c_long
+    L.tp_device_bytes.argtypes = [V]
+    L.tp_field_ptr.restype = ctypes.c_void_p
+    L.tp_field_ptr.argtypes = [V, I]
+    L.tp_upload.argtypes = [V, I, P, ctypes.c_long]
+    L.tp_download.argtypes = [V, I, P, ctypes.c_long]
+    L.tp_element_matrices.argtypes = [V, I, P]
+    L.tp_fixed_dofs.argtypes = [V, I, P, ctypes.POINTER(ctypes.c_long)]
+    L.tp_element_matrix_tables.argtypes = [I, D, P]
+    L.tp_reference_load.argtypes = [I, I, I, P]
+    for f in ("tp_assemble", "tp_init_design"):
+        getattr(L, f).argtypes = [V]
+    for f in ("tp_apply", "tp_apply_f32", "tp_restrict", "tp_prolong"):
+        getattr(L, f).argtypes = [V, I, P, P]
+    L.tp_inv_diag.argtypes = [V, I, P]
+    L.tp_smooth.argtypes = [V, I, I, D, P, P]
+    L.tp_coarse_solve.argtypes = [V, P, P]
+    L.tp_vcycle.argtypes = [V, P, P]
+    L.tp_solve.argtypes = [V, ctypes.POINTER(I), ctypes.POINTER(D)]
+    L.tp_solve_rhs.argtypes = [V, P, P, ctypes.POINTER(I), ctypes.POINTER(D)]
+    L.tp_compliance.argtypes = [V, ctypes.POINTER(D)]
+    L.tp_element_sensitivity.argtypes = [V, P, P, P]
+    L.tp_filter.argtypes = [V, P, P]
+    L.tp_filter_T.argtypes = [V, P]
+    L.tp_volume.argtypes = [V, ctypes.POINTER(D)]
+    L.tp_oc_update.argtypes = [V, D, ctypes.POINTER(D)]
+    L.tp_design_iteration.argtypes = [V, ctypes.POINTER(TpIterInfo)]
+    L.tp_run.argtypes = [V, I, ctypes.POINTER(TpIterInfo), ctypes.POINTER(I)]
+    _lib = L
+    return L
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+class TopOpt:
+    """One device context: grid, multigrid hierarchy, design state."""
+
+    def __init__(self, nelx, nely, nelz, nl, precision=TP_FP64, volfrac=None, rmin=1.5,
+                 cgtol=None, cgmax=1000, nswp=4, omega=0.6, device=0):
+        self.L = load()
+        p = TpParams()
+        self.L.tp_default_params(ctypes.byref(p))
+        p.nelx, p.nely, p.nelz, p.nl = nelx, nely, nelz, nl
+        if volfrac is not None:
+            p.volfrac = volfrac
+        p.rmin = rmin
+        if cgtol is not None:
+            p.cgtol = cgtol
+        p.cgmax, p.nswp, p.omega = cgmax, nswp, omega
+        p.precision = precision
+        p.device = device
+        self.params = p
+        self.ctx = ctypes.c_void_p()
+        st = self.L.tp_create(ctypes.byref(p), ctypes.byref(self.ctx))
+        if st != 0:
+            msg = self.L.tp_error_message(self.ctx).decode() if self.ctx else ""
+            if self.ctx:
+                self.L.tp_destroy(self.ctx)
+            self.ctx = None
+            raise TopOptError(st, msg)
+        self.shape = (nelx, nely, nelz)
+        self.nl = nl
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.L.tp_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, st, allow=()):
+        if st != 0 and st not in allow:
+            raise TopOptError(st, self.L.tp_error_message(self.ctx).decode())
+        return st
+
+    # sizes
+    def ndof(self, level=0):
+        return self.L.tp_ndof(self.ctx, level)
+
+    def nelem(self):
+        return self.L.tp_nelem(self.ctx)
+
+    def device_bytes(self):
+        return self.L.tp_device_bytes(self.ctx)
+
+    # fields
+    def upload(self, name, arr):
+        a = np.ascontiguousarray(arr, np.float64)
+        self._check(self.L.tp_upload(self.ctx, FIELDS[name], a.ctypes.data_as(ctypes.c_void_p), a.size))
+
+    def download(self, name):
+        n = self.nelem() if name not in ("F", "U") else self.ndof(0)
+        out = np.zeros(n)
+        self._check(self.L.tp_download(self.ctx, FIELDS[name], out.ctypes.data_as(ctypes.c_void_p), n))
+        return out
+
+    def field(self, name):
+        """Device pointer (int) of a context field."""
+        return self.L.tp_field_ptr(self.ctx, FIELDS[name])
+
+    def element_matrices(self, level):
+        out = np.zeros(576 * 8 ** level)
+        self._check(self.L.tp_element_matrices(self.ctx, level, out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    def fixed_dofs(self, level):
+        n = ctypes.c_long(0)
+        self._check(self.L.tp_fixed_dofs(self.ctx, level, None, ctypes.byref(n)))
+        out = np.zeros(n.value, np.int64)
+        self._check(self.L.tp_fixed_dofs(self.ctx, level, out.ctypes.data_as(ctypes.c_void_p), ctypes.byref(n)))
+        return out
+
+    # operators on torch CUDA tensors
+    def assemble(self):
+        self._check(self.L.tp_assemble(self.ctx))
+
+    def apply(self, level, u):
+        import torch
+        out = torch.empty_like(u)
+        f = self.L.tp_apply_f32 if u.dtype == torch.float32 else self.L.tp_apply
+        self._check(f(self.ctx, level, _ptr(u), _ptr(out)))
+        return out
+
+    def inv_diag(self, level):
+        import torch
+        out = torch.empty(self.ndof(level), dtype=torch.float64, device="cuda")
+        self._check(self.L.tp_inv_diag(self.ctx, level, _ptr(out)))
+        return out
+
+    def restrict(self, level, fine):
+        import torch
+        out = torch.empty(self.ndof(level + 1), dtype=torch.float64, device="cuda")
+        self._check(self.L.tp_restrict(self.ctx, level, _ptr(fine), _ptr(out)))
+        return out
+
+    def prolong(self, level, coarse):
+        import torch
+        out = torch.empty(self.ndof(level), dtype=torch.float64, device="cuda")
+        self._check(self.L.tp_prolong(self.ctx, level, _ptr(coarse), _ptr(out)))
+        return out
+
+    def smooth(self, level, nswp, omega, b, u):
+        u = u.clone()
+        self._check(self.L.tp_smooth(self.ctx, level, nswp, omega, _ptr(b), _ptr(u)))
+        return u
+
+    def coarse_solve(self, rhs):
+        import torch
+        out = torch.empty_like(rhs)
+        self._check(self.L.tp_coarse_solve(self.ctx, _ptr(rhs), _ptr(out)))
+        return out
+
+    def vcycle(self, r):
+        import torch
+        z = torch.empty_like(r)
+        self._check(self.L.tp_vcycle(self.ctx, _ptr(r), _ptr(z)))
+        return z
+
+    def solve(self):
+        it, rr = ctypes.c_int(0), ctypes.c_double(0)
+        st = self._check(self.L.tp_solve(self.ctx, ctypes.byref(it), ctypes.byref(rr)), allow=(5,))
+        return it.value, rr.value, st
+
+    def solve_rhs(self, rhs, x0=None):
+        import torch
+        sol = torch.zeros_like(rhs) if x0 is None else x0.clone()
+        it, rr = ctypes.c_int(0), ctypes.c_double(0)
+        st = self._check(self.L.tp_solve_rhs(self.ctx, _ptr(rhs), _ptr(sol), ctypes.byref(it),
+                                             ctypes.byref(rr)), allow=(5,))
+        return sol, it.value, rr.value, st
+
+    def compliance(self):
+        c = ctypes.c_double(0)
+        self._check(self.L.tp_compliance(self.ctx, ctypes.byref(c)))
+        return c.value
+
+    def element_sensitivity(self, u, w):
+        import torch
+        out = torch.empty(self.nelem(), dtype=torch.float64, device="cuda")
+        self._check(self.L.tp_element_sensitivity(self.ctx, _ptr(u), _ptr(w), _ptr(out)))
+        return out
+
+    def filter(self, x):
+        import torch
+        out = torch.empty_like(x)
+        self._check(self.L.tp_filter(self.ctx, _ptr(x), _ptr(out)))
+        return out
+
+    def filter_T(self, v):
+        v = v.clone()
+        self._check(self.L.tp_filter_T(self.ctx, _ptr(v)))
+        return v
+
+    def volume(self):
+        v = ctypes.c_double(0)
+        self._check(self.L.tp_volume(self.ctx, ctypes.byref(v)))
+        return v.value
+
+    def oc_update(self, g):
+        ch = ctypes.c_double(0)
+        self._check(self.L.tp_oc_update(self.ctx, g, ctypes.byref(ch)))
+        return ch.value
+
+    def init_design(self):
+        self._check(self.L.tp_init_design(self.ctx))
+
+    def design_iteration(self):
+        info = TpIterInfo()
+        self._check(self.L.tp_design_iteration(self.ctx, ctypes.byref(info)))
+        return info
+
+    def run(self, max_iterations):
+        hist = (TpIterInfo * max(1, max_iterations))()
+        loops = ctypes.c_int(0)
+        self._check(self.L.tp_run(self.ctx, max_iterations, hist, ctypes.byref(loops)))
+        return [hist[i] for i in range(loops.value)]

@@ -158,6 +158,15 @@ tp_status tp_init_design(tp_ctx* c);
 tp_status tp_design_iteration(tp_ctx* c, tp_iter_info* info);
 tp_status tp_run(tp_ctx* c, int max_iterations, tp_iter_info* hist, int* loops);
 
+/* Optional timing of kernel classes with CUDA events on the context's
+ * stream (fine_apply_f64, fine_jacobi_f32, stencil, coarse_solve, ...).
+ * tp_profile_get folds finished events into per-class launch counts and
+ * milliseconds; name receives a static string. */
+tp_status tp_profile_enable(tp_ctx* c, int on);
+tp_status tp_profile_reset(tp_ctx* c);
+int tp_profile_classes(void);
+tp_status tp_profile_get(tp_ctx* c, int idx, const char** name, long* launches, double* ms);
+
 #ifdef __cplusplus
 }
 #endif

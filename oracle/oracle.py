@@ -43,7 +43,7 @@ class _OrHistory(ctypes.Structure):
     _fields_ = [("loops", ctypes.c_int),
                 ("c", ctypes.c_double * 1024), ("vol", ctypes.c_double * 1024),
                 ("change", ctypes.c_double * 1024), ("relres", ctypes.c_double * 1024),
-                ("cgiters", ctypes.c_int * 1024)]
+                ("cgiters", ctypes.c_int * 1024), ("seconds", ctypes.c_double * 1024)]
 
 
 class Oracle:
@@ -206,7 +206,7 @@ class Oracle:
         hist = {
             "c": np.array(h.c[:loops]), "vol": np.array(h.vol[:loops]),
             "change": np.array(h.change[:loops]), "relres": np.array(h.relres[:loops]),
-            "cgiters": np.array(h.cgiters[:loops]),
+            "cgiters": np.array(h.cgiters[:loops]), "seconds": np.array(h.seconds[:loops]),
         }
         return loops, hist, xp, u
 

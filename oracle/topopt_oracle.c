@@ -11,6 +11,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <omp.h>
+
 #define OR_MAX(a, b) ((a) > (b) ? (a) : (b))
 #define OR_MIN(a, b) ((a) > (b) ? (b) : (a))
 
@@ -757,6 +759,7 @@ int or_run(int nelx, int nely, int nelz, double volfrac, double rmin, int nl,
   float change = 1.0f;
   while (change > 1e-2 && loop < max_iterations) {
     loop++;
+    const double t_iter = omp_get_wtime();
     int cgiter;
     double cgres;
     or_solve(g, xPhys, F, U, 4, cgtol, &cgiter, &cgres);
@@ -773,6 +776,7 @@ int or_run(int nelx, int nely, int nelz, double volfrac, double rmin, int nl,
       h->vol[loop - 1] = vol;
       h->change[loop - 1] = change;
       h->cgiters[loop - 1] = cgiter;
+      h->seconds[loop - 1] = omp_get_wtime() - t_iter;
       h->relres[loop - 1] = cgres;
     }
   }

@@ -34,6 +34,7 @@ typedef struct {
   int loops;
   double c[1024], vol[1024], change[1024], relres[1024];
   int cgiters[1024];
+  double seconds[1024]; /* wall time of each design iteration */
 } OrHistory;
 
 #ifdef __cplusplus

@@ -313,6 +313,7 @@ static void destroy_buffers(tp_ctx* c) {
   F(c->d_red); F(c->d_scal); F(c->d_flag);
   if (c->h_scal) cudaFreeHost(c->h_scal);
   coarse_free(c);
+  prof_destroy(c);
 }
 
 tp_status tp_create(const tp_params* p, tp_ctx** out) {

@@ -81,6 +81,7 @@ void coarse_free(tp_ctx* c) {
 }
 
 void coarse_assemble(tp_ctx* c) {
+  ProfScope ps(c, P_COARSE_FACTOR);
   Coarse& C = c->coarse;
   const int l = c->nl - 1;
   const Level& L = c->L[l];
@@ -203,6 +204,7 @@ __global__ void dinv_kernel(const double* __restrict__ B, long bw, long n, int n
 }
 
 void coarse_factor(tp_ctx* c) {
+  ProfScope ps(c, P_COARSE_FACTOR);
   Coarse& C = c->coarse;
   cudaMemsetAsync(C.info, 0, sizeof(int), c->s);
   for (long k = 0; k < C.n; k += NB) {
@@ -283,6 +285,7 @@ __global__ void bwd_diag_kernel(const double* __restrict__ D, long n, int nblk, 
 }
 
 void coarse_solve(tp_ctx* c, const double* rhs, double* x) {
+  ProfScope ps(c, P_COARSE_SOLVE);
   Coarse& C = c->coarse;
   double* y = C.vec;
   double* t = C.vec + C.n;

@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "topopt_gb300.h"
 
@@ -52,6 +54,14 @@ struct Coarse {
   double* dinv = nullptr;       // inverse of each diagonal block of L, nbs*nbs per block (column-major)
   double* vec = nullptr;        // work vector (n)
   int* info = nullptr;          // device status: first non-positive pivot + 1, 0 if none
+};
+
+// Kernel classes the optional CUDA-event profiler times (tp_profile_*).
+enum ProfId {
+  P_FINE_APPLY_F64 = 0, P_FINE_JACOBI_F64, P_FINE_RESID_F64,
+  P_FINE_APPLY_F32, P_FINE_JACOBI_F32, P_FINE_RESID_F32,
+  P_STENCIL, P_TRANSFER, P_COARSE_SOLVE, P_COARSE_FACTOR, P_ASSEMBLE,
+  P_VECTOR, P_DESIGN, P_COUNT
 };
 
 }  // namespace tp
@@ -102,7 +112,28 @@ struct tp_ctx {
 
   bool assembled = false;    // operators built for the current xPhys
   long mem_bytes = 0;
+
+  // optional per-kernel-class timing with CUDA events on c->s
+  bool prof = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
+  size_t ev_next = 0;
+  long prof_launches[tp::P_COUNT] = {};
+  double prof_ms[tp::P_COUNT] = {};
 };
+
+namespace tp {
+// brackets one launch (or a short sequence) of class `id` when profiling is on
+struct ProfScope {
+  tp_ctx* c;
+  int id;
+  cudaEvent_t e1 = nullptr;
+  ProfScope(tp_ctx* ctx, int i);
+  ~ProfScope();
+};
+void prof_collect(tp_ctx* c);  // folds finished event pairs into the totals
+void prof_destroy(tp_ctx* c);
+}  // namespace tp
 
 namespace tp {
 

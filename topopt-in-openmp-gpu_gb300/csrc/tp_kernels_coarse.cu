@@ -106,6 +106,7 @@ __global__ void assemble_kernel(CGeom g, const T* __restrict__ E, const T* __res
 
 template <typename T>
 void assemble_stencil(tp_ctx* c, int l, const T* E, const T* ke, T* st, double* invD) {
+  ProfScope ps(c, P_ASSEMBLE);
   const CGeom g = cgeom(c, l);
   const int masked = l >= 2;
   const int nsub = g.ncell * g.ncell * g.ncell;
@@ -156,18 +157,21 @@ __global__ void stencil_kernel(CGeom g, const T* __restrict__ st, const T* __res
 
 template <typename T>
 void stencil_apply(tp_ctx* c, int l, const T* st, const T* in, T* out) {
+  ProfScope ps(c, P_STENCIL);
   const CGeom g = cgeom(c, l);
   stencil_kernel<T, S_APPLY><<<grid_for(g.nnodes, 128), 128, 0, c->s>>>(g, st, in, out, nullptr, nullptr, T(0));
   TP_CHECK_LAUNCH(c, "stencil_apply");
 }
 template <typename T>
 void stencil_jacobi(tp_ctx* c, int l, const T* st, const T* invD, const T* b, const T* u, T* unew, T omega) {
+  ProfScope ps(c, P_STENCIL);
   const CGeom g = cgeom(c, l);
   stencil_kernel<T, S_JACOBI><<<grid_for(g.nnodes, 128), 128, 0, c->s>>>(g, st, u, unew, b, invD, omega);
   TP_CHECK_LAUNCH(c, "stencil_jacobi");
 }
 template <typename T>
 void stencil_resid(tp_ctx* c, int l, const T* st, const T* b, const T* u, T* d) {
+  ProfScope ps(c, P_STENCIL);
   const CGeom g = cgeom(c, l);
   stencil_kernel<T, S_RESID><<<grid_for(g.nnodes, 128), 128, 0, c->s>>>(g, st, u, d, b, nullptr, T(0));
   TP_CHECK_LAUNCH(c, "stencil_resid");
@@ -239,18 +243,21 @@ __global__ void prolong_kernel(CGeom f, CGeom cg, const T* __restrict__ coarse, 
 
 template <typename T>
 void restrict_fw(tp_ctx* c, int l, const T* fine, T* coarse) {
+  ProfScope ps(c, P_TRANSFER);
   const CGeom f = cgeom(c, l), cg = cgeom(c, l + 1);
   restrict_kernel<T><<<grid_for(cg.nnodes, 128), 128, 0, c->s>>>(f, cg, fine, coarse);
   TP_CHECK_LAUNCH(c, "restrict");
 }
 template <typename T>
 void prolong_add(tp_ctx* c, int l, const T* coarse, T* fine) {
+  ProfScope ps(c, P_TRANSFER);
   const CGeom f = cgeom(c, l), cg = cgeom(c, l + 1);
   prolong_kernel<T, true><<<grid_for(f.nnodes, 128), 128, 0, c->s>>>(f, cg, coarse, fine);
   TP_CHECK_LAUNCH(c, "prolong_add");
 }
 template <typename T>
 void prolong_set(tp_ctx* c, int l, const T* coarse, T* fine) {
+  ProfScope ps(c, P_TRANSFER);
   const CGeom f = cgeom(c, l), cg = cgeom(c, l + 1);
   prolong_kernel<T, false><<<grid_for(f.nnodes, 128), 128, 0, c->s>>>(f, cg, coarse, fine);
   TP_CHECK_LAUNCH(c, "prolong_set");

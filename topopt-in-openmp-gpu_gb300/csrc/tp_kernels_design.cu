@@ -105,6 +105,7 @@ static int blocks_for(long n) {
 }
 
 void compliance(tp_ctx* c, const double* u, double* dc, int* nblocks) {
+  ProfScope ps(c, P_DESIGN);
   const DGeom g = dgeom(c);
   const long ne = (long)g.ex * g.ey * g.ez;
   const int nb = blocks_for(ne);
@@ -114,6 +115,7 @@ void compliance(tp_ctx* c, const double* u, double* dc, int* nblocks) {
 }
 
 void element_sens(tp_ctx* c, const double* u, const double* w, double* out) {
+  ProfScope ps(c, P_DESIGN);
   const DGeom g = dgeom(c);
   const long ne = (long)g.ex * g.ey * g.ez;
   sens_kernel<false><<<blocks_for(ne), 256, 0, c->s>>>(g, c->d_xphys, u, w, out, nullptr);
@@ -178,6 +180,7 @@ __global__ void div_kernel(long n, const double* __restrict__ v, const double* _
 static FBox fbox(const tp_ctx* c) { return FBox{(int)std::ceil(c->p.rmin), c->p.rmin}; }
 
 void filter_hs(tp_ctx* c, double* hs) {
+  ProfScope ps(c, P_DESIGN);
   const DGeom g = dgeom(c);
   filter_kernel<0><<<blocks_for((long)g.ex * g.ey * g.ez), 256, 0, c->s>>>(g, fbox(c), nullptr, nullptr, hs, nullptr);
   TP_CHECK_LAUNCH(c, "filter_hs");
@@ -189,12 +192,14 @@ int filter_fwd_blocks(const tp_ctx* c) {
   return blocks_for((long)g.ex * g.ey * g.ez);
 }
 void filter_fwd(tp_ctx* c, const double* x, double* out) {
+  ProfScope ps(c, P_DESIGN);
   const DGeom g = dgeom(c);
   filter_kernel<1><<<filter_fwd_blocks(c), 256, 0, c->s>>>(g, fbox(c), x, c->d_hs, out, c->d_red);
   TP_CHECK_LAUNCH(c, "filter_fwd");
 }
 
 void filter_adj(tp_ctx* c, double* v, double* tmp) {
+  ProfScope ps(c, P_DESIGN);
   const DGeom g = dgeom(c);
   const long ne = (long)g.ex * g.ey * g.ez;
   div_kernel<<<grid_for(ne, 256), 256, 0, c->s>>>(ne, v, c->d_hs, tmp);
@@ -210,6 +215,7 @@ __global__ void sum_kernel(long n, const double* __restrict__ v, double* __restr
 }
 
 void volume_partials(tp_ctx* c, const double* xphys, int* nblocks) {
+  ProfScope ps(c, P_DESIGN);
   const long ne = (long)c->L[0].ex * c->L[0].ey * c->L[0].ez;
   const int nb = blocks_for(ne);
   sum_kernel<<<nb, 256, 0, c->s>>>(ne, xphys, c->d_red);
@@ -301,6 +307,7 @@ __global__ void oc_init_kernel(double* scal) {
 
 // returns 0 on success; -1 if the bisection did not finish within its cap
 int oc_update(tp_ctx* c, double g) {
+  ProfScope ps(c, P_DESIGN);
   const long ne = (long)c->L[0].ex * c->L[0].ey * c->L[0].ez;
   const int nb = blocks_for(ne);
   oc_init_kernel<<<1, 1, 0, c->s>>>(c->d_scal);

@@ -167,24 +167,28 @@ static dim3 fine_grid(const tp_ctx* c) {
 
 template <typename T>
 void fine_apply(tp_ctx* c, const T* E, const T* in, T* out) {
+  ProfScope ps(c, sizeof(T) == 8 ? P_FINE_APPLY_F64 : P_FINE_APPLY_F32);
   fine_kernel<T, M_APPLY><<<fine_grid(c), dim3(TY, TZ, TX), 0, c->s>>>(geom(c), E, in, out, nullptr,
                                                                        nullptr, T(0), nullptr);
   TP_CHECK_LAUNCH(c, "fine_apply");
 }
 template <typename T>
 void fine_apply_dot(tp_ctx* c, const T* E, const T* in, T* out) {
+  ProfScope ps(c, sizeof(T) == 8 ? P_FINE_APPLY_F64 : P_FINE_APPLY_F32);
   fine_kernel<T, M_APPLY_DOT><<<fine_grid(c), dim3(TY, TZ, TX), 0, c->s>>>(
       geom(c), E, in, out, nullptr, nullptr, T(0), c->d_red);
   TP_CHECK_LAUNCH(c, "fine_apply_dot");
 }
 template <typename T>
 void fine_jacobi(tp_ctx* c, const T* E, const T* invD, const T* b, const T* u, T* unew, T omega) {
+  ProfScope ps(c, sizeof(T) == 8 ? P_FINE_JACOBI_F64 : P_FINE_JACOBI_F32);
   fine_kernel<T, M_JACOBI><<<fine_grid(c), dim3(TY, TZ, TX), 0, c->s>>>(geom(c), E, u, unew, b, invD,
                                                                         omega, nullptr);
   TP_CHECK_LAUNCH(c, "fine_jacobi");
 }
 template <typename T>
 void fine_resid(tp_ctx* c, const T* E, const T* b, const T* u, T* d) {
+  ProfScope ps(c, sizeof(T) == 8 ? P_FINE_RESID_F64 : P_FINE_RESID_F32);
   fine_kernel<T, M_RESID><<<fine_grid(c), dim3(TY, TZ, TX), 0, c->s>>>(geom(c), E, u, d, b, nullptr,
                                                                        T(0), nullptr);
   TP_CHECK_LAUNCH(c, "fine_resid");
@@ -227,6 +231,7 @@ __global__ void fine_diag_kernel(FineGeom g, const double* __restrict__ E, doubl
 }
 
 void fine_inv_diag(tp_ctx* c, double* invD) {
+  ProfScope ps(c, P_ASSEMBLE);
   const long nn = c->L[0].nnodes;
   fine_diag_kernel<<<grid_for(nn, 256), 256, 0, c->s>>>(geom(c), c->d_E, invD);
   TP_CHECK_LAUNCH(c, "fine_inv_diag");

@@ -42,6 +42,7 @@ __global__ void dot_kernel(long n, const double* __restrict__ a, const double* _
 }
 
 void dot_partials(tp_ctx* c, long n, const double* a, const double* b, int* nblocks) {
+  ProfScope ps(c, P_VECTOR);
   int nb = (int)((n + 255) / 256);
   if (nb > kDotBlocks) nb = kDotBlocks;
   if (nb < 1) nb = 1;
@@ -68,6 +69,7 @@ __global__ void finish_kernel(const double* __restrict__ partials, int nb, doubl
 }
 
 void finish_sum(tp_ctx* c, int nblocks, int slot, int op) {
+  ProfScope ps(c, P_VECTOR);
   finish_kernel<<<1, 256, 0, c->s>>>(c->d_red, nblocks, c->d_scal + slot, op);
   TP_CHECK_LAUNCH(c, "finish");
 }
@@ -78,10 +80,12 @@ __global__ void cast_kernel(long n, const A* __restrict__ a, B* __restrict__ b) 
   if (i < n) b[i] = (B)a[i];
 }
 void cast_d2f(tp_ctx* c, long n, const double* a, float* b) {
+  ProfScope ps(c, P_VECTOR);
   cast_kernel<double, float><<<grid_for(n, 256), 256, 0, c->s>>>(n, a, b);
   TP_CHECK_LAUNCH(c, "cast_d2f");
 }
 void cast_f2d(tp_ctx* c, long n, const float* a, double* b) {
+  ProfScope ps(c, P_VECTOR);
   cast_kernel<float, double><<<grid_for(n, 256), 256, 0, c->s>>>(n, a, b);
   TP_CHECK_LAUNCH(c, "cast_f2d");
 }
@@ -95,6 +99,7 @@ __global__ void vscale_kernel(long n, const T* __restrict__ a, const T* __restri
 }
 template <typename T>
 void vscale(tp_ctx* c, long n, const T* a, const T* b, T* out, T omega) {
+  ProfScope ps(c, P_VECTOR);
   vscale_kernel<T><<<grid_for(n, 256), 256, 0, c->s>>>(n, a, b, out, omega);
   TP_CHECK_LAUNCH(c, "vscale");
 }
@@ -112,6 +117,7 @@ __global__ void pupdate_kernel(long n, const double* __restrict__ z, double* __r
     p[i] = scal[S_BETA] * p[i] + z[i];
 }
 void cg_pupdate(tp_ctx* c, long n, const double* z, double* p, int first) {
+  ProfScope ps(c, P_VECTOR);
   pupdate_kernel<<<grid_for(n, 256), 256, 0, c->s>>>(n, z, p, c->d_scal, first);
   TP_CHECK_LAUNCH(c, "cg_pupdate");
 }
@@ -132,6 +138,7 @@ __global__ void xr_kernel(long n, double* __restrict__ u, double* __restrict__ r
   if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
 void cg_xr_update(tp_ctx* c, long n, double* u, double* r, const double* p, const double* q, int* nblocks) {
+  ProfScope ps(c, P_VECTOR);
   int nb = (int)((n + 255) / 256);
   if (nb > kDotBlocks) nb = kDotBlocks;
   xr_kernel<<<nb, 256, 0, c->s>>>(n, u, r, p, q, c->d_scal, c->d_red);
@@ -151,6 +158,7 @@ __global__ void scalars_kernel(double* s, int what) {
   if (what == 2) s[S_RELRES] = sqrt(s[S_RNORM2]) / sqrt(s[S_BNORM2]);
 }
 void cg_scalars(tp_ctx* c, int what) {
+  ProfScope ps(c, P_VECTOR);
   scalars_kernel<<<1, 1, 0, c->s>>>(c->d_scal, what);
   TP_CHECK_LAUNCH(c, "cg_scalars");
 }

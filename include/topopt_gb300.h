@@ -158,6 +158,37 @@ tp_status tp_init_design(tp_ctx* c);
 tp_status tp_design_iteration(tp_ctx* c, tp_iter_info* info);
 tp_status tp_run(tp_ctx* c, int max_iterations, tp_iter_info* hist, int* loops);
 
+/* ---- entry points behind the reference-signature layer (topopt_ref_api.h) ---- */
+/* Changes the filter radius (recomputes the filter row sums). */
+tp_status tp_set_rmin(tp_ctx* c, double rmin);
+/* Changes the CG tolerance and cap and the smoother's sweeps and damping. */
+tp_status tp_set_cg(tp_ctx* c, double cgtol, int cgmax, int nswp, double omega);
+/* The reference's matrix-free subspace operator of any level >= 1
+ * (stencil_methods.c:436-519): unlike tp_apply at levels >= 2, fixed columns
+ * keep their coupling; fixed rows return the input. Level 0 = tp_apply. */
+tp_status tp_apply_subspace(tp_ctx* c, int level, const double* in_dev, double* out_dev);
+/* nswp damped-Jacobi sweeps with a caller-supplied inverse diagonal (NULL =
+ * the assembled one); subspace != 0 selects the subspace operator at levels
+ * >= 2 (stencil_solvers.c:11-49), else the V-cycle's operator of that level. */
+tp_status tp_smooth_ex(tp_ctx* c, int level, int subspace, int nswp, double omega, const double* invD_dev,
+                       const double* b_dev, double* u_dev);
+/* Copies the assembled block stencil of a level >= 1 to the host:
+ * 243*nodes doubles, A[(m*9 + 3*a + b)*nodes + n] couples DOF a of node n with
+ * DOF b of neighbour m = (dx+1)*9 + (dz+1)*3 + (dy+1). */
+tp_status tp_download_stencil(tp_ctx* c, int level, int subspace, double* host);
+/* Band-Cholesky factor of a caller's coarsest-level CSR (host arrays, n rows,
+ * entries with column <= row are read) and solves with that factor
+ * (stencil_assembly.c:428-503). */
+tp_status tp_coarse_factor_csr(tp_ctx* c, long n, const int* rowptr, const int* col, const double* val);
+tp_status tp_coarse_solve_factored(tp_ctx* c, const double* rhs_dev, double* x_dev);
+/* Reductions and the OC bisection over arbitrary device arrays of length n
+ * (gpu_definitions.c:94-157): sum, max|x - xnew| with x <- xnew, and xnew
+ * from x, dv, dc and the constraint value g. */
+tp_status tp_vec_sum(tp_ctx* c, long n, const double* v_dev, double* out);
+tp_status tp_vec_change(tp_ctx* c, long n, double* x_dev, const double* xnew_dev, double* change);
+tp_status tp_oc_bisect(tp_ctx* c, long n, const double* x_dev, const double* dv_dev, const double* dc_dev,
+                       double g, double* xnew_dev);
+
 /* Optional timing of kernel classes with CUDA events on the context's
  * stream (fine_apply_f64, fine_jacobi_f32, stencil, coarse_solve, ...).
  * tp_profile_get folds finished events into per-class launch counts and

@@ -17,6 +17,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(ROOT, "_build")
 INC = os.path.join(ROOT, "include")
 NVCC = os.environ.get("NVCC", "nvcc")
+CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INC, "-I", CSRC]
 LIB = os.path.join(PKG, "libtopopt_gb300.so")
@@ -57,8 +58,9 @@ def build(verbose=False, ptxas=False):
     if os.path.exists(ref_src):
         for flav, define in (("32", "TP_REF_FLOAT=1"), ("64", "TP_REF_FLOAT=0")):
             out = os.path.join(PKG, "libtopopt_ref%s.so" % flav)
-            cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-D" + define, "-I", INC, "-I", CSRC,
-                   ref_src, "-o", out, "-L" + PKG, "-ltopopt_gb300", "-Wl,-rpath,$ORIGIN"]
+            cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-D" + define, "-I", INC,
+                   "-I", CSRC, "-I", os.path.join(CUDA, "include"), ref_src, "-o", out, "-L" + PKG,
+                   "-ltopopt_gb300", "-L" + os.path.join(CUDA, "lib64"), "-lcudart", "-Wl,-rpath,$ORIGIN"]
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:
                 sys.stderr.write(r.stdout + r.stderr)

@@ -176,10 +176,10 @@ static tp_status assemble(tp_ctx* c) {
   for (int l = 1; l < c->nl; l++) {
     const bool coarsest = (l == c->nl - 1);
     if (!mixed(c) || coarsest) {
-      assemble_stencil<double>(c, l, c->d_E, c->d_ke[l], c->st[l], c->invD[l]);
+      assemble_stencil<double>(c, l, c->d_E, c->d_ke[l], c->st[l], c->invD[l], l >= 2);
     }
     if (mixed(c) && !coarsest) {
-      assemble_stencil<float>(c, l, c->d_Ef, c->d_kef[l], c->stf[l], c->invD[l]);
+      assemble_stencil<float>(c, l, c->d_Ef, c->d_kef[l], c->stf[l], c->invD[l], l >= 2);
       cast_d2f(c, c->L[l].ndof, c->invD[l], c->invDf[l]);
     }
     if (mixed(c) && coarsest) cast_d2f(c, c->L[l].ndof, c->invD[l], c->invDf[l]);
@@ -193,6 +193,7 @@ static tp_status assemble(tp_ctx* c) {
   st = sync_check(c);
   if (st != TP_OK) return st;
   c->assembled = true;
+  for (int l = 0; l < TP_MAXL; l++) c->st_sub_valid[l] = false;
   if (info != 0) {
     c->err = "coarse Cholesky: non-positive pivot at column " + std::to_string(info - 1);
     return TP_ERR_NOT_SPD;
@@ -305,12 +306,12 @@ static void destroy_buffers(tp_ctx* c) {
     F(c->d_ke[l]); F(c->d_kef[l]);
     F(c->mg_r[l]); F(c->mg_z[l]); F(c->mg_d[l]); F(c->mg_t[l]);
     F(c->mgf_r[l]); F(c->mgf_z[l]); F(c->mgf_d[l]); F(c->mgf_t[l]);
-    F(c->invD[l]); F(c->invDf[l]); F(c->st[l]); F(c->stf[l]);
+    F(c->invD[l]); F(c->invDf[l]); F(c->st[l]); F(c->stf[l]); F(c->st_sub[l]);
   }
   F(c->d_x); F(c->d_xphys); F(c->d_xnew); F(c->d_dc); F(c->d_dv); F(c->d_hs);
   F(c->d_E); F(c->d_Ef); F(c->d_F); F(c->d_U);
   F(c->d_r); F(c->d_z); F(c->d_p); F(c->d_q);
-  F(c->d_red); F(c->d_scal); F(c->d_flag);
+  F(c->d_red); F(c->d_scal); F(c->d_flag); F(c->scratch_invD);
   if (c->h_scal) cudaFreeHost(c->h_scal);
   coarse_free(c);
   prof_destroy(c);
@@ -443,7 +444,10 @@ tp_status tp_upload(tp_ctx* c, tp_field f, const double* host, long count) {
   if (!d) return TP_ERR_ARG;
   if (!cuda_ok(c, cudaMemcpyAsync(d, host, sizeof(double) * count, cudaMemcpyHostToDevice, c->s), "upload"))
     return TP_ERR_CUDA;
-  if (f == TP_FIELD_XPHYS) c->assembled = false;
+  if (f == TP_FIELD_XPHYS) {
+    c->assembled = false;
+    for (int l = 0; l < TP_MAXL; l++) c->st_sub_valid[l] = false;
+  }
   return sync_check(c);
 }
 

@@ -1,0 +1,178 @@
+// Handle-API entry points that serve the reference-signature layer
+// (topopt_ref_api.h): the unmasked "subspace" operator at any level, a
+// smoother with a caller-supplied diagonal, stencil export, a coarse factor
+// from a caller's CSR, and reductions / OC over arbitrary device arrays.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "tp_internal.h"
+
+using namespace tp;
+
+namespace {
+
+tp_status sync_status(tp_ctx* c) {
+  cudaError_t e = cudaStreamSynchronize(c->s);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    c->err = cudaGetErrorString(e);
+    return TP_ERR_CUDA;
+  }
+  return c->err.empty() ? TP_OK : TP_ERR_CUDA;
+}
+
+// level l >= 1 stencil with the matrix-free semantics of the reference's
+// subspace operator (stencil_methods.c:436-519): fixed columns NOT zeroed
+const double* subspace_stencil(tp_ctx* c, int l) {
+  if (l == 1 && c->assembled && c->st[1]) return c->st[1];
+  if (!c->st_sub[l]) {
+    if (cudaMalloc(&c->st_sub[l], sizeof(double) * 243 * c->L[l].nnodes) != cudaSuccess) return nullptr;
+    c->mem_bytes += 8L * 243 * c->L[l].nnodes;
+  }
+  if (!c->st_sub_valid[l]) {
+    if (!c->scratch_invD) cudaMalloc(&c->scratch_invD, sizeof(double) * c->L[0].ndof);
+    compute_E(c);
+    assemble_stencil<double>(c, l, c->d_E, c->d_ke[l], c->st_sub[l], c->scratch_invD, 0);
+    c->st_sub_valid[l] = true;
+  }
+  return c->st_sub[l];
+}
+
+}  // namespace
+
+extern "C" {
+
+tp_status tp_set_rmin(tp_ctx* c, double rmin) {
+  if (!c || !(rmin > 0)) return TP_ERR_ARG;
+  if (rmin != c->p.rmin) {
+    c->p.rmin = rmin;
+    filter_hs(c, c->d_hs);
+  }
+  return sync_status(c);
+}
+
+tp_status tp_set_cg(tp_ctx* c, double cgtol, int cgmax, int nswp, double omega) {
+  if (!c || !(cgtol > 0) || cgmax < 1 || nswp < 0) return TP_ERR_ARG;
+  c->p.cgtol = cgtol;
+  c->p.cgmax = cgmax;
+  c->p.nswp = nswp;
+  c->p.omega = omega;
+  return TP_OK;
+}
+
+tp_status tp_apply_subspace(tp_ctx* c, int level, const double* in, double* out) {
+  if (!c || level < 0 || level >= c->nl || !in || !out) return TP_ERR_ARG;
+  if (level == 0) return tp_apply(c, 0, in, out);
+  if (level == 1 && c->st[1] && c->assembled) {
+    stencil_apply<double>(c, 1, c->st[1], in, out);
+    return sync_status(c);
+  }
+  const double* st = subspace_stencil(c, level);
+  if (!st) return TP_ERR_ALLOC;
+  stencil_apply<double>(c, level, st, in, out);
+  return sync_status(c);
+}
+
+tp_status tp_smooth_ex(tp_ctx* c, int level, int subspace, int nswp, double omega, const double* invD,
+                       const double* b, double* u) {
+  if (!c || level < 0 || level >= c->nl || !b || !u || nswp < 0) return TP_ERR_ARG;
+  if (!c->assembled) {
+    tp_status st = tp_assemble(c);
+    if (st != TP_OK) return st;
+  }
+  const double* A = nullptr;
+  if (level >= 1) {
+    A = (subspace && level >= 2) ? subspace_stencil(c, level) : c->st[level];
+    if (!A) return TP_ERR_STATE;
+  }
+  const double* D = invD ? invD : c->invD[level];
+  const long nd = c->L[level].ndof;
+  double* cur = u;
+  double* nxt = c->d_q;  // level-0 sized scratch
+  for (int s = 0; s < nswp; s++) {
+    if (level == 0)
+      fine_jacobi<double>(c, c->d_E, D, b, cur, nxt, omega);
+    else
+      stencil_jacobi<double>(c, level, A, D, b, cur, nxt, omega);
+    std::swap(cur, nxt);
+  }
+  if (cur != u) cudaMemcpyAsync(u, cur, sizeof(double) * nd, cudaMemcpyDeviceToDevice, c->s);
+  return sync_status(c);
+}
+
+tp_status tp_download_stencil(tp_ctx* c, int level, int subspace, double* host) {
+  if (!c || level < 1 || level >= c->nl || !host) return TP_ERR_ARG;
+  if (!c->assembled) {
+    tp_status st = tp_assemble(c);
+    if (st != TP_OK) return st;
+  }
+  const double* A = (subspace && level >= 2) ? subspace_stencil(c, level) : c->st[level];
+  if (!A) return TP_ERR_STATE;
+  cudaMemcpyAsync(host, A, sizeof(double) * 243 * c->L[level].nnodes, cudaMemcpyDeviceToHost, c->s);
+  return sync_status(c);
+}
+
+// Factor the coarsest operator given as CSR on the host (row-major, the
+// reference's coarse CSR layout); as CHOLMOD with stype = 1 does for that
+// matrix, only entries with column <= row are read.
+tp_status tp_coarse_factor_csr(tp_ctx* c, long n, const int* rowptr, const int* col, const double* val) {
+  if (!c || !rowptr || !col || !val || n != c->coarse.n) return TP_ERR_ARG;
+  Coarse& C = c->coarse;
+  std::vector<double> band(C.band_elems, 0.0);
+  for (long r = 0; r < n; r++)
+    for (int q = rowptr[r]; q < rowptr[r + 1]; q++) {
+      const long cc = col[q];
+      if (cc > r) continue;
+      if (r - cc > C.bw) return TP_ERR_ARG;
+      band[cc * C.bw + r] = val[q];
+    }
+  cudaMemcpyAsync(C.band, band.data(), sizeof(double) * C.band_elems, cudaMemcpyHostToDevice, c->s);
+  coarse_factor(c);
+  int info = 0;
+  cudaMemcpyAsync(&info, C.info, sizeof(int), cudaMemcpyDeviceToHost, c->s);
+  tp_status st = sync_status(c);
+  if (st != TP_OK) return st;
+  if (info != 0) {
+    c->err = "coarse Cholesky: non-positive pivot at column " + std::to_string(info - 1);
+    return TP_ERR_NOT_SPD;
+  }
+  return TP_OK;
+}
+
+// coarse solve with the current factor, without re-assembling it
+tp_status tp_coarse_solve_factored(tp_ctx* c, const double* rhs, double* x) {
+  if (!c || !rhs || !x) return TP_ERR_ARG;
+  coarse_solve(c, rhs, x);
+  return sync_status(c);
+}
+
+tp_status tp_vec_sum(tp_ctx* c, long n, const double* v, double* out) {
+  if (!c || n < 0 || !v || !out) return TP_ERR_ARG;
+  vec_sum(c, n, v, S_TMP1);
+  cudaMemcpyAsync(c->h_scal + S_TMP1, c->d_scal + S_TMP1, sizeof(double), cudaMemcpyDeviceToHost, c->s);
+  tp_status st = sync_status(c);
+  *out = c->h_scal[S_TMP1];
+  return st;
+}
+
+tp_status tp_vec_change(tp_ctx* c, long n, double* x, const double* xnew, double* change) {
+  if (!c || n < 0 || !x || !xnew || !change) return TP_ERR_ARG;
+  vec_change(c, n, x, xnew);
+  cudaMemcpyAsync(c->h_scal + S_CHANGE, c->d_scal + S_CHANGE, sizeof(double), cudaMemcpyDeviceToHost, c->s);
+  tp_status st = sync_status(c);
+  *change = c->h_scal[S_CHANGE];
+  return st;
+}
+
+tp_status tp_oc_bisect(tp_ctx* c, long n, const double* x, const double* dv, const double* dc, double g,
+                       double* xnew) {
+  if (!c || n < 0 || !x || !dv || !dc || !xnew) return TP_ERR_ARG;
+  if (oc_bisect(c, n, const_cast<double*>(x), xnew, dc, dv, g, false) != 0) {
+    c->err = "OC bisection did not terminate";
+    return TP_ERR_TIMEOUT;
+  }
+  return sync_status(c);
+}
+
+}  // extern "C"

@@ -101,6 +101,11 @@ struct tp_ctx {
   // per node, coefficient-major: A[(nb*9 + c*3 + d)*nnodes + n])
   double* st[TP_MAXL] = {};
   float* stf[TP_MAXL] = {};
+  // on demand: levels >= 2 with the subspace-operator semantics (fixed
+  // columns kept), for the reference-signature entry points
+  double* st_sub[TP_MAXL] = {};
+  bool st_sub_valid[TP_MAXL] = {};
+  double* scratch_invD = nullptr;
 
   tp::Coarse coarse;
 
@@ -151,7 +156,7 @@ template <typename T> void fine_resid(tp_ctx* c, const T* E, const T* b, const T
 void fine_inv_diag(tp_ctx* c, double* invD);
 
 // levels >= 1 (assembled block stencils)
-template <typename T> void assemble_stencil(tp_ctx* c, int l, const T* E, const T* ke, T* st, double* invD);
+template <typename T> void assemble_stencil(tp_ctx* c, int l, const T* E, const T* ke, T* st, double* invD, int masked);
 template <typename T> void stencil_apply(tp_ctx* c, int l, const T* st, const T* in, T* out);
 template <typename T> void stencil_jacobi(tp_ctx* c, int l, const T* st, const T* invD, const T* b, const T* u, T* unew, T omega);
 template <typename T> void stencil_resid(tp_ctx* c, int l, const T* st, const T* b, const T* u, T* d);
@@ -185,6 +190,10 @@ void filter_fwd(tp_ctx* c, const double* x, double* out);
 void filter_adj(tp_ctx* c, double* v, double* tmp);
 void volume_partials(tp_ctx* c, const double* xphys, int* nblocks);
 int oc_update(tp_ctx* c, double g);   // bisection; leaves xnew, change and x <- xnew
+int oc_bisect(tp_ctx* c, long n, double* x, double* xnew, const double* dc, const double* dv, double g,
+              bool commit);
+void vec_change(tp_ctx* c, long n, double* x, const double* xnew);  // S_CHANGE, x <- xnew
+void vec_sum(tp_ctx* c, long n, const double* v, int slot);
 void element_sens(tp_ctx* c, const double* u, const double* w, double* out);
 int filter_fwd_blocks(const tp_ctx* c);
 void set_design_ke(const double* ke0_host);

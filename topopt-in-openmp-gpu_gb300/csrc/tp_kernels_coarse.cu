@@ -105,10 +105,9 @@ __global__ void assemble_kernel(CGeom g, const T* __restrict__ E, const T* __res
 }
 
 template <typename T>
-void assemble_stencil(tp_ctx* c, int l, const T* E, const T* ke, T* st, double* invD) {
+void assemble_stencil(tp_ctx* c, int l, const T* E, const T* ke, T* st, double* invD, int masked) {
   ProfScope ps(c, P_ASSEMBLE);
   const CGeom g = cgeom(c, l);
-  const int masked = l >= 2;
   const int nsub = g.ncell * g.ncell * g.ncell;
   const int threads = 256;
   if (nsub >= 32) {
@@ -120,8 +119,8 @@ void assemble_stencil(tp_ctx* c, int l, const T* E, const T* ke, T* st, double* 
   }
   TP_CHECK_LAUNCH(c, "assemble_stencil");
 }
-template void assemble_stencil<double>(tp_ctx*, int, const double*, const double*, double*, double*);
-template void assemble_stencil<float>(tp_ctx*, int, const float*, const float*, float*, double*);
+template void assemble_stencil<double>(tp_ctx*, int, const double*, const double*, double*, double*, int);
+template void assemble_stencil<float>(tp_ctx*, int, const float*, const float*, float*, double*, int);
 
 enum { S_APPLY = 0, S_JACOBI = 1, S_RESID = 2 };
 

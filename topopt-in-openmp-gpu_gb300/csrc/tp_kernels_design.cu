@@ -283,7 +283,7 @@ __global__ void oc_finish_kernel(const double* __restrict__ partials, int nb, do
 // final pass at the last lmid: xnew, max |x - xnew| partials, x <- xnew
 __global__ void oc_apply_kernel(long n, double* __restrict__ x, double* __restrict__ xnew,
                                 const double* __restrict__ dc, const double* __restrict__ dv,
-                                const double* __restrict__ scal, double* __restrict__ partials) {
+                                const double* __restrict__ scal, double* __restrict__ partials, int commit) {
   const double lmid = scal[S_LMID];
   double m = 0.0;
   for (long e = blockIdx.x * 256L + threadIdx.x; e < n; e += (long)gridDim.x * 256) {
@@ -291,7 +291,7 @@ __global__ void oc_apply_kernel(long n, double* __restrict__ x, double* __restri
     const double xn = oc_xnew(xo, dc[e], dv[e], lmid);
     xnew[e] = xn;
     m = fmax(m, fabs(xo - xn));
-    x[e] = xn;
+    if (commit) x[e] = xn;
   }
   m = bmax256(m);
   if (threadIdx.x == 0) partials[blockIdx.x] = m;
@@ -305,17 +305,19 @@ __global__ void oc_init_kernel(double* scal) {
   scal[S_LMID] = 0.0;
 }
 
-// returns 0 on success; -1 if the bisection did not finish within its cap
-int oc_update(tp_ctx* c, double g) {
+// Bisection over any n design variables; leaves xnew, S_CHANGE and, when
+// commit is set, x <- xnew. Returns 0, or -1 if the bisection did not finish
+// within its step cap.
+int oc_bisect(tp_ctx* c, long ne, double* x, double* xnew, const double* dc, const double* dv, double g,
+              bool commit) {
   ProfScope ps(c, P_DESIGN);
-  const long ne = (long)c->L[0].ex * c->L[0].ey * c->L[0].ez;
   const int nb = blocks_for(ne);
   oc_init_kernel<<<1, 1, 0, c->s>>>(c->d_scal);
   const int kBatch = 24, kMaxSteps = 240;
   int taken = 0;
   for (;;) {
     for (int q = 0; q < kBatch; q++) {
-      oc_step_kernel<<<nb, 256, 0, c->s>>>(ne, c->d_x, c->d_dc, c->d_dv, c->d_scal, c->d_red);
+      oc_step_kernel<<<nb, 256, 0, c->s>>>(ne, x, dc, dv, c->d_scal, c->d_red);
       oc_finish_kernel<<<1, 256, 0, c->s>>>(c->d_red, nb, c->d_scal, g);
     }
     taken += kBatch;
@@ -324,10 +326,43 @@ int oc_update(tp_ctx* c, double g) {
     if (c->h_scal[S_OCDONE] != 0.0) break;
     if (taken >= kMaxSteps) return -1;
   }
-  oc_apply_kernel<<<nb, 256, 0, c->s>>>(ne, c->d_x, c->d_xnew, c->d_dc, c->d_dv, c->d_scal, c->d_red);
+  oc_apply_kernel<<<nb, 256, 0, c->s>>>(ne, x, xnew, dc, dv, c->d_scal, c->d_red, commit ? 1 : 0);
   finish_sum(c, nb, S_CHANGE, 1);
   TP_CHECK_LAUNCH(c, "oc_update");
   return 0;
+}
+
+int oc_update(tp_ctx* c, double g) {
+  const long ne = (long)c->L[0].ex * c->L[0].ey * c->L[0].ez;
+  return oc_bisect(c, ne, c->d_x, c->d_xnew, c->d_dc, c->d_dv, g, true);
+}
+
+// max |x - xnew| into S_CHANGE, then x <- xnew (gpu_definitions.c:110-125)
+__global__ void change_kernel(long n, double* __restrict__ x, const double* __restrict__ xnew,
+                              double* __restrict__ partials) {
+  double m = 0.0;
+  for (long e = blockIdx.x * 256L + threadIdx.x; e < n; e += (long)gridDim.x * 256) {
+    m = fmax(m, fabs(x[e] - xnew[e]));
+    x[e] = xnew[e];
+  }
+  m = bmax256(m);
+  if (threadIdx.x == 0) partials[blockIdx.x] = m;
+}
+
+void vec_change(tp_ctx* c, long n, double* x, const double* xnew) {
+  ProfScope ps(c, P_DESIGN);
+  const int nb = blocks_for(n);
+  change_kernel<<<nb, 256, 0, c->s>>>(n, x, xnew, c->d_red);
+  finish_sum(c, nb, S_CHANGE, 1);
+  TP_CHECK_LAUNCH(c, "vec_change");
+}
+
+void vec_sum(tp_ctx* c, long n, const double* v, int slot) {
+  ProfScope ps(c, P_DESIGN);
+  const int nb = blocks_for(n);
+  sum_kernel<<<nb, 256, 0, c->s>>>(n, v, c->d_red);
+  finish_sum(c, nb, slot, 0);
+  TP_CHECK_LAUNCH(c, "vec_sum");
 }
 
 }  // namespace tp

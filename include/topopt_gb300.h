@@ -189,6 +189,22 @@ tp_status tp_vec_change(tp_ctx* c, long n, double* x_dev, const double* xnew_dev
 tp_status tp_oc_bisect(tp_ctx* c, long n, const double* x_dev, const double* dv_dev, const double* dc_dev,
                        double g, double* xnew_dev);
 
+/* Density-filter adjoint v <- H (v / Hs) without any device allocation and
+ * without a context; it has no counterpart in the reference. It is for callers
+ * that cannot call cudaMalloc: work recorded while a CUDA stream is being
+ * captured into a graph (allocation is not allowed during capture), and
+ * applications whose device memory belongs to another allocator or runtime.
+ * The caller passes v (device, nelx*nely*nelz doubles, overwritten in place)
+ * and a cudaStream_t (NULL = the default stream); the work is queued on that
+ * stream and the call returns without waiting. The intermediate v/Hs lives in
+ * a fixed 16 MiB device array compiled into the library, so grids above
+ * tp_filter_T_noalloc_max_elements() elements (2^21) are rejected with
+ * TP_ERR_ARG. The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress) and should come before any stream capture. All calls
+ * share the array: calls that overlap on the GPU race. */
+tp_status tp_filter_T_noalloc(int nelx, int nely, int nelz, double rmin, double* v_dev, void* stream);
+long tp_filter_T_noalloc_max_elements(void);
+
 /* Optional timing of kernel classes with CUDA events on the context's
  * stream (fine_apply_f64, fine_jacobi_f32, stencil, coarse_solve, ...).
  * tp_profile_get folds finished events into per-class launch counts and

@@ -49,6 +49,7 @@ def args_parse():
     ap.add_argument("--nl", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison pass")
+    ap.add_argument("--passes", default="ABC", help="GPU passes to run (A resident, B e2e, C FP64)")
     ap.add_argument("--cpu-budget", type=float, default=150.0, help="seconds of CPU work for the reference arm")
     ap.add_argument("--cpu-sample", default=None, help=argparse.SUPPRESS)  # internal: child process mode
     return ap.parse_args()
@@ -307,9 +308,12 @@ def main():
     all_a, timed_a, ms_a, wall_a, prof = design_pass(tp, torch, shape, a.nl, tp.TP_MIXED, W, K, profile=True,
                                                      barrier=barrier)
     clk = clocks.stop()
-    _, timed_b, ms_b, wall_b, _ = design_pass(tp, torch, shape, a.nl, tp.TP_MIXED, W, K, e2e=True, barrier=barrier)
+    wall_b = ms_a / 1000.0
+    if "B" in a.passes:
+        _, timed_b, ms_b, wall_b, _ = design_pass(tp, torch, shape, a.nl, tp.TP_MIXED, W, K, e2e=True,
+                                                  barrier=barrier)
     fp64 = None
-    if not a.no_fp64:
+    if not a.no_fp64 and "C" in a.passes:
         all_c, timed_c, ms_c, wall_c, _ = design_pass(tp, torch, shape, a.nl, tp.TP_FP64, W, K, barrier=barrier)
         cm = np.array([h.c for h in all_a])
         cd = np.array([h.c for h in all_c])

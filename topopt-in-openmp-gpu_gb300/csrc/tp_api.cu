@@ -384,7 +384,7 @@ tp_status tp_create(const tp_params* p, tp_ctx** out) {
   if (ok) ok = cuda_ok(c, cudaMallocHost(&c->h_scal, sizeof(double) * S_COUNT), "cudaMallocHost");
   if (ok) {
     coarse_alloc(c);
-    ok = c->coarse.band && c->coarse.dinv && c->coarse.vec && c->coarse.info;
+    ok = c->coarse.band && c->coarse.dinv && c->coarse.dinvT && c->coarse.lrow && c->coarse.vec && c->coarse.info;
     if (!ok) c->err = "coarse solver allocation failed";
   }
   if (!ok) {

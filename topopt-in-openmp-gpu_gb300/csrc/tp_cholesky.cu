@@ -23,7 +23,7 @@
 namespace tp {
 
 constexpr int NB = 32;    // factor panel width
-constexpr int NBS = 128;  // solve block size
+constexpr int NBS = 512;  // solve block size (largest)
 
 __host__ __device__ __forceinline__ long lmax(long a, long b) { return a > b ? a : b; }
 __host__ __device__ __forceinline__ long lmin(long a, long b) { return a < b ? a : b; }
@@ -63,19 +63,28 @@ void coarse_alloc(tp_ctx* c) {
   if (C.bw > C.n - 1) C.bw = std::max(1L, C.n - 1);
   C.band_elems = (size_t)C.n * (C.bw + 1) + 1;
   cudaMalloc(&C.band, C.band_elems * sizeof(double));
-  C.nbs = NBS;
-  C.nblk = (int)((C.n + NBS - 1) / NBS);
-  cudaMalloc(&C.dinv, (size_t)C.nblk * NBS * NBS * 2 * sizeof(double));
-  cudaMalloc(&C.vec, (size_t)C.n * 2 * sizeof(double));
+  C.nbs = (int)std::min((long)NBS, ((C.n + 31) / 32) * 32);
+  C.nblk = (int)((C.n + C.nbs - 1) / C.nbs);
+  const size_t dsz = (size_t)C.nblk * C.nbs * C.nbs;
+  const size_t lsz = (size_t)C.nblk * C.nbs * C.bw;
+  cudaMalloc(&C.dinv, dsz * sizeof(double));
+  cudaMalloc(&C.dinvT, dsz * sizeof(double));
+  cudaMalloc(&C.lrow, lsz * sizeof(double));
+  cudaMalloc(&C.vec, (size_t)C.n * 4 * sizeof(double));
+  C.rhs = C.vec + 2 * C.n;
+  C.sol = C.vec + 3 * C.n;
   cudaMalloc(&C.info, sizeof(int));
-  c->mem_bytes += (long)(C.band_elems + (size_t)C.nblk * NBS * NBS * 2 + C.n * 2) * 8;
+  c->mem_bytes += (long)(C.band_elems + 2 * dsz + lsz + C.n * 4) * 8;
 }
 
 void coarse_free(tp_ctx* c) {
   Coarse& C = c->coarse;
   cudaFree(C.band);
   cudaFree(C.dinv);
+  cudaFree(C.dinvT);
+  cudaFree(C.lrow);
   cudaFree(C.vec);
+  if (C.graph_exec) cudaGraphExecDestroy(C.graph_exec);
   cudaFree(C.info);
   C = Coarse();
 }
@@ -179,28 +188,99 @@ __global__ void syrk_kernel(double* __restrict__ B, long bw, long k, int nb, lon
   }
 }
 
-// inverse of each diagonal block: thread per column, forward substitution;
-// writes both column-major (dinv) and row-major (dinv + nblk*NBS*NBS) copies
-__global__ void dinv_kernel(const double* __restrict__ B, long bw, long n, int nblk, double* __restrict__ D) {
-  const int blk = blockIdx.y;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const long b0 = (long)blk * NBS;
-  const int s = (int)lmin((long)NBS, n - b0);
-  if (j >= NBS) return;
-  double* Dc = D + (long)blk * NBS * NBS;
-  double* Dr = D + (long)nblk * NBS * NBS + (long)blk * NBS * NBS;
-  for (int i = 0; i < NBS; i++) {
-    Dc[(long)j * NBS + i] = 0.0;
-    Dr[(long)i * NBS + j] = 0.0;
+// Inverse of each diagonal NBSxNBS block of L, one CTA per (block, 32-column
+// chunk): the chunk's columns X of L_bb^{-1} are found by blocked forward
+// substitution over 32-row chunks R,
+//   acc = E_R - sum_{S<R} L_RS X_S,    X_R = L_RR^{-1} acc (substitution),
+// with X kept in shared memory. Writes D (row-major) and D^T (row-major).
+constexpr int kDinvThreads = 256;
+
+__global__ void __launch_bounds__(kDinvThreads)
+    dinv_kernel(const double* __restrict__ B, long bw, long n, int nbs, double* __restrict__ D,
+                double* __restrict__ DT) {
+  extern __shared__ double smem[];
+  double* X = smem;                    // nbs x 33
+  double* Lt = X + (long)nbs * 33;     // 32 x 33
+  double* Acc = Lt + 32 * 33;          // 32 x 33
+  const int blk = blockIdx.y, cc = blockIdx.x, tid = threadIdx.x;
+  const long b0 = (long)blk * nbs;
+  const int s = (int)lmin((long)nbs, n - b0);
+  const int j0 = cc * 32;
+  double* Db = D + (long)blk * nbs * nbs;
+  double* DTb = DT + (long)blk * nbs * nbs;
+  const int a = tid >> 3, q0 = (tid & 7) * 4;
+  const int nR = (s + 31) / 32;
+  for (int R = cc; R < nR; R++) {
+    double acc[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) acc[q] = (R == cc && a == q0 + q) ? 1.0 : 0.0;
+    for (int S = cc; S < R; S++) {
+      for (int idx = tid; idx < 1024; idx += kDinvThreads) {
+        const int ra = idx & 31, cs = idx >> 5;
+        const long r = b0 + R * 32 + ra, col = b0 + S * 32 + cs;
+        Lt[ra * 33 + cs] = (R * 32 + ra < s) ? bget(B, bw, r, col) : 0.0;
+      }
+      __syncthreads();
+#pragma unroll 4
+      for (int t = 0; t < 32; t++) {
+        const double l = Lt[a * 33 + t];
+        const double* xr = X + (long)(S * 32 + t) * 33 + q0;
+#pragma unroll
+        for (int q = 0; q < 4; q++) acc[q] -= l * xr[q];
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) Acc[a * 33 + q0 + q] = acc[q];
+    for (int idx = tid; idx < 1024; idx += kDinvThreads) {
+      const int ra = idx & 31, cs = idx >> 5;
+      const long r = b0 + R * 32 + ra, col = b0 + R * 32 + cs;
+      Lt[ra * 33 + cs] = (R * 32 + ra < s && R * 32 + cs < s && ra >= cs) ? bget(B, bw, r, col) : 0.0;
+    }
+    __syncthreads();
+    if (tid < 32) {
+      const int col = tid;
+      for (int ra = 0; ra < 32; ra++) {
+        double v = Acc[ra * 33 + col];
+        for (int t = 0; t < ra; t++) v -= Lt[ra * 33 + t] * X[(long)(R * 32 + t) * 33 + col];
+        const double d = Lt[ra * 33 + ra];
+        X[(long)(R * 32 + ra) * 33 + col] = (R * 32 + ra < s && d != 0.0) ? v / d : 0.0;
+      }
+    }
+    __syncthreads();
   }
-  if (j >= s) return;
-  Dc[(long)j * NBS + j] = 1.0 / B[(b0 + j) * bw + (b0 + j)];
-  for (int i = j + 1; i < s; i++) {
+  // D[r][j0+col] for r in [0, nbs): zero above the diagonal chunk and past s
+  for (int idx = tid; idx < nbs * 32; idx += kDinvThreads) {
+    const int r = idx >> 5, col = idx & 31;
+    const double v = (r >= j0 && r < s && j0 + col < s) ? X[(long)r * 33 + col] : 0.0;
+    Db[(long)r * nbs + j0 + col] = v;
+  }
+  for (int idx = tid; idx < nbs * 32; idx += kDinvThreads) {
+    const int col = idx / nbs, r = idx % nbs;
+    const double v = (r >= j0 && r < s && j0 + col < s) ? X[(long)r * 33 + col] : 0.0;
+    DTb[(long)(j0 + col) * nbs + r] = v;
+  }
+}
+
+// row-major copy of the band rows of each block left of the block:
+// Lrow[blk][i][t] = L(b0 + i, b0 - bw + t), zero outside the band or the matrix
+__global__ void lrow_kernel(const double* __restrict__ B, long bw, long n, int nbs, double* __restrict__ Lrow) {
+  __shared__ double tile[32][33];
+  const int blk = blockIdx.z;
+  const long b0 = (long)blk * nbs;
+  const int i0 = blockIdx.y * 32, t0 = blockIdx.x * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  for (int k = ty; k < 32; k += 8) {
+    const long r = b0 + i0 + tx, col = b0 - bw + t0 + k;
     double v = 0.0;
-    for (int t = j; t < i; t++) v += bget(B, bw, b0 + i, b0 + t) * Dc[(long)j * NBS + t];
-    Dc[(long)j * NBS + i] = -v / B[(b0 + i) * bw + (b0 + i)];
+    if (i0 + tx < nbs && r < n && col >= 0 && t0 + k < bw) v = bget(B, bw, r, col);
+    tile[k][tx] = v;
   }
-  for (int i = j; i < s; i++) Dr[(long)i * NBS + j] = Dc[(long)j * NBS + i];
+  __syncthreads();
+  for (int k = ty; k < 32; k += 8) {
+    const int i = i0 + k, t = t0 + tx;
+    if (i < nbs && t < bw) Lrow[((long)blk * nbs + i) * bw + t] = tile[tx][k];
+  }
 }
 
 void coarse_factor(tp_ctx* c) {
@@ -218,49 +298,54 @@ void coarse_factor(tp_ctx* c) {
       syrk_kernel<<<(unsigned)(T * (T + 1) / 2), 256, 0, c->s>>>(C.band, C.bw, k, nb, R0, R1);
     }
   }
-  dinv_kernel<<<dim3(NBS / 64, C.nblk), 64, 0, c->s>>>(C.band, C.bw, C.n, C.nblk, C.dinv);
+  const size_t smem = ((size_t)C.nbs * 33 + 2 * 32 * 33) * sizeof(double);
+  cudaFuncSetAttribute(dinv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  dinv_kernel<<<dim3(C.nbs / 32, C.nblk), kDinvThreads, smem, c->s>>>(C.band, C.bw, C.n, C.nbs, C.dinv, C.dinvT);
+  lrow_kernel<<<dim3((unsigned)((C.bw + 31) / 32), C.nbs / 32, C.nblk), dim3(32, 8), 0, c->s>>>(C.band, C.bw, C.n,
+                                                                                               C.nbs, C.lrow);
   TP_CHECK_LAUNCH(c, "coarse_factor");
 }
 
 // ----------------------------------------------------------------------------
-// forward: t_r = b_r - sum_{c<b0} L(r,c) y_c for the rows of block blk (warp per row)
-__global__ void fwd_rows_kernel(const double* __restrict__ B, long bw, long n, int blk,
+// Block triangular solves, NBS rows per block, warp per row, coalesced:
+//   forward   t = b_k - Lrow_k y,   y_k = D_k t
+//   backward  t = y_k - L_{.,k}^T x (band columns are contiguous), x_k = D_k^T t
+__global__ void fwd_rows_kernel(const double* __restrict__ Lrow, long bw, long n, int nbs, int blk,
                                 const double* __restrict__ b, const double* __restrict__ y,
                                 double* __restrict__ t) {
-  const long b0 = (long)blk * NBS;
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  const long r = b0 + w;
-  if (w >= NBS || r >= n) return;
-  const long c0 = lmax(0L, r - bw);
+  const long b0 = (long)blk * nbs;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const long r = b0 + i;
+  if (i >= nbs || r >= n) return;
+  const long tlo = lmax(lmax(0L, bw - b0), (long)i);  // columns >= 0 and inside the band
+  const double* L = Lrow + ((long)blk * nbs + i) * bw;
+  const double* yy = y + (b0 - bw);
   double s = 0.0;
-  for (long cc = c0 + lane; cc < b0; cc += 32) s += B[cc * bw + r] * y[cc];
+  for (long q = tlo + lane; q < bw; q += 32) s += L[q] * yy[q];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   if (lane == 0) t[r] = b[r] - s;
 }
 
-// y_blk = Dinv_blk t_blk (column-major Dinv, thread per output row)
-__global__ void fwd_diag_kernel(const double* __restrict__ D, long n, int blk, const double* __restrict__ t,
+__global__ void fwd_diag_kernel(const double* __restrict__ D, long n, int nbs, int blk, const double* __restrict__ t,
                                 double* __restrict__ y) {
-  __shared__ double ts[NBS];
-  const long b0 = (long)blk * NBS;
-  const int i = threadIdx.x;
-  ts[i] = (b0 + i < n) ? t[b0 + i] : 0.0;
-  __syncthreads();
-  if (b0 + i >= n) return;
-  const double* Dc = D + (long)blk * NBS * NBS;
+  const long b0 = (long)blk * nbs;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (i >= nbs || b0 + i >= n) return;
+  const double* Dr = D + ((long)blk * nbs + i) * nbs;
+  const double* tt = t + b0;
   double s = 0.0;
-  for (int j = 0; j <= i; j++) s += Dc[(long)j * NBS + i] * ts[j];
-  y[b0 + i] = s;
+  for (int j = lane; j <= i; j += 32) s += Dr[j] * tt[j];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) y[b0 + i] = s;
 }
 
-// backward: t_r = y_r - sum_{c>=b1} L(c,r) x_c (warp per row)
-__global__ void bwd_rows_kernel(const double* __restrict__ B, long bw, long n, int blk,
+__global__ void bwd_rows_kernel(const double* __restrict__ B, long bw, long n, int nbs, int blk,
                                 const double* __restrict__ y, const double* __restrict__ x,
                                 double* __restrict__ t) {
-  const long b0 = (long)blk * NBS, b1 = lmin(n, b0 + NBS);
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  const long r = b0 + w;
-  if (w >= NBS || r >= n) return;
+  const long b0 = (long)blk * nbs, b1 = lmin(n, b0 + nbs);
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const long r = b0 + i;
+  if (i >= nbs || r >= n) return;
   const long c1 = lmin(n - 1, r + bw);
   double s = 0.0;
   for (long cc = b1 + lane; cc <= c1; cc += 32) s += B[r * bw + cc] * x[cc];
@@ -268,35 +353,66 @@ __global__ void bwd_rows_kernel(const double* __restrict__ B, long bw, long n, i
   if (lane == 0) t[r] = y[r] - s;
 }
 
-// x_blk = Dinv_blk^T t_blk (row-major copy, thread per output)
-__global__ void bwd_diag_kernel(const double* __restrict__ D, long n, int nblk, int blk,
+__global__ void bwd_diag_kernel(const double* __restrict__ DT, long n, int nbs, int blk,
                                 const double* __restrict__ t, double* __restrict__ x) {
-  __shared__ double ts[NBS];
-  const long b0 = (long)blk * NBS;
-  const int i = threadIdx.x;
-  ts[i] = (b0 + i < n) ? t[b0 + i] : 0.0;
-  __syncthreads();
-  if (b0 + i >= n) return;
-  const double* Dr = D + (long)nblk * NBS * NBS + (long)blk * NBS * NBS;
-  const int s = (int)lmin((long)NBS, n - b0);
+  const long b0 = (long)blk * nbs;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (i >= nbs || b0 + i >= n) return;
+  const int s = (int)lmin((long)nbs, n - b0);
+  const double* Dr = DT + ((long)blk * nbs + i) * nbs;
+  const double* tt = t + b0;
   double acc = 0.0;
-  for (int j = i; j < s; j++) acc += Dr[(long)j * NBS + i] * ts[j];
-  x[b0 + i] = acc;
+  for (int j = i + lane; j < s; j += 32) acc += Dr[j] * tt[j];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) x[b0 + i] = acc;
 }
 
-void coarse_solve(tp_ctx* c, const double* rhs, double* x) {
-  ProfScope ps(c, P_COARSE_SOLVE);
+// the launch sequence of one solve from C.rhs into C.sol
+static void coarse_solve_launches(tp_ctx* c) {
   Coarse& C = c->coarse;
   double* y = C.vec;
   double* t = C.vec + C.n;
+  const unsigned g = (unsigned)((C.nbs + 7) / 8);  // 8 warps per CTA, one row per warp
   for (int b = 0; b < C.nblk; b++) {
-    fwd_rows_kernel<<<NBS / 8, 256, 0, c->s>>>(C.band, C.bw, C.n, b, rhs, y, t);
-    fwd_diag_kernel<<<1, NBS, 0, c->s>>>(C.dinv, C.n, b, t, y);
+    const double* tin = C.rhs;
+    if (b > 0) {
+      fwd_rows_kernel<<<g, 256, 0, c->s>>>(C.lrow, C.bw, C.n, C.nbs, b, C.rhs, y, t);
+      tin = t;
+    }
+    fwd_diag_kernel<<<g, 256, 0, c->s>>>(C.dinv, C.n, C.nbs, b, tin, y);
   }
   for (int b = C.nblk - 1; b >= 0; b--) {
-    bwd_rows_kernel<<<NBS / 8, 256, 0, c->s>>>(C.band, C.bw, C.n, b, y, x, t);
-    bwd_diag_kernel<<<1, NBS, 0, c->s>>>(C.dinv, C.n, C.nblk, b, t, x);
+    const double* tin = y;
+    if (b < C.nblk - 1) {
+      bwd_rows_kernel<<<g, 256, 0, c->s>>>(C.band, C.bw, C.n, C.nbs, b, y, C.sol, t);
+      tin = t;
+    }
+    bwd_diag_kernel<<<g, 256, 0, c->s>>>(C.dinvT, C.n, C.nbs, b, tin, C.sol);
   }
+}
+
+// x = K_c^{-1} rhs; the block launches are captured once into a CUDA graph
+// (on the context's stream) and replayed
+void coarse_solve(tp_ctx* c, const double* rhs, double* x) {
+  ProfScope ps(c, P_COARSE_SOLVE);
+  Coarse& C = c->coarse;
+  cudaMemcpyAsync(C.rhs, rhs, sizeof(double) * C.n, cudaMemcpyDeviceToDevice, c->s);
+  if (!C.graph_exec) {
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      coarse_solve_launches(c);
+      if (cudaStreamEndCapture(c->s, &g) == cudaSuccess && g) {
+        if (cudaGraphInstantiate(&C.graph_exec, g, 0) != cudaSuccess) C.graph_exec = nullptr;
+        cudaGraphDestroy(g);
+      }
+    }
+    cudaGetLastError();
+  }
+  if (C.graph_exec)
+    cudaGraphLaunch(C.graph_exec, c->s);
+  else
+    coarse_solve_launches(c);
+  cudaMemcpyAsync(x, C.sol, sizeof(double) * C.n, cudaMemcpyDeviceToDevice, c->s);
   TP_CHECK_LAUNCH(c, "coarse_solve");
 }
 

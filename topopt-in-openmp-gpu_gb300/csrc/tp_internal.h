@@ -51,9 +51,14 @@ struct Coarse {
   double* band = nullptr;       // L(r,c) at c*bw + r, 0 <= r - c <= bw (column-major, ld = bw)
   size_t band_elems = 0;
   int nbs = 0, nblk = 0;        // solve block size and count
-  double* dinv = nullptr;       // inverse of each diagonal block of L, nbs*nbs per block (column-major)
-  double* vec = nullptr;        // work vector (n)
+  double* dinv = nullptr;       // inverse D_k of each diagonal block of L, row-major nbs*nbs per block
+  double* dinvT = nullptr;      // D_k^T, row-major
+  double* lrow = nullptr;       // row-major band rows left of each block: nbs x bw per block
+  double* vec = nullptr;        // work vectors: y, t, rhs, sol (n each)
+  double* rhs = nullptr;
+  double* sol = nullptr;
   int* info = nullptr;          // device status: first non-positive pivot + 1, 0 if none
+  cudaGraphExec_t graph_exec = nullptr;  // the captured block-solve sequence
 };
 
 // Kernel classes the optional CUDA-event profiler times (tp_profile_*).

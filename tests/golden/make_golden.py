@@ -86,6 +86,29 @@ def history(shape, nl, iters, flavour=64):
     return h
 
 
+def adjoint(shape=(64, 32, 32), nl=4):
+    """Sensitivities of the reference on i.i.d. U[0.01, 1] design variables
+    (numpy default_rng(0)) through the density filter, rmin 1.5 and 2.5: the
+    compliance, dc/dxPhys and dc/dx = H^T(dc/Hs), and dv = H^T(1/Hs). Only
+    seeded samples and norms of the element arrays are stored."""
+    R = Reference(*shape, nl)
+    n = R.nelem()
+    x = np.random.default_rng(0).uniform(0.01, 1.0, n)
+    idx = np.sort(np.random.default_rng(7).choice(n, 256, replace=False))
+    out = {"shape": np.array(shape), "nl": nl, "x_sum": x.sum(), "x_head": x[:16], "idx": idx}
+    F = R.load()
+    for tag, rmin in (("15", 1.5), ("25", 2.5)):
+        xp = R.filter(rmin, x)
+        u, it, rr = R.solve(xp, F, None, 4, F32(1e-5))
+        c, dc = R.compliance(xp, u)
+        dcdx = R.filter_T(rmin, dc)
+        dv = R.filter_T(rmin, np.ones(n))
+        out.update({"c_" + tag: c, "iters_" + tag: it, "dc_" + tag: dc[idx], "dcdx_" + tag: dcdx[idx],
+                    "dv_" + tag: dv[idx], "dcdx_norm_" + tag: np.linalg.norm(dcdx),
+                    "dc_norm_" + tag: np.linalg.norm(dc), "dv_sum_" + tag: dv.sum()})
+    return out
+
+
 def ke_fixture():
     R = Reference(8, 4, 4, 4)
     out = {}

@@ -139,10 +139,11 @@ def test_state_solve(case):
     ctx.assemble()
 
 
-HISTORIES = [("history_48x24x24_l3.npz", (48, 24, 24), 3), ("history_32x16x16_l4.npz", (32, 16, 16), 4)]
+HISTORIES = [("history_48x24x24_l3.npz", (48, 24, 24), 3), ("history_32x16x16_l4.npz", (32, 16, 16), 4),
+             ("history_128x64x64_l4.npz", (128, 64, 64), 4)]
 
 
-@pytest.mark.parametrize("name,shape,nl", HISTORIES, ids=["48x24x24_l3", "32x16x16_l4"])
+@pytest.mark.parametrize("name,shape,nl", HISTORIES, ids=["48x24x24_l3", "32x16x16_l4", "128x64x64_l4"])
 def test_design_history_fp64(cuda, name, shape, nl):
     g = golden(name)
     ctx = tp.TopOpt(*shape, nl)
@@ -156,7 +157,7 @@ def test_design_history_fp64(cuda, name, shape, nl):
     ctx.close()
 
 
-@pytest.mark.parametrize("name,shape,nl", HISTORIES, ids=["48x24x24_l3", "32x16x16_l4"])
+@pytest.mark.parametrize("name,shape,nl", HISTORIES, ids=["48x24x24_l3", "32x16x16_l4", "128x64x64_l4"])
 def test_design_history_mixed(cuda, name, shape, nl):
     g = golden(name)
     ctx = tp.TopOpt(*shape, nl, precision=tp.TP_MIXED)

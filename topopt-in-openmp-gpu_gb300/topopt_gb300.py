@@ -95,6 +95,8 @@ def load():
     L.tp_filter_T.argtypes = [V, P]
     L.tp_volume.argtypes = [V, ctypes.POINTER(D)]
     L.tp_oc_update.argtypes = [V, D, ctypes.POINTER(D)]
+    L.tp_set_cg.argtypes = [V, D, I, I, D]
+    L.tp_set_rmin.argtypes = [V, D]
     L.tp_design_iteration.argtypes = [V, ctypes.POINTER(TpIterInfo)]
     L.tp_run.argtypes = [V, I, ctypes.POINTER(TpIterInfo), ctypes.POINTER(I)]
     _lib = L
@@ -183,6 +185,16 @@ class TopOpt:
         out = np.zeros(n.value, np.int64)
         self._check(self.L.tp_fixed_dofs(self.ctx, level, out.ctypes.data_as(ctypes.c_void_p), ctypes.byref(n)))
         return out
+
+    def set_cg(self, cgtol, cgmax=1000, nswp=4, omega=0.6):
+        self._check(self.L.tp_set_cg(self.ctx, cgtol, cgmax, nswp, omega))
+
+    def set_rmin(self, rmin):
+        self._check(self.L.tp_set_rmin(self.ctx, rmin))
+
+    def set_field(self, name, t):
+        """Copies a float64 tensor (any device) into a context field."""
+        self.upload(name, t.detach().cpu().numpy())
 
     # operators on torch CUDA tensors
     def assemble(self):

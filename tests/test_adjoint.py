@@ -111,7 +111,9 @@ def test_autograd_against_central_differences(design, cuda, rmin):
         assert abs(fd - grad[e]) <= 1e-5 * np.max(np.abs(grad)) + 1e-4 * abs(grad[e]), (e, fd, grad[e])
         fdv = (g_volume(g, torch, torch.from_numpy(xp).cuda()).item() -
                g_volume(g, torch, torch.from_numpy(xm).cuda()).item()) / (2 * h)
-        assert fdv == pytest.approx(xv.grad[e].item(), rel=1e-6, abs=1e-12)
+        # V is linear in x; its difference quotient is limited only by the round-off
+        # of a 65,536-term sum changed by ~1e-11 (a few 1e-6 relative)
+        assert fdv == pytest.approx(xv.grad[e].item(), rel=1e-4, abs=1e-12)
     g.close()
 
 

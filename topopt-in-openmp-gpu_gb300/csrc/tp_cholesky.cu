@@ -74,6 +74,7 @@ void coarse_alloc(tp_ctx* c) {
   C.rhs = C.vec + 2 * C.n;
   C.sol = C.vec + 3 * C.n;
   cudaMalloc(&C.info, sizeof(int));
+  cudaMalloc(&C.linv, NB * NB * sizeof(double));
   c->mem_bytes += (long)(C.band_elems + 2 * dsz + lsz + C.n * 4) * 8;
 }
 
@@ -86,6 +87,7 @@ void coarse_free(tp_ctx* c) {
   cudaFree(C.vec);
   if (C.graph_exec) cudaGraphExecDestroy(C.graph_exec);
   cudaFree(C.info);
+  cudaFree(C.linv);
   C = Coarse();
 }
 
@@ -101,67 +103,90 @@ void coarse_assemble(tp_ctx* c) {
 }
 
 // ----------------------------------------------------------------------------
-__global__ void potrf_kernel(double* __restrict__ B, long bw, long k, int nb, int* info) {
-  __shared__ double S[NB][NB + 1];
-  const int tid = threadIdx.x;
-  for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
+// Factor the nb x nb diagonal block held (updated, lower part) in S with one
+// warp: L into S and into the band, and L^{-1} into Inv and linv_out
+// (row-major 32x32, zero above the diagonal). A non-positive pivot sets *info
+// (first column + 1) and is replaced by 1 so that the factor completes.
+__device__ void factor_diag_block(double* __restrict__ B, long bw, long k, int nb, double (*S)[NB + 1],
+                                  double (*Inv)[NB + 1], double* __restrict__ linv_out, int* info) {
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x < 32) {
+    for (int j = 0; j < nb; j++) {
+      if (lane == j) {
+        double d = S[j][j];
+        if (!(d > 0.0)) {
+          atomicCAS(info, 0, (int)(k + j + 1));
+          d = 1.0;
+        }
+        S[j][j] = sqrt(d);
+      }
+      __syncwarp();
+      if (lane > j && lane < nb) S[lane][j] /= S[j][j];
+      __syncwarp();
+      if (lane > j && lane < nb) {
+        const double lij = S[lane][j];
+        for (int t = j + 1; t <= lane; t++) S[lane][t] -= lij * S[t][j];
+      }
+      __syncwarp();
+    }
+    // column `lane` of L^{-1} by forward substitution
+    const int jc = lane;
+    for (int i = 0; i < NB; i++) Inv[i][jc] = 0.0;
+    if (jc < nb) {
+      Inv[jc][jc] = 1.0 / S[jc][jc];
+      for (int i = jc + 1; i < nb; i++) {
+        double v = 0.0;
+        for (int t = jc; t < i; t++) v += S[i][t] * Inv[t][jc];
+        Inv[i][jc] = -v / S[i][i];
+      }
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
+    const int r = idx % NB, cc = idx / NB;
+    if (r < nb && cc < nb && r >= cc && r - cc <= bw) B[(k + cc) * bw + (k + r)] = S[r][cc];
+    linv_out[r * NB + cc] = Inv[r][cc];
+  }
+}
+
+// the first diagonal block (later ones are factored inside syrk_kernel)
+__global__ void potrf_kernel(double* __restrict__ B, long bw, long k, int nb, double* __restrict__ linv, int* info) {
+  __shared__ double S[NB][NB + 1], Inv[NB][NB + 1];
+  for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
     const int r = idx % NB, cc = idx / NB;
     S[r][cc] = (r < nb && cc < nb && r >= cc) ? bget(B, bw, k + r, k + cc) : 0.0;
   }
   __syncthreads();
-  for (int j = 0; j < nb; j++) {
-    if (tid == 0) {
-      double d = S[j][j];
-      if (!(d > 0.0)) {
-        atomicCAS(info, 0, (int)(k + j + 1));
-        d = 1.0;
-      }
-      S[j][j] = sqrt(d);
-    }
-    __syncthreads();
-    for (int r = j + 1 + tid; r < nb; r += blockDim.x) S[r][j] /= S[j][j];
-    __syncthreads();
-    for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
-      const int r = idx % NB, cc = idx / NB;
-      if (cc > j && r >= cc && r < nb) S[r][cc] -= S[r][j] * S[cc][j];
-    }
-    __syncthreads();
-  }
-  for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
-    const int r = idx % NB, cc = idx / NB;
-    if (r < nb && cc < nb && r >= cc && r - cc <= bw) B[(k + cc) * bw + (k + r)] = S[r][cc];
-  }
+  factor_diag_block(B, bw, k, nb, S, Inv, linv, info);
 }
 
-// rows R0..R1 of panel columns k..k+nb-1: solve x L_kk^T = a, one thread per row
-__global__ void trsm_kernel(double* __restrict__ B, long bw, long k, int nb, long R0, long R1) {
-  __shared__ double S[NB][NB + 1];
-  for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
-    const int r = idx % NB, cc = idx / NB;
-    S[r][cc] = (r < nb && cc < nb && r >= cc) ? B[(k + cc) * bw + (k + r)] : 0.0;
-  }
+// panel rows R0..R1 of columns k..k+nb-1: L(r, k+t) = sum_{t'<=t} A(r, k+t') Linv(t, t');
+// one warp per row, lane t computes output t
+__global__ void trsm_kernel(double* __restrict__ B, long bw, long k, int nb, long R0, long R1,
+                            const double* __restrict__ linv) {
+  __shared__ double Li[NB][NB + 1];
+  for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) Li[idx / NB][idx % NB] = linv[idx];
   __syncthreads();
-  const long r = R0 + blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int w = threadIdx.x >> 5, t = threadIdx.x & 31;
+  const long r = R0 + (long)blockIdx.x * (blockDim.x >> 5) + w;
   if (r > R1) return;
-  double x[NB];
-  const long t0 = lmax(0L, r - k - bw);  // columns before t0 lie outside the band
+  const double a = (t < nb) ? bget(B, bw, r, k + t) : 0.0;
+  double x = 0.0;
 #pragma unroll
-  for (int t = 0; t < NB; t++) {
-    if (t >= nb) break;
-    double v = 0.0;
-    if (t >= t0) {
-      v = B[(k + t) * bw + r];
-      for (int tt = (int)t0; tt < t; tt++) v -= x[tt] * S[t][tt];
-      v /= S[t][t];
-      B[(k + t) * bw + r] = v;
-    }
-    x[t] = v;
+  for (int tp = 0; tp < NB; tp++) {
+    const double at = __shfl_sync(0xffffffffu, a, tp);
+    if (tp <= t) x += at * Li[t][tp];
   }
+  if (t < nb && r - (k + t) <= bw) B[(k + t) * bw + r] = x;
 }
 
-// A(r,c) -= sum_t L(r,k+t) L(c,k+t), R0 <= c <= r <= R1, 32x32 tiles
-__global__ void syrk_kernel(double* __restrict__ B, long bw, long k, int nb, long R0, long R1) {
+// A(r,c) -= sum_t L(r,k+t) L(c,k+t), R0 <= c <= r <= R1, 32x32 tiles. The CTA of
+// tile (0,0) -- the next diagonal block -- then factors it for the next step.
+__global__ void syrk_kernel(double* __restrict__ B, long bw, long n, long k, int nb, long R0, long R1,
+                            double* __restrict__ linv, int* info) {
   __shared__ double Lr[NB][33], Lc[NB][33];
+  __shared__ double S[NB][NB + 1], Inv[NB][NB + 1];
   // blockIdx.x -> lower-triangular tile (tr, tc)
   const long b = blockIdx.x;
   long tr = (long)((sqrt(8.0 * (double)b + 1.0) - 1.0) / 2.0);
@@ -176,6 +201,7 @@ __global__ void syrk_kernel(double* __restrict__ B, long bw, long k, int nb, lon
     Lc[t][tx] = (t < nb && cc <= R1) ? bget(B, bw, cc, k + t) : 0.0;
   }
   __syncthreads();
+  const bool diag_next = (b == 0);
   const long r = rb + tx;
 #pragma unroll
   for (int q = 0; q < 4; q++) {
@@ -184,7 +210,19 @@ __global__ void syrk_kernel(double* __restrict__ B, long bw, long k, int nb, lon
     double s = 0.0;
 #pragma unroll
     for (int t = 0; t < NB; t++) s += Lr[t][tx] * Lc[t][cy];
-    if (r <= R1 && cc <= R1 && cc <= r && r - cc <= bw) B[cc * bw + r] -= s;
+    double v = 0.0;
+    const bool upd = r <= R1 && cc <= R1 && cc <= r && r - cc <= bw;
+    if (upd) {
+      v = B[cc * bw + r] - s;
+      B[cc * bw + r] = v;
+    }
+    // entries of the next diagonal block that this step leaves alone keep their value
+    if (diag_next) S[tx][cy] = upd ? v : ((cc <= r && r < n) ? bget(B, bw, r, cc) : 0.0);
+  }
+  if (diag_next) {
+    __syncthreads();
+    const int nb2 = (int)lmin((long)NB, n - R0);
+    factor_diag_block(B, bw, R0, nb2, S, Inv, linv, info);
   }
 }
 
@@ -287,15 +325,15 @@ void coarse_factor(tp_ctx* c) {
   ProfScope ps(c, P_COARSE_FACTOR);
   Coarse& C = c->coarse;
   cudaMemsetAsync(C.info, 0, sizeof(int), c->s);
+  potrf_kernel<<<1, 256, 0, c->s>>>(C.band, C.bw, 0, (int)std::min((long)NB, C.n), C.linv, C.info);
   for (long k = 0; k < C.n; k += NB) {
     const int nb = (int)std::min((long)NB, C.n - k);
-    potrf_kernel<<<1, 256, 0, c->s>>>(C.band, C.bw, k, nb, C.info);
     const long R0 = k + nb, R1 = std::min(C.n - 1, k + nb - 1 + C.bw);
     if (R0 <= R1) {
       const long m = R1 - R0 + 1;
-      trsm_kernel<<<grid_for(m, 64), 64, 0, c->s>>>(C.band, C.bw, k, nb, R0, R1);
+      trsm_kernel<<<(unsigned)((m + 7) / 8), 256, 0, c->s>>>(C.band, C.bw, k, nb, R0, R1, C.linv);
       const long T = (m + 31) / 32;
-      syrk_kernel<<<(unsigned)(T * (T + 1) / 2), 256, 0, c->s>>>(C.band, C.bw, k, nb, R0, R1);
+      syrk_kernel<<<(unsigned)(T * (T + 1) / 2), 256, 0, c->s>>>(C.band, C.bw, C.n, k, nb, R0, R1, C.linv, C.info);
     }
   }
   const size_t smem = ((size_t)C.nbs * 33 + 2 * 32 * 33) * sizeof(double);

@@ -58,6 +58,7 @@ struct Coarse {
   double* rhs = nullptr;
   double* sol = nullptr;
   int* info = nullptr;          // device status: first non-positive pivot + 1, 0 if none
+  double* linv = nullptr;       // inverse of the current 32x32 diagonal block of the factor
   cudaGraphExec_t graph_exec = nullptr;  // the captured block-solve sequence
 };
 

@@ -311,7 +311,7 @@ static void destroy_buffers(tp_ctx* c) {
   F(c->d_x); F(c->d_xphys); F(c->d_xnew); F(c->d_dc); F(c->d_dv); F(c->d_hs);
   F(c->d_E); F(c->d_Ef); F(c->d_F); F(c->d_U);
   F(c->d_r); F(c->d_z); F(c->d_p); F(c->d_q);
-  F(c->d_red); F(c->d_scal); F(c->d_flag); F(c->scratch_invD);
+  F(c->d_red); F(c->d_scal); F(c->d_flag); F(c->scratch_invD); F(c->d_fw);
   if (c->h_scal) cudaFreeHost(c->h_scal);
   coarse_free(c);
   prof_destroy(c);

@@ -86,6 +86,7 @@ void coarse_free(tp_ctx* c) {
   cudaFree(C.lrow);
   cudaFree(C.vec);
   if (C.graph_exec) cudaGraphExecDestroy(C.graph_exec);
+  if (C.factor_exec) cudaGraphExecDestroy(C.factor_exec);
   cudaFree(C.info);
   cudaFree(C.linv);
   C = Coarse();
@@ -321,8 +322,7 @@ __global__ void lrow_kernel(const double* __restrict__ B, long bw, long n, int n
   }
 }
 
-void coarse_factor(tp_ctx* c) {
-  ProfScope ps(c, P_COARSE_FACTOR);
+static void coarse_factor_launches(tp_ctx* c, size_t dinv_smem) {
   Coarse& C = c->coarse;
   cudaMemsetAsync(C.info, 0, sizeof(int), c->s);
   potrf_kernel<<<1, 256, 0, c->s>>>(C.band, C.bw, 0, (int)std::min((long)NB, C.n), C.linv, C.info);
@@ -336,11 +336,33 @@ void coarse_factor(tp_ctx* c) {
       syrk_kernel<<<(unsigned)(T * (T + 1) / 2), 256, 0, c->s>>>(C.band, C.bw, C.n, k, nb, R0, R1, C.linv, C.info);
     }
   }
-  const size_t smem = ((size_t)C.nbs * 33 + 2 * 32 * 33) * sizeof(double);
-  cudaFuncSetAttribute(dinv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  dinv_kernel<<<dim3(C.nbs / 32, C.nblk), kDinvThreads, smem, c->s>>>(C.band, C.bw, C.n, C.nbs, C.dinv, C.dinvT);
+  dinv_kernel<<<dim3(C.nbs / 32, C.nblk), kDinvThreads, dinv_smem, c->s>>>(C.band, C.bw, C.n, C.nbs, C.dinv, C.dinvT);
   lrow_kernel<<<dim3((unsigned)((C.bw + 31) / 32), C.nbs / 32, C.nblk), dim3(32, 8), 0, c->s>>>(C.band, C.bw, C.n,
                                                                                                C.nbs, C.lrow);
+}
+
+// The launch sequence (about 2 per 32 columns) is captured once into a CUDA
+// graph on the context's stream and replayed at every design iteration.
+void coarse_factor(tp_ctx* c) {
+  ProfScope ps(c, P_COARSE_FACTOR);
+  Coarse& C = c->coarse;
+  const size_t smem = ((size_t)C.nbs * 33 + 2 * 32 * 33) * sizeof(double);
+  if (!C.factor_exec) {
+    cudaFuncSetAttribute(dinv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      coarse_factor_launches(c, smem);
+      if (cudaStreamEndCapture(c->s, &g) == cudaSuccess && g) {
+        if (cudaGraphInstantiate(&C.factor_exec, g, 0) != cudaSuccess) C.factor_exec = nullptr;
+        cudaGraphDestroy(g);
+      }
+    }
+    cudaGetLastError();
+  }
+  if (C.factor_exec)
+    cudaGraphLaunch(C.factor_exec, c->s);
+  else
+    coarse_factor_launches(c, smem);
   TP_CHECK_LAUNCH(c, "coarse_factor");
 }
 

@@ -59,7 +59,8 @@ struct Coarse {
   double* sol = nullptr;
   int* info = nullptr;          // device status: first non-positive pivot + 1, 0 if none
   double* linv = nullptr;       // inverse of the current 32x32 diagonal block of the factor
-  cudaGraphExec_t graph_exec = nullptr;  // the captured block-solve sequence
+  cudaGraphExec_t graph_exec = nullptr;   // the captured block-solve sequence
+  cudaGraphExec_t factor_exec = nullptr;  // the captured factorisation sequence
 };
 
 // Kernel classes the optional CUDA-event profiler times (tp_profile_*).
@@ -88,6 +89,7 @@ struct tp_ctx {
   double *d_x = nullptr, *d_xphys = nullptr, *d_xnew = nullptr, *d_dc = nullptr,
          *d_dv = nullptr, *d_hs = nullptr;
   double* d_E = nullptr;  // E(xPhys) per fine element
+  double* d_fw = nullptr; // filter weights per offset, (2*ceil(rmin))^3
   float* d_Ef = nullptr;
 
   // state: load and displacement (FP64), nrhs columns, column-contiguous

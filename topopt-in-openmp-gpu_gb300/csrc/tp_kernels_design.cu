@@ -5,6 +5,7 @@
 // (gpu_definitions.c:110-157). All FP64, all reductions two-pass and
 // order-fixed.
 #include <cmath>
+#include <vector>
 
 #include "tp_internal.h"
 
@@ -125,10 +126,14 @@ void element_sens(tp_ctx* c, const double* u, const double* w, double* out) {
 // ----------------------------------------------------------------------------
 // Filter neighbourhood: [i-(ceil(rmin)-1), i+ceil(rmin)] clipped to the grid
 // (stencil_optimization.c:254-269), weights max(0, rmin - |d|), loops in the
-// reference's x, z, y order.
+// reference's x, z, y order. The weight depends only on the offset, so it is
+// tabulated once per radius on the host (IEEE sqrt, the same bits as the
+// reference's expression) and zero weights are skipped, which leaves every
+// sum unchanged.
 struct FBox {
-  int cr;       // ceil(rmin)
-  double rmin;
+  int cr;               // ceil(rmin)
+  int side;             // 2*cr: offsets -(cr-1) .. cr
+  const double* w;      // side^3 weights, [(di+cr-1)*side + (dk+cr-1)]*side + (dj+cr-1)
 };
 
 __device__ __forceinline__ void box(int i, int n, int cr, int& lo, int& hi) {
@@ -151,13 +156,15 @@ __global__ void filter_kernel(DGeom g, FBox fb, const double* __restrict__ in, c
     box(j, g.ey, fb.cr, j0, j1);
     double o = 0.0, h = 0.0;
     for (int i2 = i0; i2 < i1; i2++)
-      for (int k2 = k0; k2 < k1; k2++)
+      for (int k2 = k0; k2 < k1; k2++) {
+        const double* wr = fb.w + ((i2 - i + fb.cr - 1) * fb.side + (k2 - k + fb.cr - 1)) * fb.side + (fb.cr - 1 - j);
+        const double* xr = in + ((long)i2 * g.ez + k2) * g.ey;
         for (int j2 = j0; j2 < j1; j2++) {
-          const unsigned d2 = (unsigned)((i - i2) * (i - i2) + (j - j2) * (j - j2) + (k - k2) * (k - k2));
-          const double wgt = fmax(0.0, fb.rmin - sqrt((double)d2));
+          const double wgt = __ldg(wr + j2);
           if (MODE == 0) h += wgt;
-          if (MODE != 0) o += wgt * in[((long)i2 * g.ez + k2) * g.ey + j2];
+          if (MODE != 0 && wgt != 0.0) o += wgt * xr[j2];
         }
+      }
     if (MODE == 0) out[e] = h;
     if (MODE == 1) {
       const double v = o / hs[e];
@@ -177,10 +184,31 @@ __global__ void div_kernel(long n, const double* __restrict__ v, const double* _
   if (e < n) t[e] = v[e] / hs[e];
 }
 
-static FBox fbox(const tp_ctx* c) { return FBox{(int)std::ceil(c->p.rmin), c->p.rmin}; }
+static FBox fbox(const tp_ctx* c) {
+  const int cr = (int)std::ceil(c->p.rmin);
+  return FBox{cr, 2 * cr, c->d_fw};
+}
 
+// (re)tabulates the weights of the context's radius and the row sums Hs
 void filter_hs(tp_ctx* c, double* hs) {
   ProfScope ps(c, P_DESIGN);
+  const int cr = (int)std::ceil(c->p.rmin), side = 2 * cr;
+  std::vector<double> w((size_t)side * side * side);
+  for (int di = -(cr - 1); di <= cr; di++)
+    for (int dk = -(cr - 1); dk <= cr; dk++)
+      for (int dj = -(cr - 1); dj <= cr; dj++) {
+        const unsigned d2 = (unsigned)(di * di + dj * dj + dk * dk);
+        const double v = c->p.rmin - std::sqrt((double)d2);
+        w[((size_t)(di + cr - 1) * side + (dk + cr - 1)) * side + (dj + cr - 1)] = v > 0.0 ? v : 0.0;
+      }
+  if (c->d_fw) cudaFree(c->d_fw);
+  c->d_fw = nullptr;
+  if (cudaMalloc(&c->d_fw, sizeof(double) * w.size()) != cudaSuccess) {
+    c->err = "cudaMalloc of the filter weights failed";
+    return;
+  }
+  cudaMemcpyAsync(c->d_fw, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice, c->s);
+  cudaStreamSynchronize(c->s);
   const DGeom g = dgeom(c);
   filter_kernel<0><<<blocks_for((long)g.ex * g.ey * g.ez), 256, 0, c->s>>>(g, fbox(c), nullptr, nullptr, hs, nullptr);
   TP_CHECK_LAUNCH(c, "filter_hs");

@@ -163,6 +163,17 @@ tp_status tp_run(tp_ctx* c, int max_iterations, tp_iter_info* hist, int* loops);
 tp_status tp_set_rmin(tp_ctx* c, double rmin);
 /* Changes the CG tolerance and cap and the smoother's sweeps and damping. */
 tp_status tp_set_cg(tp_ctx* c, double cgtol, int cgmax, int nswp, double omega);
+/* Level-0 kernel selection (no counterpart in the reference): variant 0 =
+ * the element-centric, sum-factorised kernel wherever its launch plan
+ * applies (nely <= 256, 16-byte aligned vectors), else the node-centric
+ * stencil; variant 1 = the node-centric stencil everywhere. */
+tp_status tp_set_fine_variant(tp_ctx* c, int variant);
+/* Times the element-centric kernel's launch shapes (z groups per CTA, x
+ * chunks) for each precision and fused mode on the context's grid and keeps
+ * the fastest. It overwrites the solver work vectors (not F, U, x, xPhys):
+ * call it before a solve, not inside one. ms_out (optional, 8 entries)
+ * receives the best time per (precision, mode). */
+tp_status tp_autotune(tp_ctx* c, double* ms_out);
 /* The reference's matrix-free subspace operator of any level >= 1
  * (stencil_methods.c:436-519): unlike tp_apply at levels >= 2, fixed columns
  * keep their coupling; fixed rows return the input. Level 0 = tp_apply. */

@@ -1,0 +1,116 @@
+"""The element-centric, sum-factorised level-0 kernel against the node-centric
+stencil and the oracle, through the C ABI, on grids that exercise its launch
+plan: y extents that are and are not multiples of the 32-thread warp (the
+columns shared by two warps go through shared memory), z extents that split
+unevenly into row groups, single-element-thick slabs, and a y extent past
+the kernel's envelope (falls back to the stencil)."""
+import numpy as np
+import pytest
+
+from conftest import relerr
+import topopt_gb300 as tp
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(16, 66, 6), (8, 32, 10), (12, 64, 4), (6, 8, 30), (10, 96, 2), (4, 256, 4), (4, 258, 4),
+          (2, 2, 2)]
+
+
+def _rand(g, seed):
+    rng = np.random.default_rng(seed)
+    return rng.uniform(0.01, 1.0, g.nelem()), rng.uniform(-1.0, 1.0, g.ndof(0))
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=["x".join(map(str, s)) for s in SHAPES])
+def test_apply_fp64_matches_stencil(cuda, shape):
+    torch = cuda
+    g = tp.TopOpt(*shape, 2)
+    x, u = _rand(g, 0)
+    g.upload("xphys", x)
+    ud = torch.from_numpy(u).cuda()
+    y_ec = g.apply(0, ud).cpu().numpy()
+    g.set_fine_variant(1)
+    y_nc = g.apply(0, ud).cpu().numpy()
+    assert relerr(y_ec, y_nc) < 1e-13
+    b = torch.from_numpy(np.random.default_rng(1).uniform(-1, 1, g.ndof(0))).cuda()
+    s_nc = g.smooth(0, 3, 0.6, b, ud).cpu().numpy()
+    g.set_fine_variant(0)
+    s_ec = g.smooth(0, 3, 0.6, b, ud).cpu().numpy()
+    assert relerr(s_ec, s_nc) < 1e-12
+    g.close()
+
+
+@pytest.mark.parametrize("shape", SHAPES[:4], ids=["x".join(map(str, s)) for s in SHAPES[:4]])
+def test_apply_against_oracle(cuda, shape):
+    from oracle import Oracle
+    torch = cuda
+    g = tp.TopOpt(*shape, 2)
+    x, u = _rand(g, 2)
+    g.upload("xphys", x)
+    y = g.apply(0, torch.from_numpy(u).cuda()).cpu().numpy()
+    assert relerr(y, Oracle(*shape, 2).apply(0, x, u)) < 1e-12
+    g.close()
+
+
+@pytest.mark.parametrize("shape", SHAPES[:3], ids=["x".join(map(str, s)) for s in SHAPES[:3]])
+def test_apply_fp32(cuda, shape):
+    torch = cuda
+    g = tp.TopOpt(*shape, 2, precision=tp.TP_MIXED)
+    x, u = _rand(g, 3)
+    g.upload("xphys", x)
+    g.assemble()
+    ud = torch.from_numpy(u).cuda()
+    y64 = g.apply(0, ud).cpu().numpy()
+    y32 = g.apply(0, ud.float()).double().cpu().numpy()
+    assert relerr(y32, y64) < 1e-5
+    g.set_fine_variant(1)
+    y32n = g.apply(0, ud.float()).double().cpu().numpy()
+    assert relerr(y32, y32n) < 1e-5
+    g.close()
+
+
+@pytest.mark.parametrize("prec", [tp.TP_FP64, tp.TP_MIXED], ids=["fp64", "mixed"])
+@pytest.mark.parametrize("shape", [(16, 64, 12), (8, 32, 10), (16, 66, 6)], ids=["16x64x12", "8x32x10", "16x66x6"])
+def test_vcycle_matches_stencil(cuda, shape, prec):
+    """One V-cycle: the fused Jacobi sweeps and the residual of level 0."""
+    torch = cuda
+    g = tp.TopOpt(*shape, 2, precision=prec)
+    x, _ = _rand(g, 5)
+    g.upload("xphys", x)
+    g.assemble()
+    r = torch.from_numpy(np.random.default_rng(6).uniform(-1, 1, g.ndof(0))).cuda()
+    z_ec = g.vcycle(r).cpu().numpy()
+    g.set_fine_variant(1)
+    z_nc = g.vcycle(r).cpu().numpy()
+    assert relerr(z_ec, z_nc) < (1e-12 if prec == tp.TP_FP64 else 1e-4)
+    g.close()
+
+
+def test_autotune_keeps_results(cuda):
+    torch = cuda
+    g = tp.TopOpt(16, 64, 12, 2, precision=tp.TP_MIXED)
+    x, u = _rand(g, 4)
+    g.upload("xphys", x)
+    g.assemble()
+    ud = torch.from_numpy(u).cuda()
+    y0 = g.apply(0, ud).cpu().numpy()
+    ms = g.autotune()
+    assert np.all(ms > 0) and np.all(ms < 1e3)
+    g.upload("xphys", x)
+    g.assemble()
+    y1 = g.apply(0, ud).cpu().numpy()
+    # every node is owned by one thread whatever the launch shape, with the
+    # same order of accumulation: the result is bit for bit the same
+    assert np.array_equal(y0, y1)
+    # the cantilever state solve with the tuned shapes and with the stencil
+    g.init_design()
+    g.upload("U", np.zeros(g.ndof(0)))
+    it, rr, st = g.solve()
+    assert st == 0 and rr < 1e-5
+    u_ec = g.download("U")
+    g.set_fine_variant(1)
+    g.upload("U", np.zeros(g.ndof(0)))
+    it1, rr1, st1 = g.solve()
+    assert st1 == 0 and it1 == it
+    assert relerr(u_ec, g.download("U")) < 1e-6
+    g.close()

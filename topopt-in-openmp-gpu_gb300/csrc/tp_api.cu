@@ -219,8 +219,7 @@ static tp_status pcg(tp_ctx* c, const double* b, double* u, int* iters, double* 
     finish_sum(c, nb, S_RHO, 0);
     if (iter > 0) cg_scalars(c, 0);
     cg_pupdate(c, n, z, p, iter == 0);
-    fine_apply_dot<double>(c, c->d_E, p, q);
-    finish_sum(c, fine_blocks(c), S_DPR, 0);
+    finish_sum(c, fine_apply_dot<double>(c, c->d_E, p, q), S_DPR, 0);
     cg_scalars(c, 1);
     cg_xr_update(c, n, u, r, p, q, &nb);
     finish_sum(c, nb, S_RNORM2, 0);
@@ -354,6 +353,7 @@ tp_status tp_create(const tp_params* p, tp_ctx** out) {
     if (l == 0) {
       set_fine_ke(ke.data());
       set_design_ke(ke.data());
+      c->ec_ok = set_fine_kz(ke.data(), nullptr);
     }
   }
   const bool mx = p->precision == TP_MIXED;
@@ -405,6 +405,7 @@ tp_status tp_create(const tp_params* p, tp_ctx** out) {
     cudaStreamSynchronize(c->s);
   }
   filter_hs(c, c->d_hs);
+  ec_default_plans(c);
   tp_status st = sync_check(c);
   *out = c;
   if (st != TP_OK) return st;

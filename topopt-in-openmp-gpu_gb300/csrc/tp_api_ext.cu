@@ -61,6 +61,12 @@ tp_status tp_set_cg(tp_ctx* c, double cgtol, int cgmax, int nswp, double omega) 
   return TP_OK;
 }
 
+tp_status tp_set_fine_variant(tp_ctx* c, int variant) {
+  if (!c || variant < 0 || variant > 1) return TP_ERR_ARG;
+  c->fine_variant = variant;
+  return TP_OK;
+}
+
 tp_status tp_apply_subspace(tp_ctx* c, int level, const double* in, double* out) {
   if (!c || level < 0 || level >= c->nl || !in || !out) return TP_ERR_ARG;
   if (level == 0) return tp_apply(c, 0, in, out);

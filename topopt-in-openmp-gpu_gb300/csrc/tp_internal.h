@@ -63,6 +63,22 @@ struct Coarse {
   cudaGraphExec_t factor_exec = nullptr;  // the captured factorisation sequence
 };
 
+// Launch plan of the element-centric level-0 kernel (tp_kernels_fine_ec.cu):
+// z groups of node rows (ngz groups of zbase or zbase + 1 rows), nzg groups
+// per CTA, ncx chunks of cx node planes along x, nyt threads along y.
+struct EcPlan {
+  bool ok = false;
+  int nyt = 0, nzg = 1, ngz = 0, zbase = 0, zextra = 0, ncx = 1, cx = 0;
+};
+struct EcGeom {
+  int nx, ny, nz, ex, ey, ez, lim;
+  int ngz, zbase, zextra, cx;
+  long vstride;               // distance between right-hand sides
+  int slab_bytes, own_bytes;  // shared memory per stage
+};
+// fused consumers of the level-0 operator
+enum { FM_APPLY = 0, FM_APPLY_DOT = 1, FM_JACOBI = 2, FM_RESID = 3 };
+
 // Kernel classes the optional CUDA-event profiler times (tp_profile_*).
 enum ProfId {
   P_FINE_APPLY_F64 = 0, P_FINE_JACOBI_F64, P_FINE_RESID_F64,
@@ -123,6 +139,12 @@ struct tp_ctx {
   double* h_scal = nullptr;  // pinned mirror
   int* d_flag = nullptr;     // device error flag (bounded waits)
 
+  // level-0 kernel selection: 0 element-centric where it applies, 1 the
+  // node-centric stencil everywhere; plans per precision and fused mode
+  int fine_variant = 0;
+  bool ec_ok = false;        // KZ built and its sparsity pattern verified
+  tp::EcPlan ec_f32[4], ec_f64[4];
+
   bool assembled = false;    // operators built for the current xPhys
   long mem_bytes = 0;
 
@@ -158,10 +180,16 @@ int fine_blocks(const tp_ctx* c);
 
 // level 0 (matrix-free hex8 stencil)
 template <typename T> void fine_apply(tp_ctx* c, const T* E, const T* in, T* out);
-template <typename T> void fine_apply_dot(tp_ctx* c, const T* E, const T* in, T* out);  // + <in,out> partials
+template <typename T> int fine_apply_dot(tp_ctx* c, const T* E, const T* in, T* out);  // + <in,out> partials; returns their count
 template <typename T> void fine_jacobi(tp_ctx* c, const T* E, const T* invD, const T* b, const T* u, T* unew, T omega);
 template <typename T> void fine_resid(tp_ctx* c, const T* E, const T* b, const T* u, T* d);
 void fine_inv_diag(tp_ctx* c, double* invD);
+// element-centric form (tp_kernels_fine_ec.cu): returns the number of CTAs
+// launched, or -1 when the plan or the pointers rule it out
+bool set_fine_kz(const double* ke0, double* kz_out);
+bool ec_plan(tp_ctx* c, int nzg, int ncx, EcPlan* p);
+void ec_default_plans(tp_ctx* c);
+template <typename T> int fine_ec(tp_ctx* c, int mode, const T* E, const T* in, T* out, const T* b, const T* invD, T omega);
 
 // levels >= 1 (assembled block stencils)
 template <typename T> void assemble_stencil(tp_ctx* c, int l, const T* E, const T* ke, T* st, double* invD, int masked);

@@ -21,6 +21,7 @@ __constant__ float c_ke0f[576];
 
 void set_fine_ke(const double* ke0) {
   float f[576];
+  set_fine_kz(ke0, nullptr);
   for (int i = 0; i < 576; i++) f[i] = (float)ke0[i];
   cudaMemcpyToSymbol(c_ke0, ke0, sizeof(double) * 576);
   cudaMemcpyToSymbol(c_ke0f, f, sizeof(float) * 576);
@@ -165,23 +166,33 @@ static dim3 fine_grid(const tp_ctx* c) {
   return dim3((L.ny + TY - 1) / TY, (L.nz + TZ - 1) / TZ, (L.nx + TX - 1) / TX);
 }
 
+// The element-centric kernel (tp_kernels_fine_ec.cu) takes every call it
+// has a plan for; this node-centric kernel covers the rest (y extents above
+// 256 elements, unaligned vectors) and serves as its cross-check.
 template <typename T>
 void fine_apply(tp_ctx* c, const T* E, const T* in, T* out) {
   ProfScope ps(c, sizeof(T) == 8 ? P_FINE_APPLY_F64 : P_FINE_APPLY_F32);
+  if (c->fine_variant == 0 && fine_ec<T>(c, FM_APPLY, E, in, out, nullptr, nullptr, T(0)) >= 0) return;
   fine_kernel<T, M_APPLY><<<fine_grid(c), dim3(TY, TZ, TX), 0, c->s>>>(geom(c), E, in, out, nullptr,
                                                                        nullptr, T(0), nullptr);
   TP_CHECK_LAUNCH(c, "fine_apply");
 }
 template <typename T>
-void fine_apply_dot(tp_ctx* c, const T* E, const T* in, T* out) {
+int fine_apply_dot(tp_ctx* c, const T* E, const T* in, T* out) {
   ProfScope ps(c, sizeof(T) == 8 ? P_FINE_APPLY_F64 : P_FINE_APPLY_F32);
+  if (c->fine_variant == 0) {
+    const int nb = fine_ec<T>(c, FM_APPLY_DOT, E, in, out, nullptr, nullptr, T(0));
+    if (nb >= 0) return nb;
+  }
   fine_kernel<T, M_APPLY_DOT><<<fine_grid(c), dim3(TY, TZ, TX), 0, c->s>>>(
       geom(c), E, in, out, nullptr, nullptr, T(0), c->d_red);
   TP_CHECK_LAUNCH(c, "fine_apply_dot");
+  return fine_blocks(c);
 }
 template <typename T>
 void fine_jacobi(tp_ctx* c, const T* E, const T* invD, const T* b, const T* u, T* unew, T omega) {
   ProfScope ps(c, sizeof(T) == 8 ? P_FINE_JACOBI_F64 : P_FINE_JACOBI_F32);
+  if (c->fine_variant == 0 && fine_ec<T>(c, FM_JACOBI, E, u, unew, b, invD, omega) >= 0) return;
   fine_kernel<T, M_JACOBI><<<fine_grid(c), dim3(TY, TZ, TX), 0, c->s>>>(geom(c), E, u, unew, b, invD,
                                                                         omega, nullptr);
   TP_CHECK_LAUNCH(c, "fine_jacobi");
@@ -189,6 +200,7 @@ void fine_jacobi(tp_ctx* c, const T* E, const T* invD, const T* b, const T* u, T
 template <typename T>
 void fine_resid(tp_ctx* c, const T* E, const T* b, const T* u, T* d) {
   ProfScope ps(c, sizeof(T) == 8 ? P_FINE_RESID_F64 : P_FINE_RESID_F32);
+  if (c->fine_variant == 0 && fine_ec<T>(c, FM_RESID, E, u, d, b, nullptr, T(0)) >= 0) return;
   fine_kernel<T, M_RESID><<<fine_grid(c), dim3(TY, TZ, TX), 0, c->s>>>(geom(c), E, u, d, b, nullptr,
                                                                        T(0), nullptr);
   TP_CHECK_LAUNCH(c, "fine_resid");
@@ -201,7 +213,7 @@ int fine_blocks(const tp_ctx* c) {
 
 template void fine_apply<double>(tp_ctx*, const double*, const double*, double*);
 template void fine_apply<float>(tp_ctx*, const float*, const float*, float*);
-template void fine_apply_dot<double>(tp_ctx*, const double*, const double*, double*);
+template int fine_apply_dot<double>(tp_ctx*, const double*, const double*, double*);
 template void fine_jacobi<double>(tp_ctx*, const double*, const double*, const double*, const double*, double*, double);
 template void fine_jacobi<float>(tp_ctx*, const float*, const float*, const float*, const float*, float*, float);
 template void fine_resid<double>(tp_ctx*, const double*, const double*, const double*, double*);

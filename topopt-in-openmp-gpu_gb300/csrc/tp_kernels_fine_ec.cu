@@ -1,0 +1,679 @@
+// Level-0 operator, element-centric and sum-factorised: the same
+// y = K(rho) u as the hex8 stencil of stencil_methods.c:7-428, with the same
+// fused consumers (CG matvec + dot, Jacobi sweep, residual), at about a third
+// of the arithmetic.
+//
+// Basis. Per axis, the two nodal values of an element edge are replaced by
+// their sum and difference. For the 8 nodes of an element this is the
+// transform T8[b][q] = prod_axes s(bit_b, offset_q) with s(0, .) = 1,
+// s(1, 0) = -1, s(1, 1) = +1, b = bx*4 + by*2 + bz; T8 T8^T = 8 I, so
+//   KE = T^T KZ T,   KZ = T KE T^T / 64   (T = T8 (x) I_3).
+// For the isotropic trilinear hexahedron KZ has 45 non-zeros out of 576 (row
+// and column b = 0 -- rigid translations -- vanish); the host checks that
+// pattern numerically when it builds KZ from KE. Per element the operator is
+// then: three butterfly stages forward (y, x, z), 45 multiply-adds, three
+// butterfly stages back, with E(rho) folded into the last accumulation.
+//
+// Schedule. One thread per element column in y (thread t <-> elements
+// ej = t); a thread owns node column t+1 (thread 0 also column 0), and a z
+// group of at most RMAX consecutive node rows. The CTA streams along x over
+// a chunk of node planes: element layer L (between planes L and L+1) is
+// computed from the two planes, its contributions complete plane L (which
+// already holds layer L-1's share, carried in registers) and start plane
+// L+1. Node planes of the CTA's rows (plus one halo row each side) and, for
+// the sweep, the b and invD rows are staged in shared memory by cp.async,
+// two planes ahead of the compute. The y-neighbour exchange is a warp
+// shuffle; the column shared by two warps goes through shared memory.
+// Halo work: one element row per z group and one element layer per x chunk
+// are computed twice.
+#include <algorithm>
+#include <cmath>
+
+#include "tp_internal.h"
+
+namespace tp {
+
+__constant__ double c_kz[45];
+__constant__ float c_kzf[45];
+
+template <typename T>
+__device__ __forceinline__ T kz(int i);
+template <>
+__device__ __forceinline__ double kz<double>(int i) { return c_kz[i]; }
+template <>
+__device__ __forceinline__ float kz<float>(int i) { return c_kzf[i]; }
+
+// (row, column) of the 45 non-zeros of KZ, row = 3*b + c, in the order the
+// kernel consumes them
+static const unsigned char kKzPattern[45][2] = {
+    {3, 3},   {3, 14},  {4, 4},   {4, 8},   {5, 5},   {5, 7},   {5, 12},  {6, 6},   {6, 13},
+    {9, 9},   {9, 16},  {9, 20},  {7, 5},   {7, 7},   {7, 12},  {10, 10}, {10, 15}, {8, 4},
+    {8, 8},   {11, 11}, {11, 18}, {12, 5},  {12, 7},  {12, 12}, {15, 10}, {15, 15}, {13, 6},
+    {13, 13}, {16, 9},  {16, 16}, {16, 20}, {14, 3},  {14, 14}, {17, 17}, {17, 19}, {18, 11},
+    {18, 18}, {21, 21}, {19, 17}, {19, 19}, {22, 22}, {20, 9},  {20, 16}, {20, 20}, {23, 23}};
+
+static int loc_node(int dx, int dy, int dz) { return dz * 4 + (dy ? (dx ? 1 : 0) : (dx ? 2 : 3)); }
+
+bool set_fine_kz(const double* ke0, double* kz_out) {
+  double t8[8][8];
+  for (int b = 0; b < 8; b++)
+    for (int dx = 0; dx < 2; dx++)
+      for (int dy = 0; dy < 2; dy++)
+        for (int dz = 0; dz < 2; dz++) {
+          const int bits[3] = {(b >> 2) & 1, (b >> 1) & 1, b & 1}, off[3] = {dx, dy, dz};
+          double w = 1.0;
+          for (int a = 0; a < 3; a++)
+            if (bits[a]) w *= off[a] ? 1.0 : -1.0;
+          t8[b][loc_node(dx, dy, dz)] = w;
+        }
+  static double KZ[24][24];
+  double mx = 0.0;
+  for (int b = 0; b < 8; b++)
+    for (int c = 0; c < 3; c++)
+      for (int b2 = 0; b2 < 8; b2++)
+        for (int c2 = 0; c2 < 3; c2++) {
+          double s = 0.0;
+          for (int q = 0; q < 8; q++)
+            for (int q2 = 0; q2 < 8; q2++) s += t8[b][q] * ke0[(3 * q + c) * 24 + 3 * q2 + c2] * t8[b2][q2];
+          KZ[3 * b + c][3 * b2 + c2] = s / 64.0;
+          mx = std::fmax(mx, std::fabs(s / 64.0));
+        }
+  bool in_pat[24][24] = {};
+  double v[45];
+  float vf[45];
+  for (int i = 0; i < 45; i++) {
+    in_pat[kKzPattern[i][0]][kKzPattern[i][1]] = true;
+    v[i] = KZ[kKzPattern[i][0]][kKzPattern[i][1]];
+    vf[i] = (float)v[i];
+  }
+  bool ok = mx > 0.0;
+  for (int r = 0; r < 24; r++)
+    for (int s = 0; s < 24; s++)
+      if (!in_pat[r][s] && std::fabs(KZ[r][s]) > 1e-12 * mx) ok = false;
+  if (kz_out)
+    for (int i = 0; i < 45; i++) kz_out[i] = v[i];
+  if (ok) {
+    cudaMemcpyToSymbol(c_kz, v, sizeof(v));
+    cudaMemcpyToSymbol(c_kzf, vf, sizeof(vf));
+  }
+  return ok;
+}
+
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, int bytes) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Stage the contiguous range [src, src + n) into buf (16-byte aligned) in
+// 16-byte chunks from the 16-byte boundary at or below src; element 0 lands
+// at buf + (src & 15). The last chunk copies only the bytes inside the range
+// (zero fill), so nothing past src + n is read. The caller guarantees that
+// the bytes between the boundary and src belong to the same allocation (its
+// base is 16-byte aligned).
+template <typename T>
+__device__ __forceinline__ void ec_stage(unsigned char* buf, const T* src, long n, int tid, int nthr) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(src);
+  const uintptr_t a0 = a & ~uintptr_t(15);
+  const uintptr_t ae = a + (uintptr_t)n * sizeof(T);
+  const int nch = (int)((ae - a0 + 15) >> 4);
+  for (int q = tid; q < nch; q += nthr) {
+    const uintptr_t s = a0 + ((uintptr_t)q << 4);
+    const uintptr_t rem = ae - s;
+    cp_async16(buf + ((size_t)q << 4), reinterpret_cast<const void*>(s), rem < 16 ? (int)rem : 16);
+  }
+}
+template <typename T>
+__device__ __forceinline__ const T* ec_view(const unsigned char* buf, const T* src) {
+  return reinterpret_cast<const T*>(buf + (reinterpret_cast<uintptr_t>(src) & 15));
+}
+
+__device__ __forceinline__ void ec_rows(const EcGeom& g, int gi, int& k0, int& k1) {
+  k0 = gi * g.zbase + min(gi, g.zextra);
+  k1 = k0 + g.zbase + (gi < g.zextra ? 1 : 0);
+}
+
+constexpr int EC_APPLY = FM_APPLY, EC_APPLY_DOT = FM_APPLY_DOT, EC_JACOBI = FM_JACOBI, EC_RESID = FM_RESID;
+
+template <typename T, int MODE, int RMAX>
+__global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restrict__ E, const T* __restrict__ in,
+                                                      T* __restrict__ out, const T* __restrict__ bv,
+                                                      const T* __restrict__ invD, T omega,
+                                                      double* __restrict__ partials) {
+  constexpr int NST = 3;  // slab stages: planes L, L+1 in use, L+2 in flight
+  constexpr bool HASB = (MODE == EC_JACOBI || MODE == EC_RESID);
+  constexpr bool HASD = (MODE == EC_JACOBI);
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int t = threadIdx.x, tz = threadIdx.y;
+  const int nyt = blockDim.x, nzg = blockDim.y;
+  const int nthr = nyt * nzg, tid = t + nyt * tz;
+  const int lane = t & 31, wy = t >> 5, nwy = nyt >> 5;
+  const int ny = g.ny, nz = g.nz, ey = g.ey, ez = g.ez;
+  const long row3 = 3L * ny;
+  {
+    const long rs = (long)blockIdx.z * g.vstride;
+    in += rs;
+    out += rs;
+    if (HASB) bv += rs;
+  }
+  const int gfirst = blockIdx.x * nzg;
+  const int glast = min(gfirst + nzg, g.ngz) - 1;
+  int K0, K1, k0 = 0, k1 = 0, dum;
+  ec_rows(g, gfirst, K0, dum);
+  ec_rows(g, glast, dum, K1);
+  const int gi = gfirst + tz;
+  const bool gact = gi <= glast;
+  if (gact) ec_rows(g, gi, k0, k1);
+  const int nrow = k1 - k0;
+  const int kmin = max(K0 - 1, 0), kmax = min(K1, nz - 1);
+  const long slab_n = (long)(kmax - kmin + 1) * row3;
+  const long own_n = (long)(K1 - K0) * row3;
+  const bool stage_own = g.own_bytes > 0;
+
+  const int i0 = blockIdx.y * g.cx;
+  const int i1 = min(i0 + g.cx, g.nx);
+  const int Ls = max(i0 - 1, 0), Le = min(i1, g.ex);  // element layers [Ls, Le), planes Ls..Le
+
+  unsigned char* sl = smem;
+  unsigned char* sb = sl + NST * g.slab_bytes;
+  unsigned char* sd = sb + 2 * g.own_bytes;
+  T* bnd_nb = reinterpret_cast<T*>(sd + 2 * g.own_bytes);  // [nzg][nwy][RMAX][6]
+  T* bnd_own = bnd_nb + nzg * nwy * RMAX * 6;              // [nzg][nwy][RMAX][6]
+  T* carry_b = bnd_own + nzg * nwy * RMAX * 6;             // [nzg][nwy + 1][RMAX][3]
+
+  auto slab_src = [&](int p) { return in + ((long)p * nz + kmin) * row3; };
+  auto own_src = [&](const T* v, int p) { return v + ((long)p * nz + K0) * row3; };
+  auto issue_slab = [&](int p) { ec_stage<T>(sl + (p % NST) * g.slab_bytes, slab_src(p), slab_n, tid, nthr); };
+  auto issue_own = [&](int p) {
+    if (HASB && stage_own) ec_stage<T>(sb + (p & 1) * g.own_bytes, own_src(bv, p), own_n, tid, nthr);
+    if (HASD && stage_own) ec_stage<T>(sd + (p & 1) * g.own_bytes, own_src(invD, p), own_n, tid, nthr);
+  };
+  // views: value of node row kr, column j, component c at [(kr - base row) * row3 + 3 j + c]
+  auto slab_at = [&](int p) { return ec_view<T>(sl + (p % NST) * g.slab_bytes, slab_src(p)); };
+
+  for (int q = tid; q < nzg * (nwy + 1) * RMAX * 3; q += nthr) carry_b[q] = T(0);
+
+  double dot = 0.0;
+  // one output component of plane P, node row kr, column j
+  auto epi = [&](const T* uP, const T* bP, const T* dP, int P, int kr, int j, int c, T y) {
+    if (P < i0) return;
+    const long li = (long)(kr - kmin) * row3 + 3 * j + c;
+    const long n3 = ((long)P * nz + kr) * row3 + 3 * j + c;
+    const T u = uP[li];
+    if (P == 0 && (j < g.lim || j >= ny - g.lim)) y = u;  // fixed DOF: identity row
+    if (MODE == EC_APPLY || MODE == EC_APPLY_DOT) out[n3] = y;
+    if (MODE == EC_APPLY_DOT) dot += (double)u * (double)y;
+    if (HASB) {
+      const long lo = (long)(kr - K0) * row3 + 3 * j + c;
+      const T b = stage_own ? bP[lo] : bv[n3];
+      if (MODE == EC_RESID) out[n3] = b - y;
+      if (MODE == EC_JACOBI) {
+        const T d = stage_own ? dP[lo] : invD[n3];
+        out[n3] = u + omega * d * (b - y);
+      }
+    }
+  };
+  auto own_at = [&](unsigned char* base, const T* v, int p) -> const T* {
+    if (!stage_own) return nullptr;
+    return ec_view<T>(base + (p & 1) * g.own_bytes, own_src(v, p));
+  };
+
+  issue_slab(Ls);
+  issue_slab(Ls + 1);
+  issue_own(Ls);
+  cp_async_commit();
+
+  T carry[RMAX][3];
+#pragma unroll
+  for (int r = 0; r < RMAX; r++) carry[r][0] = carry[r][1] = carry[r][2] = T(0);
+  const bool lact = gact && t < ey;
+
+  for (int L = Ls; L < Le; ++L) {
+    T Ev[RMAX + 1];
+#pragma unroll
+    for (int q = 0; q <= RMAX; q++) {
+      const int ek = k0 - 1 + q;
+      Ev[q] = (lact && q <= nrow && ek >= 0 && ek < ez) ? E[((long)L * ez + ek) * g.ey + t] : T(0);
+    }
+    if (L + 2 <= Le) issue_slab(L + 2);
+    if (L + 1 <= Le) issue_own(L + 1);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    const T* u0 = slab_at(L);
+    const T* u1 = slab_at(L + 1);
+    const T* bL = HASB ? own_at(sb, bv, L) : nullptr;
+    const T* dL = HASD ? own_at(sd, invD, L) : nullptr;
+
+    if (gact) {
+      // y and x butterflies of node row kr: X[(bx*2 + by)*3 + c]
+      auto xrow = [&](int kr, T* X) {
+        if (lact && kr >= 0 && kr < nz) {
+          const long o = (long)(kr - kmin) * row3 + 3 * t;
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            const T a0 = u0[o + c], a1 = u0[o + 3 + c], b0 = u1[o + c], b1 = u1[o + 3 + c];
+            const T s0 = a0 + a1, d0 = a1 - a0, s1 = b0 + b1, d1 = b1 - b0;
+            X[c] = s0 + s1;
+            X[3 + c] = d0 + d1;
+            X[6 + c] = s1 - s0;
+            X[9 + c] = d1 - d0;
+          }
+        } else {
+#pragma unroll
+          for (int a = 0; a < 12; a++) X[a] = T(0);
+        }
+      };
+      T Xp[12], Xn[12], accp[12], accn[12];
+      xrow(k0 - 1, Xp);
+#pragma unroll
+      for (int a = 0; a < 12; a++) accp[a] = T(0);
+#pragma unroll
+      for (int q = 0; q <= RMAX; q++) {
+        if (q > nrow) break;
+        const int ek = k0 - 1 + q;
+        xrow(ek + 1, Xn);
+        if (ek >= 0 && ek < ez) {
+          const T Ee = Ev[q];
+          T Z[24];
+#pragma unroll
+          for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+              // a = bx*2 + by  ->  b = bx*4 + by*2 + bz = 2a + bz
+              Z[(2 * a) * 3 + c] = Xp[a * 3 + c] + Xn[a * 3 + c];
+              Z[(2 * a + 1) * 3 + c] = Xn[a * 3 + c] - Xp[a * 3 + c];
+            }
+          // w = KZ Z, pairs (bz = 0, 1) of each (bx, by, c); node row ek takes
+          // E (w0 - w1), node row ek + 1 takes E (w0 + w1)
+          {
+            const T w1 = kz<T>(0) * Z[3] + kz<T>(1) * Z[14];
+            accp[0] -= Ee * w1;
+            accn[0] = Ee * w1;
+          }
+          {
+            const T w1 = kz<T>(2) * Z[4] + kz<T>(3) * Z[8];
+            accp[1] -= Ee * w1;
+            accn[1] = Ee * w1;
+          }
+          {
+            const T w1 = kz<T>(4) * Z[5] + kz<T>(5) * Z[7] + kz<T>(6) * Z[12];
+            accp[2] -= Ee * w1;
+            accn[2] = Ee * w1;
+          }
+          {
+            const T w0 = kz<T>(7) * Z[6] + kz<T>(8) * Z[13];
+            const T w1 = kz<T>(9) * Z[9] + kz<T>(10) * Z[16] + kz<T>(11) * Z[20];
+            accp[3] += Ee * (w0 - w1);
+            accn[3] = Ee * (w0 + w1);
+          }
+          {
+            const T w0 = kz<T>(12) * Z[5] + kz<T>(13) * Z[7] + kz<T>(14) * Z[12];
+            const T w1 = kz<T>(15) * Z[10] + kz<T>(16) * Z[15];
+            accp[4] += Ee * (w0 - w1);
+            accn[4] = Ee * (w0 + w1);
+          }
+          {
+            const T w0 = kz<T>(17) * Z[4] + kz<T>(18) * Z[8];
+            const T w1 = kz<T>(19) * Z[11] + kz<T>(20) * Z[18];
+            accp[5] += Ee * (w0 - w1);
+            accn[5] = Ee * (w0 + w1);
+          }
+          {
+            const T w0 = kz<T>(21) * Z[5] + kz<T>(22) * Z[7] + kz<T>(23) * Z[12];
+            const T w1 = kz<T>(24) * Z[10] + kz<T>(25) * Z[15];
+            accp[6] += Ee * (w0 - w1);
+            accn[6] = Ee * (w0 + w1);
+          }
+          {
+            const T w0 = kz<T>(26) * Z[6] + kz<T>(27) * Z[13];
+            const T w1 = kz<T>(28) * Z[9] + kz<T>(29) * Z[16] + kz<T>(30) * Z[20];
+            accp[7] += Ee * (w0 - w1);
+            accn[7] = Ee * (w0 + w1);
+          }
+          {
+            const T w0 = kz<T>(31) * Z[3] + kz<T>(32) * Z[14];
+            const T w1 = kz<T>(33) * Z[17] + kz<T>(34) * Z[19];
+            accp[8] += Ee * (w0 - w1);
+            accn[8] = Ee * (w0 + w1);
+          }
+          {
+            const T w0 = kz<T>(35) * Z[11] + kz<T>(36) * Z[18];
+            const T w1 = kz<T>(37) * Z[21];
+            accp[9] += Ee * (w0 - w1);
+            accn[9] = Ee * (w0 + w1);
+          }
+          {
+            const T w0 = kz<T>(38) * Z[17] + kz<T>(39) * Z[19];
+            const T w1 = kz<T>(40) * Z[22];
+            accp[10] += Ee * (w0 - w1);
+            accn[10] = Ee * (w0 + w1);
+          }
+          {
+            const T w0 = kz<T>(41) * Z[9] + kz<T>(42) * Z[16] + kz<T>(43) * Z[20];
+            const T w1 = kz<T>(44) * Z[23];
+            accp[11] += Ee * (w0 - w1);
+            accn[11] = Ee * (w0 + w1);
+          }
+        } else {
+#pragma unroll
+          for (int a = 0; a < 12; a++) accn[a] = T(0);
+        }
+        if (q >= 1) {
+          // node row ek = k0 + r is complete: x and y butterflies back
+          const int r = q - 1;
+          T own0[3], own1[3], nb0[3], nb1[3];
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            const T p0s = accp[c] - accp[6 + c], p0d = accp[3 + c] - accp[9 + c];
+            const T p1s = accp[c] + accp[6 + c], p1d = accp[3 + c] + accp[9 + c];
+            own0[c] = p0s + p0d;  // plane L,   column t + 1
+            own1[c] = p1s + p1d;  // plane L+1, column t + 1
+            nb0[c] = p0s - p0d;   // plane L,   column t
+            nb1[c] = p1s - p1d;   // plane L+1, column t
+          }
+          T rv0[3], rv1[3];
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            rv0[c] = __shfl_down_sync(0xffffffffu, nb0[c], 1);
+            rv1[c] = __shfl_down_sync(0xffffffffu, nb1[c], 1);
+          }
+          const int bo = ((tz * nwy + wy) * RMAX + r) * 6;
+          if (lane == 0) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+              bnd_nb[bo + c] = nb0[c];
+              bnd_nb[bo + 3 + c] = nb1[c];
+            }
+          }
+          if (lane == 31) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+              bnd_own[bo + c] = own0[c];
+              bnd_own[bo + 3 + c] = own1[c];
+            }
+          } else if (lact) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+              const T y = carry[r][c] + own0[c] + rv0[c];
+              carry[r][c] = own1[c] + rv1[c];
+              epi(u0, bL, dL, L, k0 + r, t + 1, c, y);
+            }
+          }
+        }
+#pragma unroll
+        for (int a = 0; a < 12; a++) {
+          Xp[a] = Xn[a];
+          accp[a] = accn[a];
+        }
+      }
+    }
+    __syncthreads();
+    // columns 0, 32, 64, ...: the own share of lane 31 of the warp on the
+    // left plus the share of lane 0 of the warp on the right
+    if (gact) {
+      const int ncb = ey / 32 + 1;
+      for (int it = t; it < ncb * nrow * 3; it += nyt) {
+        const int c = it % 3, r = (it / 3) % nrow, cb = it / (3 * nrow);
+        const int j = 32 * cb;
+        T o0 = T(0), o1 = T(0), n0 = T(0), n1 = T(0);
+        if (cb >= 1) {
+          const int bo = ((tz * nwy + cb - 1) * RMAX + r) * 6;
+          o0 = bnd_own[bo + c];
+          o1 = bnd_own[bo + 3 + c];
+        }
+        if (j < ey) {
+          const int bo = ((tz * nwy + cb) * RMAX + r) * 6;
+          n0 = bnd_nb[bo + c];
+          n1 = bnd_nb[bo + 3 + c];
+        }
+        T& cr = carry_b[((tz * (nwy + 1) + cb) * RMAX + r) * 3 + c];
+        const T y = cr + o0 + n0;
+        cr = o1 + n1;
+        epi(u0, bL, dL, L, k0 + r, j, c, y);
+      }
+    }
+    __syncthreads();
+  }
+  cp_async_wait<0>();
+  __syncthreads();
+  if (i1 == g.nx && gact) {
+    // last plane (x = nelx): only layer nelx-1 touches it, its share is the carry
+    const int P = g.ex;
+    const T* uP = slab_at(P);
+    const T* bP = HASB ? own_at(sb, bv, P) : nullptr;
+    const T* dP = HASD ? own_at(sd, invD, P) : nullptr;
+    if (lact && lane != 31) {
+#pragma unroll
+      for (int r = 0; r < RMAX; r++)
+        if (r < nrow)
+#pragma unroll
+          for (int c = 0; c < 3; c++) epi(uP, bP, dP, P, k0 + r, t + 1, c, carry[r][c]);
+    }
+    const int ncb = ey / 32 + 1;
+    for (int it = t; it < ncb * nrow * 3; it += nyt) {
+      const int c = it % 3, r = (it / 3) % nrow, cb = it / (3 * nrow);
+      epi(uP, bP, dP, P, k0 + r, 32 * cb, c, carry_b[((tz * (nwy + 1) + cb) * RMAX + r) * 3 + c]);
+    }
+  }
+  if (MODE == EC_APPLY_DOT) {
+    __shared__ double red[32];
+    for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
+    __syncthreads();
+    if (lane == 0) red[tid >> 5] = dot;
+    __syncthreads();
+    if (tid == 0) {
+      double s = 0.0;
+      for (int w = 0; w < nthr / 32; w++) s += red[w];
+      partials[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = s;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side: plan, shared-memory size, launch
+
+constexpr int kEcRmax = 5;
+
+static long roundup16(long b) { return (b + 15) / 16 * 16; }
+
+// shape-only part of the plan (no launch); false if the grid is outside the
+// kernel's envelope (nely + 1 columns in one CTA of at most 256 threads)
+bool ec_plan(tp_ctx* c, int nzg, int ncx, EcPlan* P) {
+  const Level& L = c->L[0];
+  EcPlan p;
+  p.nyt = (L.ey + 31) / 32 * 32;
+  if (p.nyt > 256 || L.ex < 1 || L.ey < 1 || L.ez < 1) return false;
+  p.nzg = std::max(1, std::min(nzg, 256 / p.nyt));
+  p.ngz = (L.nz + kEcRmax - 1) / kEcRmax;
+  p.zbase = L.nz / p.ngz;
+  p.zextra = L.nz % p.ngz;
+  if (p.zbase + (p.zextra > 0) > kEcRmax) return false;
+  p.ncx = std::max(1, std::min(ncx, L.nx));
+  p.cx = (L.nx + p.ncx - 1) / p.ncx;
+  p.ncx = (L.nx + p.cx - 1) / p.cx;
+  p.ok = true;
+  *P = p;
+  return true;
+}
+
+// Defaults before any tuning: FP32 (bandwidth-bound) aims at about three
+// CTAs per SM, FP64 (FP64-pipe-bound) at two; x chunks make up the count.
+void ec_default_plans(tp_ctx* c) {
+  int sms = 148;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  for (int m = 0; m < 4; m++) {
+    c->ec_f32[m] = EcPlan();
+    c->ec_f64[m] = EcPlan();
+  }
+  if (!c->ec_ok) return;
+  for (int prec = 0; prec < 2; prec++) {
+    EcPlan p;
+    const int nzg = prec == 0 ? 2 : 1;
+    if (!ec_plan(c, nzg, 1, &p)) return;
+    const int zctas = (p.ngz + p.nzg - 1) / p.nzg;
+    const int want = (prec == 0 ? 3 : 2) * sms;
+    ec_plan(c, nzg, (want + zctas - 1) / zctas, &p);
+    for (int m = 0; m < 4; m++) (prec == 0 ? c->ec_f32 : c->ec_f64)[m] = p;
+  }
+}
+
+static EcGeom ec_geom(const tp_ctx* c, const EcPlan& p, size_t tsize, bool own, long vstride) {
+  const Level& L = c->L[0];
+  EcGeom g;
+  g.nx = L.nx;
+  g.ny = L.ny;
+  g.nz = L.nz;
+  g.ex = L.ex;
+  g.ey = L.ey;
+  g.ez = L.ez;
+  g.lim = L.lim;
+  g.ngz = p.ngz;
+  g.zbase = p.zbase;
+  g.zextra = p.zextra;
+  g.cx = p.cx;
+  g.vstride = vstride;
+  const long rows = (long)p.nzg * (p.zbase + (p.zextra > 0 ? 1 : 0));
+  const long row_bytes = 3L * L.ny * (long)tsize;
+  g.slab_bytes = (int)roundup16((rows + 2) * row_bytes + 32);
+  g.own_bytes = own ? (int)roundup16(rows * row_bytes + 32) : 0;
+  return g;
+}
+
+static size_t ec_smem(const EcGeom& g, const EcPlan& p, size_t tsize) {
+  const int nwy = p.nyt / 32;
+  return 3 * (size_t)g.slab_bytes + 4 * (size_t)g.own_bytes +
+         tsize * (size_t)(2 * p.nzg * nwy * kEcRmax * 6 + p.nzg * (nwy + 1) * kEcRmax * 3);
+}
+
+template <typename T, int MODE>
+static int ec_launch(tp_ctx* c, const EcPlan& p, const T* E, const T* in, T* out, const T* b, const T* invD,
+                     T omega, int nrhs, long vstride) {
+  const bool own = (MODE == EC_JACOBI || MODE == EC_RESID) && sizeof(T) == 4;
+  const EcGeom g = ec_geom(c, p, sizeof(T), own, vstride);
+  const size_t smem = ec_smem(g, p, sizeof(T));
+  auto kern = fine_ec_kernel<T, MODE, kEcRmax>;
+  static size_t set_for = 0;  // largest size the attribute was raised to
+  if (smem > 48 * 1024 && smem > set_for) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+      c->err = "fine_ec: shared memory request of " + std::to_string(smem) + " bytes refused";
+      return 0;
+    }
+    set_for = smem;
+  }
+  const dim3 grid((unsigned)((p.ngz + p.nzg - 1) / p.nzg), (unsigned)p.ncx, (unsigned)nrhs);
+  kern<<<grid, dim3(p.nyt, p.nzg), smem, c->s>>>(g, E, in, out, b, invD, omega, c->d_red);
+  TP_CHECK_LAUNCH(c, "fine_ec");
+  return (int)(grid.x * grid.y * grid.z);
+}
+
+template <typename T>
+const EcPlan& ec_plan_for(const tp_ctx* c, int mode) {
+  return sizeof(T) == 8 ? c->ec_f64[mode] : c->ec_f32[mode];
+}
+
+static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+template <typename T>
+int fine_ec(tp_ctx* c, int mode, const T* E, const T* in, T* out, const T* b, const T* invD, T omega) {
+  const EcPlan& p = ec_plan_for<T>(c, mode);
+  if (!p.ok || !aligned16(in) || (b && !aligned16(b)) || (invD && !aligned16(invD))) return -1;
+  switch (mode) {
+    case EC_APPLY: return ec_launch<T, EC_APPLY>(c, p, E, in, out, b, invD, omega, 1, 0);
+    case EC_APPLY_DOT: return ec_launch<T, EC_APPLY_DOT>(c, p, E, in, out, b, invD, omega, 1, 0);
+    case EC_JACOBI: return ec_launch<T, EC_JACOBI>(c, p, E, in, out, b, invD, omega, 1, 0);
+    default: return ec_launch<T, EC_RESID>(c, p, E, in, out, b, invD, omega, 1, 0);
+  }
+}
+
+template int fine_ec<double>(tp_ctx*, int, const double*, const double*, double*, const double*, const double*,
+                             double);
+template int fine_ec<float>(tp_ctx*, int, const float*, const float*, float*, const float*, const float*, float);
+
+}  // namespace tp
+
+// ---------------------------------------------------------------------------
+// The small autotuner: for each precision and fused mode, time the candidate
+// launch shapes on the context's own grid and keep the fastest.
+namespace {
+
+template <typename T>
+float ec_time(tp_ctx* c, int mode, const tp::EcPlan& p, const T* E, const T* in, T* out, const T* b,
+              const T* d) {
+  using namespace tp;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  auto run = [&]() {
+    switch (mode) {
+      case FM_APPLY: return ec_launch<T, FM_APPLY>(c, p, E, in, out, b, d, T(0.6), 1, 0);
+      case FM_APPLY_DOT: return ec_launch<T, FM_APPLY_DOT>(c, p, E, in, out, b, d, T(0.6), 1, 0);
+      case FM_JACOBI: return ec_launch<T, FM_JACOBI>(c, p, E, in, out, b, d, T(0.6), 1, 0);
+      default: return ec_launch<T, FM_RESID>(c, p, E, in, out, b, d, T(0.6), 1, 0);
+    }
+  };
+  run();
+  cudaEventRecord(e0, c->s);
+  const int reps = 3;
+  for (int r = 0; r < reps; r++) run();
+  cudaEventRecord(e1, c->s);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return c->err.empty() ? ms / reps : 1e30f;
+}
+
+template <typename T>
+void ec_tune(tp_ctx* c, tp::EcPlan* plans, const T* E, const T* in, T* out, const T* b, const T* d, int sms,
+             double* ms_out) {
+  using namespace tp;
+  for (int mode = 0; mode < 4; mode++) {
+    EcPlan best = plans[mode];
+    float tbest = 1e30f;
+    for (int nzg = 1; nzg <= 4; nzg *= 2) {
+      EcPlan p;
+      if (!ec_plan(c, nzg, 1, &p) || p.nzg != nzg) continue;
+      const int zctas = (p.ngz + p.nzg - 1) / p.nzg;
+      int last_ncx = -1;
+      for (int mult = 1; mult <= 6; mult++) {
+        if (!ec_plan(c, nzg, (mult * sms + zctas - 1) / zctas, &p) || p.ncx == last_ncx) continue;
+        last_ncx = p.ncx;
+        const float ms = ec_time<T>(c, mode, p, E, in, out, b, d);
+        if (ms < tbest) {
+          tbest = ms;
+          best = p;
+        }
+      }
+    }
+    plans[mode] = best;
+    if (ms_out) ms_out[mode] = tbest;
+  }
+}
+
+}  // namespace
+
+extern "C" tp_status tp_autotune(tp_ctx* c, double* ms_out) {
+  using namespace tp;
+  if (!c) return TP_ERR_ARG;
+  if (ms_out)
+    for (int i = 0; i < 8; i++) ms_out[i] = 0.0;
+  if (!c->ec_ok || !c->ec_f64[0].ok) return TP_OK;
+  int sms = 148;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  ec_tune<double>(c, c->ec_f64, c->d_E, c->d_p, c->d_q, c->d_r, c->invD[0], sms, ms_out ? ms_out + 4 : nullptr);
+  if (c->mgf_r[0] && c->invDf[0])
+    ec_tune<float>(c, c->ec_f32, c->d_Ef, c->mgf_z[0], c->mgf_t[0], c->mgf_r[0], c->invDf[0], sms, ms_out);
+  cudaError_t e = cudaStreamSynchronize(c->s);
+  if (e != cudaSuccess) {
+    c->err = std::string("autotune: ") + cudaGetErrorString(e);
+    return TP_ERR_CUDA;
+  }
+  return c->err.empty() ? TP_OK : TP_ERR_CUDA;
+}

@@ -96,6 +96,8 @@ def load():
     L.tp_volume.argtypes = [V, ctypes.POINTER(D)]
     L.tp_oc_update.argtypes = [V, D, ctypes.POINTER(D)]
     L.tp_set_cg.argtypes = [V, D, I, I, D]
+    L.tp_set_fine_variant.argtypes = [V, I]
+    L.tp_autotune.argtypes = [V, P]
     L.tp_set_rmin.argtypes = [V, D]
     L.tp_design_iteration.argtypes = [V, ctypes.POINTER(TpIterInfo)]
     L.tp_run.argtypes = [V, I, ctypes.POINTER(TpIterInfo), ctypes.POINTER(I)]
@@ -188,6 +190,16 @@ class TopOpt:
 
     def set_cg(self, cgtol, cgmax=1000, nswp=4, omega=0.6):
         self._check(self.L.tp_set_cg(self.ctx, cgtol, cgmax, nswp, omega))
+
+    def set_fine_variant(self, variant):
+        """0: element-centric level-0 kernel where it applies; 1: node-centric stencil."""
+        self._check(self.L.tp_set_fine_variant(self.ctx, variant))
+
+    def autotune(self):
+        """Tunes the level-0 launch shapes; returns the best ms per (f32, f64) x mode."""
+        ms = np.zeros(8)
+        self._check(self.L.tp_autotune(self.ctx, ms.ctypes.data))
+        return ms
 
     def set_rmin(self, rmin):
         self._check(self.L.tp_set_rmin(self.ctx, rmin))

@@ -104,46 +104,75 @@ void coarse_assemble(tp_ctx* c) {
 }
 
 // ----------------------------------------------------------------------------
-// Factor the nb x nb diagonal block held (updated, lower part) in S with one
-// warp: L into S and into the band, and L^{-1} into Inv and linv_out
-// (row-major 32x32, zero above the diagonal). A non-positive pivot sets *info
-// (first column + 1) and is replaced by 1 so that the factor completes.
+// Factor the nb x nb diagonal block held (updated, lower part, zero above the
+// diagonal) in S with the 256 threads of the CTA: L into S and into the band,
+// and L^{-1} into Inv and linv_out (row-major 32x32, zero above the
+// diagonal). A non-positive pivot sets *info (first column + 1) and is
+// replaced by 1 so that the factor completes.
+//
+// This block lies on the factorisation's critical path (one per 32 columns),
+// and FP64 issue per SM is scarce on this part, so the work is spread over
+// all warps and the serial chain per column is kept to one multiply-add and
+// one reciprocal square root: thread (i, g) owns row i, columns g, g+8, g+16,
+// g+24; column j is updated unscaled (with 1/L(j,j)^2) and scaled one step
+// later; the owner of (j+1, j+1) forms the next pivot right after its last
+// update. L^{-1} follows by recursive doubling over diagonal blocks,
+// Inv_BA = -Inv_BB (L_BA Inv_AA), with Tm as scratch.
+__device__ __forceinline__ void diag_pivot(double (*S)[NB + 1], double* rp, int j, long k, int* info) {
+  double d = S[j][j];
+  if (!(d > 0.0)) {
+    atomicCAS(info, 0, (int)(k + j + 1));
+    d = 1.0;
+  }
+  const double r = rsqrt(d);
+  rp[j] = r;
+  S[j][j] = d * r;
+}
+
 __device__ void factor_diag_block(double* __restrict__ B, long bw, long k, int nb, double (*S)[NB + 1],
-                                  double (*Inv)[NB + 1], double* __restrict__ linv_out, int* info) {
-  const int lane = threadIdx.x & 31;
-  if (threadIdx.x < 32) {
-    for (int j = 0; j < nb; j++) {
-      if (lane == j) {
-        double d = S[j][j];
-        if (!(d > 0.0)) {
-          atomicCAS(info, 0, (int)(k + j + 1));
-          d = 1.0;
-        }
-        S[j][j] = sqrt(d);
-      }
-      __syncwarp();
-      if (lane > j && lane < nb) S[lane][j] /= S[j][j];
-      __syncwarp();
-      if (lane > j && lane < nb) {
-        const double lij = S[lane][j];
-        for (int t = j + 1; t <= lane; t++) S[lane][t] -= lij * S[t][j];
-      }
-      __syncwarp();
-    }
-    // column `lane` of L^{-1} by forward substitution
-    const int jc = lane;
-    for (int i = 0; i < NB; i++) Inv[i][jc] = 0.0;
-    if (jc < nb) {
-      Inv[jc][jc] = 1.0 / S[jc][jc];
-      for (int i = jc + 1; i < nb; i++) {
-        double v = 0.0;
-        for (int t = jc; t < i; t++) v += S[i][t] * Inv[t][jc];
-        Inv[i][jc] = -v / S[i][i];
+                                  double (*Inv)[NB + 1], double (*Tm)[NB + 1], double* __restrict__ linv_out,
+                                  int* info) {
+  __shared__ double rp[NB];
+  const int tid = threadIdx.x;
+  const int i = tid >> 3, g = tid & 7;
+  if (tid == 0) diag_pivot(S, rp, 0, k, info);
+  __syncthreads();
+  for (int j = 0; j < nb; j++) {
+    const double r2 = rp[j] * rp[j];
+    if (j >= 1 && g == 0 && i >= j && i < nb) S[i][j - 1] *= rp[j - 1];
+    if (i > j && i < nb) {
+      const double sij = S[i][j] * r2;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int t = g + 8 * q;
+        if (t > j && t <= i) S[i][t] -= sij * S[t][j];
       }
     }
-    __syncwarp();
+    if (j + 1 < nb && i == j + 1 && g == ((j + 1) & 7)) diag_pivot(S, rp, j + 1, k, info);
+    __syncthreads();
+  }
+  for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
+    const int r = idx / NB, cc = idx % NB;
+    Inv[r][cc] = (r == cc && r < nb) ? rp[r] : 0.0;
   }
   __syncthreads();
+  for (int s = 1; s < NB; s *= 2) {
+    const int ent = (NB / (2 * s)) * s * s;  // entries of all L_BA Inv_AA products
+    for (int e = tid; e < ent; e += blockDim.x) {
+      const int p = (e / (s * s)) * 2 * s, a = (e % (s * s)) / s, b = e % s;
+      double v = 0.0;
+      for (int m = b; m < s; m++) v += S[p + s + a][p + m] * Inv[p + m][p + b];
+      Tm[p + s + a][p + b] = v;
+    }
+    __syncthreads();
+    for (int e = tid; e < ent; e += blockDim.x) {
+      const int p = (e / (s * s)) * 2 * s, a = (e % (s * s)) / s, b = e % s;
+      double v = 0.0;
+      for (int m = 0; m <= a; m++) v += Inv[p + s + a][p + s + m] * Tm[p + s + m][p + b];
+      Inv[p + s + a][p + b] = -v;
+    }
+    __syncthreads();
+  }
   for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
     const int r = idx % NB, cc = idx / NB;
     if (r < nb && cc < nb && r >= cc && r - cc <= bw) B[(k + cc) * bw + (k + r)] = S[r][cc];
@@ -153,13 +182,13 @@ __device__ void factor_diag_block(double* __restrict__ B, long bw, long k, int n
 
 // the first diagonal block (later ones are factored inside syrk_kernel)
 __global__ void potrf_kernel(double* __restrict__ B, long bw, long k, int nb, double* __restrict__ linv, int* info) {
-  __shared__ double S[NB][NB + 1], Inv[NB][NB + 1];
+  __shared__ double S[NB][NB + 1], Inv[NB][NB + 1], Tm[NB][NB + 1];
   for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
     const int r = idx % NB, cc = idx / NB;
     S[r][cc] = (r < nb && cc < nb && r >= cc) ? bget(B, bw, k + r, k + cc) : 0.0;
   }
   __syncthreads();
-  factor_diag_block(B, bw, k, nb, S, Inv, linv, info);
+  factor_diag_block(B, bw, k, nb, S, Inv, Tm, linv, info);
 }
 
 // panel rows R0..R1 of columns k..k+nb-1: L(r, k+t) = sum_{t'<=t} A(r, k+t') Linv(t, t');
@@ -223,7 +252,7 @@ __global__ void syrk_kernel(double* __restrict__ B, long bw, long n, long k, int
   if (diag_next) {
     __syncthreads();
     const int nb2 = (int)lmin((long)NB, n - R0);
-    factor_diag_block(B, bw, R0, nb2, S, Inv, linv, info);
+    factor_diag_block(B, bw, R0, nb2, S, Inv, Lr, linv, info);
   }
 }
 

@@ -174,6 +174,23 @@ tp_status tp_set_fine_variant(tp_ctx* c, int variant);
  * call it before a solve, not inside one. ms_out (optional, 8 entries)
  * receives the best time per (precision, mode). */
 tp_status tp_autotune(tp_ctx* c, double* ms_out);
+/* Multi-load problem generator (no counterpart in the reference, whose one
+ * load is built at stencil_optimization.c:41-95): fills F_host (ncase columns
+ * of 3*(nelx+1)*(nely+1)*(nelz+1) doubles) with ncase load cases of nload unit
+ * nodal forces each, on distinct nodes of the free end face x = nelx drawn
+ * uniformly, directions uniform on the unit sphere; SplitMix64 from seed.
+ * Upload it as TP_FIELD_F of a context created with nrhs = ncase; the design
+ * loop then minimises the summed compliance of the cases. */
+tp_status tp_multiload(int nelx, int nely, int nelz, int ncase, int nload, unsigned long long seed,
+                       double* F_host);
+/* on = 1: tp_solve runs the CG loop as one CUDA graph launch (a conditional
+ * while node over the captured iteration) also for a single load; contexts
+ * with nrhs > 1 always do. No counterpart in the reference. */
+tp_status tp_set_graph_solve(tp_ctx* c, int on);
+/* Per load case of the last tp_solve: iters[r] = index of the CG iteration at
+ * which case r met the tolerance (-1 if it did not), relres[r] its relative
+ * residual then (nrhs entries each). */
+tp_status tp_solve_columns(tp_ctx* c, int* iters, double* relres);
 /* The reference's matrix-free subspace operator of any level >= 1
  * (stencil_methods.c:436-519): unlike tp_apply at levels >= 2, fixed columns
  * keep their coupling; fixed rows return the input. Level 0 = tp_apply. */

@@ -68,59 +68,60 @@ struct MG {
 };
 
 template <typename T>
-static void op_jacobi(tp_ctx* c, MG<T>& m, int l, const T* u, T* unew) {
+static void op_jacobi(tp_ctx* c, MG<T>& m, int l, const T* u, T* unew, int nr) {
   const T om = (T)c->p.omega;
   if (l == 0)
-    fine_jacobi<T>(c, m.E, m.invD[0], m.r[0], u, unew, om);
+    fine_jacobi<T>(c, m.E, m.invD[0], m.r[0], u, unew, om, nr);
   else
-    stencil_jacobi<T>(c, l, m.st[l], m.invD[l], m.r[l], u, unew, om);
+    stencil_jacobi<T>(c, l, m.st[l], m.invD[l], m.r[l], u, unew, om, nr);
 }
 template <typename T>
-static void op_resid(tp_ctx* c, MG<T>& m, int l, const T* u, T* d) {
+static void op_resid(tp_ctx* c, MG<T>& m, int l, const T* u, T* d, int nr) {
   if (l == 0)
-    fine_resid<T>(c, m.E, m.r[0], u, d);
+    fine_resid<T>(c, m.E, m.r[0], u, d, nr);
   else
-    stencil_resid<T>(c, l, m.st[l], m.r[l], u, d);
+    stencil_resid<T>(c, l, m.st[l], m.r[l], u, d, nr);
 }
 
 // coarsest correction in FP64 (rhs and solution through the double buffers
 // of the coarsest level)
-static void coarse_correct(tp_ctx* c, MG<double>& m, int lc) { coarse_solve(c, m.r[lc], m.z[lc]); }
-static void coarse_correct(tp_ctx* c, MG<float>& m, int lc) {
+static void coarse_correct(tp_ctx* c, MG<double>& m, int lc, int nr) { coarse_solve(c, m.r[lc], m.z[lc], nr); }
+static void coarse_correct(tp_ctx* c, MG<float>& m, int lc, int nr) {
   const long n = c->L[lc].ndof;
-  cast_f2d(c, n, m.r[lc], c->mg_r[lc]);
-  coarse_solve(c, c->mg_r[lc], c->mg_z[lc]);
-  cast_d2f(c, n, c->mg_z[lc], m.z[lc]);
+  cast_f2d(c, n * nr, m.r[lc], c->mg_r[lc]);
+  coarse_solve(c, c->mg_r[lc], c->mg_z[lc], nr);
+  cast_d2f(c, n * nr, c->mg_z[lc], m.z[lc]);
 }
 
 // One V(nswp, nswp) cycle from m.r[l] (stencil_solvers.c:129-252); the
 // result lands in m.z[l]. The pre-smoothing starts from z = 0, whose first
-// sweep needs no operator application (K*0 = 0, also at fixed DOFs).
+// sweep needs no operator application (K*0 = 0, also at fixed DOFs). nr
+// load cases go through together, each level's vectors holding nr columns.
 template <typename T>
-static void vcycle(tp_ctx* c, MG<T>& m, int l) {
+static void vcycle(tp_ctx* c, MG<T>& m, int l, int nr) {
   const long nd = c->L[l].ndof;
   const int nswp = c->p.nswp;
   // the sweeps alternate buffers 2*nswp - 1 times: start in t so z ends in z
   T* za = (nswp > 0) ? m.t[l] : m.z[l];
   T* zb = (nswp > 0) ? m.z[l] : m.t[l];
   if (nswp > 0) {
-    vscale<T>(c, nd, m.invD[l], m.r[l], za, (T)c->p.omega);
+    vscale<T>(c, nd, m.invD[l], m.r[l], za, (T)c->p.omega, nr);
     for (int s = 1; s < nswp; s++) {
-      op_jacobi<T>(c, m, l, za, zb);
+      op_jacobi<T>(c, m, l, za, zb, nr);
       std::swap(za, zb);
     }
   } else {
-    cudaMemsetAsync(za, 0, sizeof(T) * nd, c->s);
+    cudaMemsetAsync(za, 0, sizeof(T) * nd * nr, c->s);
   }
-  op_resid<T>(c, m, l, za, m.d[l]);
-  restrict_fw<T>(c, l, m.d[l], m.r[l + 1]);
+  op_resid<T>(c, m, l, za, m.d[l], nr);
+  restrict_fw<T>(c, l, m.d[l], m.r[l + 1], nr);
   if (l + 2 == c->nl)
-    coarse_correct(c, m, l + 1);
+    coarse_correct(c, m, l + 1, nr);
   else
-    vcycle<T>(c, m, l + 1);
-  prolong_add<T>(c, l, m.z[l + 1], za);
+    vcycle<T>(c, m, l + 1, nr);
+  prolong_add<T>(c, l, m.z[l + 1], za, nr);
   for (int s = 0; s < nswp; s++) {
-    op_jacobi<T>(c, m, l, za, zb);
+    op_jacobi<T>(c, m, l, za, zb, nr);
     std::swap(za, zb);
   }
 }
@@ -152,19 +153,19 @@ static MG<float> mg_float(tp_ctx* c) {
   return m;
 }
 
-// z = M^{-1} r on level 0 (FP64 in and out)
-static void precondition(tp_ctx* c, const double* r, double* z) {
+// z = M^{-1} r on level 0 (FP64 in and out), nr columns
+static void precondition(tp_ctx* c, const double* r, double* z, int nr = 1) {
   const long n = c->L[0].ndof;
   if (!mixed(c)) {
     MG<double> m = mg_double(c);
     m.r[0] = const_cast<double*>(r);  // read only on level 0
     m.z[0] = z;
-    vcycle<double>(c, m, 0);
+    vcycle<double>(c, m, 0, nr);
   } else {
     MG<float> m = mg_float(c);
-    cast_d2f(c, n, r, m.r[0]);
-    vcycle<float>(c, m, 0);
-    cast_f2d(c, n, m.z[0], z);
+    cast_d2f(c, n * nr, r, m.r[0]);
+    vcycle<float>(c, m, 0, nr);
+    cast_f2d(c, n * nr, m.z[0], z);
   }
 }
 
@@ -201,32 +202,48 @@ static tp_status assemble(tp_ctx* c) {
   return TP_OK;
 }
 
-// PCG (stencil_solvers.c:259-397) in FP64 for K u = b, warm start from u
-static tp_status pcg(tp_ctx* c, const double* b, double* u, int* iters, double* relres) {
+// PCG set-up: r = b - K u, |b|^2 per column, converged marks cleared
+void pcg_prologue(tp_ctx* c, const double* b, const double* u, int nr) {
+  const long n = c->L[0].ndof;
+  int nb = 0;
+  fine_resid<double>(c, c->d_E, b, u, c->d_r, nr);
+  dot_partials(c, n, b, b, &nb, nr);
+  finish_sum(c, nb, S_BNORM2, 0, nr);
+  cg_reset(c, nr);
+}
+
+// One PCG iteration over nr columns. iter >= 0 is the host's iteration
+// index; iter = -1 takes it from the device counter (the captured loop).
+void pcg_iteration(tp_ctx* c, double* u, int iter, int nr) {
   const long n = c->L[0].ndof;
   double *r = c->d_r, *z = c->d_z, *p = c->d_p, *q = c->d_q;
   int nb = 0;
-  fine_resid<double>(c, c->d_E, b, u, r);
-  dot_partials(c, n, b, b, &nb);
-  finish_sum(c, nb, S_BNORM2, 0);
+  precondition(c, r, z, nr);
+  dot_partials(c, n, r, z, &nb, nr);
+  finish_sum(c, nb, S_RHO, 0, nr);
+  if (iter != 0) cg_scalars(c, 0, nr);
+  cg_pupdate(c, n, z, p, iter < 0 ? -1 : (iter == 0), nr);
+  finish_sum(c, fine_apply_dot<double>(c, c->d_E, p, q, nr), S_DPR, 0, nr);
+  cg_scalars(c, 1, nr);
+  cg_xr_update(c, n, u, r, p, q, &nb, nr);
+  finish_sum(c, nb, S_RNORM2, 0, nr);
+  cg_scalars(c, 2, nr, c->p.cgtol, iter);
+}
+
+// PCG (stencil_solvers.c:259-397) in FP64 for K u = b, warm start from u,
+// host-driven: the largest relres of the nr columns is read back once per
+// iteration, as the reference reads its residual norm.
+static tp_status pcg(tp_ctx* c, const double* b, double* u, int* iters, double* relres, int nr = 1) {
+  pcg_prologue(c, b, u, nr);
   const double tol = c->p.cgtol;
   int it = 0;
   double rr = 0.0;
   bool converged = false;
   for (int iter = 0; iter < c->p.cgmax; iter++) {
-    precondition(c, r, z);
-    dot_partials(c, n, r, z, &nb);
-    finish_sum(c, nb, S_RHO, 0);
-    if (iter > 0) cg_scalars(c, 0);
-    cg_pupdate(c, n, z, p, iter == 0);
-    finish_sum(c, fine_apply_dot<double>(c, c->d_E, p, q), S_DPR, 0);
-    cg_scalars(c, 1);
-    cg_xr_update(c, n, u, r, p, q, &nb);
-    finish_sum(c, nb, S_RNORM2, 0);
-    cg_scalars(c, 2);
+    pcg_iteration(c, u, iter, nr);
     tp_status st = check(c);
     if (st != TP_OK) return st;
-    rr = read_scalar(c, S_RELRES);
+    rr = read_scalar(c, S_MAXRR);
     it = iter;
     if (!std::isfinite(rr)) {
       *iters = it;
@@ -312,6 +329,7 @@ static void destroy_buffers(tp_ctx* c) {
   F(c->d_r); F(c->d_z); F(c->d_p); F(c->d_q);
   F(c->d_red); F(c->d_scal); F(c->d_flag); F(c->scratch_invD); F(c->d_fw);
   if (c->h_scal) cudaFreeHost(c->h_scal);
+  graph_free(c);
   coarse_free(c);
   prof_destroy(c);
 }
@@ -322,7 +340,7 @@ tp_status tp_create(const tp_params* p, tp_ctx** out) {
   if (p->nl < 2 || p->nl > TP_MAXL || p->nelx < 1 || p->nely < 1 || p->nelz < 1) return TP_ERR_ARG;
   const int q = 1 << (p->nl - 1);
   if (p->nelx % q || p->nely % q || p->nelz % q) return TP_ERR_ARG;
-  if (p->nrhs != 1 || p->cgmax < 1 || p->nswp < 0 || !(p->rmin > 0)) return TP_ERR_ARG;
+  if (p->nrhs < 1 || p->nrhs > 16 || p->cgmax < 1 || p->nswp < 0 || !(p->rmin > 0)) return TP_ERR_ARG;
   if (p->precision != TP_FP64 && p->precision != TP_MIXED) return TP_ERR_ARG;
 
   tp_ctx* c = new tp_ctx();
@@ -357,31 +375,34 @@ tp_status tp_create(const tp_params* p, tp_ctx** out) {
     }
   }
   const bool mx = p->precision == TP_MIXED;
+  const long nv = L0.ndof * p->nrhs;
   ok = ok && (c->d_x = dalloc<double>(c, ne)) && (c->d_xphys = dalloc<double>(c, ne)) &&
        (c->d_xnew = dalloc<double>(c, ne)) && (c->d_dc = dalloc<double>(c, ne)) &&
        (c->d_dv = dalloc<double>(c, ne)) && (c->d_hs = dalloc<double>(c, ne)) &&
        (c->d_E = dalloc<double>(c, ne)) && (c->d_Ef = dalloc<float>(c, ne)) &&
-       (c->d_F = dalloc<double>(c, L0.ndof)) && (c->d_U = dalloc<double>(c, L0.ndof)) &&
-       (c->d_r = dalloc<double>(c, L0.ndof)) && (c->d_z = dalloc<double>(c, L0.ndof)) &&
-       (c->d_p = dalloc<double>(c, L0.ndof)) && (c->d_q = dalloc<double>(c, L0.ndof));
+       (c->d_F = dalloc<double>(c, nv)) && (c->d_U = dalloc<double>(c, nv)) &&
+       (c->d_r = dalloc<double>(c, nv)) && (c->d_z = dalloc<double>(c, nv)) &&
+       (c->d_p = dalloc<double>(c, nv)) && (c->d_q = dalloc<double>(c, nv));
+  // every solver vector holds one column per load case
   for (int l = 0; l < c->nl && ok; l++) {
-    const long nd = c->L[l].ndof;
+    const long nd = c->L[l].ndof, ndr = nd * p->nrhs;
     const bool coarsest = l == c->nl - 1;
     ok = (c->invD[l] = dalloc<double>(c, nd)) != nullptr;
     if (ok && (!mx || coarsest))
-      ok = (c->mg_r[l] = dalloc<double>(c, nd)) && (c->mg_z[l] = dalloc<double>(c, nd)) &&
-           (c->mg_d[l] = dalloc<double>(c, nd)) && (c->mg_t[l] = dalloc<double>(c, nd));
+      ok = (c->mg_r[l] = dalloc<double>(c, ndr)) && (c->mg_z[l] = dalloc<double>(c, ndr)) &&
+           (c->mg_d[l] = dalloc<double>(c, ndr)) && (c->mg_t[l] = dalloc<double>(c, ndr));
     if (ok && mx)
-      ok = (c->mgf_r[l] = dalloc<float>(c, nd)) && (c->mgf_z[l] = dalloc<float>(c, nd)) &&
-           (c->mgf_d[l] = dalloc<float>(c, nd)) && (c->mgf_t[l] = dalloc<float>(c, nd)) &&
+      ok = (c->mgf_r[l] = dalloc<float>(c, ndr)) && (c->mgf_z[l] = dalloc<float>(c, ndr)) &&
+           (c->mgf_d[l] = dalloc<float>(c, ndr)) && (c->mgf_t[l] = dalloc<float>(c, ndr)) &&
            (c->invDf[l] = dalloc<float>(c, nd));
     if (ok && l >= 1 && (!mx || coarsest)) ok = (c->st[l] = dalloc<double>(c, 243 * c->L[l].nnodes)) != nullptr;
     if (ok && l >= 1 && mx && !coarsest) ok = (c->stf[l] = dalloc<float>(c, 243 * c->L[l].nnodes)) != nullptr;
   }
-  const long red = std::max<long>(1 << 16, fine_blocks(c));
-  ok = ok && (c->d_red = dalloc<double>(c, red)) && (c->d_scal = dalloc<double>(c, S_COUNT)) &&
+  const long red = std::max<long>(1 << 16, (long)fine_blocks(c) * p->nrhs);
+  const long nscal = (long)S_COUNT * p->nrhs;
+  ok = ok && (c->d_red = dalloc<double>(c, red)) && (c->d_scal = dalloc<double>(c, nscal)) &&
        (c->d_flag = dalloc<int>(c, 4));
-  if (ok) ok = cuda_ok(c, cudaMallocHost(&c->h_scal, sizeof(double) * S_COUNT), "cudaMallocHost");
+  if (ok) ok = cuda_ok(c, cudaMallocHost(&c->h_scal, sizeof(double) * nscal), "cudaMallocHost");
   if (ok) {
     coarse_alloc(c);
     ok = c->coarse.band && c->coarse.dinv && c->coarse.dinvT && c->coarse.lrow && c->coarse.vec && c->coarse.info;
@@ -392,11 +413,12 @@ tp_status tp_create(const tp_params* p, tp_ctx** out) {
     *out = c;
     return TP_ERR_ALLOC;
   }
-  cudaMemsetAsync(c->d_scal, 0, sizeof(double) * S_COUNT, c->s);
-  cudaMemsetAsync(c->d_U, 0, sizeof(double) * L0.ndof, c->s);
+  cudaMemsetAsync(c->d_scal, 0, sizeof(double) * nscal, c->s);
+  cudaMemsetAsync(c->d_U, 0, sizeof(double) * nv, c->s);
+  cudaMemsetAsync(c->d_F, 0, sizeof(double) * nv, c->s);
   for (int l = 0; l < c->nl; l++) {
-    if (c->mg_z[l]) cudaMemsetAsync(c->mg_z[l], 0, sizeof(double) * c->L[l].ndof, c->s);
-    if (c->mgf_z[l]) cudaMemsetAsync(c->mgf_z[l], 0, sizeof(float) * c->L[l].ndof, c->s);
+    if (c->mg_z[l]) cudaMemsetAsync(c->mg_z[l], 0, sizeof(double) * c->L[l].ndof * p->nrhs, c->s);
+    if (c->mgf_z[l]) cudaMemsetAsync(c->mgf_z[l], 0, sizeof(float) * c->L[l].ndof * p->nrhs, c->s);
   }
   {
     std::vector<double> F(L0.ndof);
@@ -594,7 +616,7 @@ tp_status tp_solve(tp_ctx* c, int* iters, double* relres) {
   if (st != TP_OK) return st;
   int it = 0;
   double rr = 0;
-  st = pcg(c, c->d_F, c->d_U, &it, &rr);
+  st = (c->p.nrhs > 1 || c->graph_solve) ? pcg_graph(c, &it, &rr) : pcg(c, c->d_F, c->d_U, &it, &rr);
   if (iters) *iters = it;
   if (relres) *relres = rr;
   return st;
@@ -617,7 +639,7 @@ tp_status tp_solve_rhs(tp_ctx* c, const double* rhs, double* sol, int* iters, do
 tp_status tp_compliance(tp_ctx* c, double* c_out) {
   if (!c) return TP_ERR_ARG;
   int nb = 0;
-  compliance(c, c->d_U, c->d_dc, &nb);
+  compliance(c, c->d_U, c->d_dc, &nb, c->p.nrhs);
   finish_sum(c, nb, S_C, 0);
   tp_status st = check(c);
   if (st != TP_OK) return st;
@@ -701,7 +723,7 @@ tp_status tp_design_iteration(tp_ctx* c, tp_iter_info* info) {
   if (st != TP_OK) return st;
   double comp = 0;
   int nb = 0;
-  compliance(c, c->d_U, c->d_dc, &nb);
+  compliance(c, c->d_U, c->d_dc, &nb, c->p.nrhs);
   finish_sum(c, nb, S_C, 0);
   filter_adj(c, c->d_dc, c->d_xnew);
   const double g = vol - c->p.volfrac;

@@ -58,12 +58,14 @@ tp_status tp_set_cg(tp_ctx* c, double cgtol, int cgmax, int nswp, double omega) 
   c->p.cgmax = cgmax;
   c->p.nswp = nswp;
   c->p.omega = omega;
+  graph_free(c);  // the captured CG loop holds the old values
   return TP_OK;
 }
 
 tp_status tp_set_fine_variant(tp_ctx* c, int variant) {
   if (!c || variant < 0 || variant > 1) return TP_ERR_ARG;
   c->fine_variant = variant;
+  graph_free(c);
   return TP_OK;
 }
 

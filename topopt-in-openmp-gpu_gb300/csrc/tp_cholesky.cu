@@ -70,12 +70,13 @@ void coarse_alloc(tp_ctx* c) {
   cudaMalloc(&C.dinv, dsz * sizeof(double));
   cudaMalloc(&C.dinvT, dsz * sizeof(double));
   cudaMalloc(&C.lrow, lsz * sizeof(double));
-  cudaMalloc(&C.vec, (size_t)C.n * 4 * sizeof(double));
-  C.rhs = C.vec + 2 * C.n;
-  C.sol = C.vec + 3 * C.n;
+  // work columns: y and t, kSolveCols each, then rhs and sol of a single solve
+  cudaMalloc(&C.vec, (size_t)C.n * (2 * 8 + 2) * sizeof(double));
+  C.rhs = C.vec + 16 * C.n;
+  C.sol = C.vec + 17 * C.n;
   cudaMalloc(&C.info, sizeof(int));
   cudaMalloc(&C.linv, NB * NB * sizeof(double));
-  c->mem_bytes += (long)(C.band_elems + 2 * dsz + lsz + C.n * 4) * 8;
+  c->mem_bytes += (long)(C.band_elems + 2 * dsz + lsz + C.n * 18) * 8;
 }
 
 void coarse_free(tp_ctx* c) {
@@ -399,7 +400,15 @@ void coarse_factor(tp_ctx* c) {
 // Block triangular solves, NBS rows per block, warp per row, coalesced:
 //   forward   t = b_k - Lrow_k y,   y_k = D_k t
 //   backward  t = y_k - L_{.,k}^T x (band columns are contiguous), x_k = D_k^T t
-__global__ void fwd_rows_kernel(const double* __restrict__ Lrow, long bw, long n, int nbs, int blk,
+// Up to kSolveCols right-hand sides (columns n apart) share each load of L.
+constexpr int kSolveCols = 8;
+
+__device__ __forceinline__ double wsum(double s) {
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  return s;
+}
+
+__global__ void fwd_rows_kernel(const double* __restrict__ Lrow, long bw, long n, int nbs, int blk, int nr,
                                 const double* __restrict__ b, const double* __restrict__ y,
                                 double* __restrict__ t) {
   const long b0 = (long)blk * nbs;
@@ -409,26 +418,44 @@ __global__ void fwd_rows_kernel(const double* __restrict__ Lrow, long bw, long n
   const long tlo = lmax(lmax(0L, bw - b0), (long)i);  // columns >= 0 and inside the band
   const double* L = Lrow + ((long)blk * nbs + i) * bw;
   const double* yy = y + (b0 - bw);
-  double s = 0.0;
-  for (long q = tlo + lane; q < bw; q += 32) s += L[q] * yy[q];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  if (lane == 0) t[r] = b[r] - s;
+  double s[kSolveCols] = {};
+  for (long q = tlo + lane; q < bw; q += 32) {
+    const double l = L[q];
+#pragma unroll
+    for (int v = 0; v < kSolveCols; v++)
+      if (v < nr) s[v] += l * yy[v * n + q];
+  }
+#pragma unroll
+  for (int v = 0; v < kSolveCols; v++)
+    if (v < nr) {
+      const double sv = wsum(s[v]);
+      if (lane == 0) t[v * n + r] = b[v * n + r] - sv;
+    }
 }
 
-__global__ void fwd_diag_kernel(const double* __restrict__ D, long n, int nbs, int blk, const double* __restrict__ t,
-                                double* __restrict__ y) {
+__global__ void fwd_diag_kernel(const double* __restrict__ D, long n, int nbs, int blk, int nr,
+                                const double* __restrict__ t, double* __restrict__ y) {
   const long b0 = (long)blk * nbs;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (i >= nbs || b0 + i >= n) return;
   const double* Dr = D + ((long)blk * nbs + i) * nbs;
   const double* tt = t + b0;
-  double s = 0.0;
-  for (int j = lane; j <= i; j += 32) s += Dr[j] * tt[j];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  if (lane == 0) y[b0 + i] = s;
+  double s[kSolveCols] = {};
+  for (int j = lane; j <= i; j += 32) {
+    const double d = Dr[j];
+#pragma unroll
+    for (int v = 0; v < kSolveCols; v++)
+      if (v < nr) s[v] += d * tt[v * n + j];
+  }
+#pragma unroll
+  for (int v = 0; v < kSolveCols; v++)
+    if (v < nr) {
+      const double sv = wsum(s[v]);
+      if (lane == 0) y[v * n + b0 + i] = sv;
+    }
 }
 
-__global__ void bwd_rows_kernel(const double* __restrict__ B, long bw, long n, int nbs, int blk,
+__global__ void bwd_rows_kernel(const double* __restrict__ B, long bw, long n, int nbs, int blk, int nr,
                                 const double* __restrict__ y, const double* __restrict__ x,
                                 double* __restrict__ t) {
   const long b0 = (long)blk * nbs, b1 = lmin(n, b0 + nbs);
@@ -436,13 +463,22 @@ __global__ void bwd_rows_kernel(const double* __restrict__ B, long bw, long n, i
   const long r = b0 + i;
   if (i >= nbs || r >= n) return;
   const long c1 = lmin(n - 1, r + bw);
-  double s = 0.0;
-  for (long cc = b1 + lane; cc <= c1; cc += 32) s += B[r * bw + cc] * x[cc];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  if (lane == 0) t[r] = y[r] - s;
+  double s[kSolveCols] = {};
+  for (long cc = b1 + lane; cc <= c1; cc += 32) {
+    const double l = B[r * bw + cc];
+#pragma unroll
+    for (int v = 0; v < kSolveCols; v++)
+      if (v < nr) s[v] += l * x[v * n + cc];
+  }
+#pragma unroll
+  for (int v = 0; v < kSolveCols; v++)
+    if (v < nr) {
+      const double sv = wsum(s[v]);
+      if (lane == 0) t[v * n + r] = y[v * n + r] - sv;
+    }
 }
 
-__global__ void bwd_diag_kernel(const double* __restrict__ DT, long n, int nbs, int blk,
+__global__ void bwd_diag_kernel(const double* __restrict__ DT, long n, int nbs, int blk, int nr,
                                 const double* __restrict__ t, double* __restrict__ x) {
   const long b0 = (long)blk * nbs;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
@@ -450,46 +486,65 @@ __global__ void bwd_diag_kernel(const double* __restrict__ DT, long n, int nbs, 
   const int s = (int)lmin((long)nbs, n - b0);
   const double* Dr = DT + ((long)blk * nbs + i) * nbs;
   const double* tt = t + b0;
-  double acc = 0.0;
-  for (int j = i + lane; j < s; j += 32) acc += Dr[j] * tt[j];
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-  if (lane == 0) x[b0 + i] = acc;
+  double acc[kSolveCols] = {};
+  for (int j = i + lane; j < s; j += 32) {
+    const double d = Dr[j];
+#pragma unroll
+    for (int v = 0; v < kSolveCols; v++)
+      if (v < nr) acc[v] += d * tt[v * n + j];
+  }
+#pragma unroll
+  for (int v = 0; v < kSolveCols; v++)
+    if (v < nr) {
+      const double sv = wsum(acc[v]);
+      if (lane == 0) x[v * n + b0 + i] = sv;
+    }
 }
 
-// the launch sequence of one solve from C.rhs into C.sol
-static void coarse_solve_launches(tp_ctx* c) {
+// the launch sequence of one solve of nr columns from rhs into sol (y and t
+// are work columns of the same count)
+static void coarse_solve_launches(tp_ctx* c, const double* rhs, double* sol, double* y, double* t, int nr) {
   Coarse& C = c->coarse;
-  double* y = C.vec;
-  double* t = C.vec + C.n;
   const unsigned g = (unsigned)((C.nbs + 7) / 8);  // 8 warps per CTA, one row per warp
   for (int b = 0; b < C.nblk; b++) {
-    const double* tin = C.rhs;
+    const double* tin = rhs;
     if (b > 0) {
-      fwd_rows_kernel<<<g, 256, 0, c->s>>>(C.lrow, C.bw, C.n, C.nbs, b, C.rhs, y, t);
+      fwd_rows_kernel<<<g, 256, 0, c->s>>>(C.lrow, C.bw, C.n, C.nbs, b, nr, rhs, y, t);
       tin = t;
     }
-    fwd_diag_kernel<<<g, 256, 0, c->s>>>(C.dinv, C.n, C.nbs, b, tin, y);
+    fwd_diag_kernel<<<g, 256, 0, c->s>>>(C.dinv, C.n, C.nbs, b, nr, tin, y);
   }
   for (int b = C.nblk - 1; b >= 0; b--) {
     const double* tin = y;
     if (b < C.nblk - 1) {
-      bwd_rows_kernel<<<g, 256, 0, c->s>>>(C.band, C.bw, C.n, C.nbs, b, y, C.sol, t);
+      bwd_rows_kernel<<<g, 256, 0, c->s>>>(C.band, C.bw, C.n, C.nbs, b, nr, y, sol, t);
       tin = t;
     }
-    bwd_diag_kernel<<<g, 256, 0, c->s>>>(C.dinvT, C.n, C.nbs, b, tin, C.sol);
+    bwd_diag_kernel<<<g, 256, 0, c->s>>>(C.dinvT, C.n, C.nbs, b, nr, tin, sol);
   }
 }
 
-// x = K_c^{-1} rhs; the block launches are captured once into a CUDA graph
-// (on the context's stream) and replayed
-void coarse_solve(tp_ctx* c, const double* rhs, double* x) {
+// x = K_c^{-1} rhs for nr columns (n apart). Single solves replay a graph of
+// the block launches captured once on the context's stream; inside a stream
+// capture of a larger sequence (c->capturing) the launches are recorded
+// directly, in chunks of kSolveCols columns working in the caller's buffers
+// with the internal work columns.
+void coarse_solve(tp_ctx* c, const double* rhs, double* x, int nr) {
   ProfScope ps(c, P_COARSE_SOLVE);
   Coarse& C = c->coarse;
+  if (nr > 1 || c->capturing) {
+    for (int r0 = 0; r0 < nr; r0 += kSolveCols) {
+      const int k = std::min(kSolveCols, nr - r0);
+      coarse_solve_launches(c, rhs + (long)r0 * C.n, x + (long)r0 * C.n, C.vec, C.vec + (long)kSolveCols * C.n, k);
+    }
+    TP_CHECK_LAUNCH(c, "coarse_solve");
+    return;
+  }
   cudaMemcpyAsync(C.rhs, rhs, sizeof(double) * C.n, cudaMemcpyDeviceToDevice, c->s);
   if (!C.graph_exec) {
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-      coarse_solve_launches(c);
+      coarse_solve_launches(c, C.rhs, C.sol, C.vec, C.vec + C.n, 1);
       if (cudaStreamEndCapture(c->s, &g) == cudaSuccess && g) {
         if (cudaGraphInstantiate(&C.graph_exec, g, 0) != cudaSuccess) C.graph_exec = nullptr;
         cudaGraphDestroy(g);
@@ -500,7 +555,7 @@ void coarse_solve(tp_ctx* c, const double* rhs, double* x) {
   if (C.graph_exec)
     cudaGraphLaunch(C.graph_exec, c->s);
   else
-    coarse_solve_launches(c);
+    coarse_solve_launches(c, C.rhs, C.sol, C.vec, C.vec + C.n, 1);
   cudaMemcpyAsync(x, C.sol, sizeof(double) * C.n, cudaMemcpyDeviceToDevice, c->s);
   TP_CHECK_LAUNCH(c, "coarse_solve");
 }

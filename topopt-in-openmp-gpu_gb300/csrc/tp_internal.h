@@ -42,6 +42,10 @@ constexpr int kRedSlots = 4096;
 enum Scalar {
   S_RHO = 0, S_RHOOLD, S_ALPHA, S_BETA, S_DPR, S_RNORM2, S_BNORM2, S_RELRES,
   S_C, S_VOL, S_CHANGE, S_L1, S_L2, S_LMID, S_GT, S_OCDONE, S_TMP0, S_TMP1,
+  S_CONV,   // column converged (1) in the current solve
+  S_ITER,   // iteration at which it converged
+  S_MAXRR,  // (column 0) largest relres over the columns
+  S_IT,     // (column 0) iteration counter of the captured CG loop
   S_COUNT
 };
 
@@ -54,7 +58,7 @@ struct Coarse {
   double* dinv = nullptr;       // inverse D_k of each diagonal block of L, row-major nbs*nbs per block
   double* dinvT = nullptr;      // D_k^T, row-major
   double* lrow = nullptr;       // row-major band rows left of each block: nbs x bw per block
-  double* vec = nullptr;        // work vectors: y, t, rhs, sol (n each)
+  double* vec = nullptr;        // work columns: y (8), t (8), rhs, sol (n each)
   double* rhs = nullptr;
   double* sol = nullptr;
   int* info = nullptr;          // device status: first non-positive pivot + 1, 0 if none
@@ -148,6 +152,13 @@ struct tp_ctx {
   bool assembled = false;    // operators built for the current xPhys
   long mem_bytes = 0;
 
+  // the multi-load solve: one CUDA graph per context, a while-node looping
+  // over the captured CG iteration (tp_api_batch.cu)
+  bool capturing = false;    // launches are being recorded into a graph
+  cudaGraphExec_t cg_exec = nullptr;
+  int cg_exec_nr = 0;        // columns the captured graph solves
+  int graph_solve = 0;       // 1: tp_solve runs the captured graph also for one load
+
   // optional per-kernel-class timing with CUDA events on c->s
   bool prof = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -179,48 +190,50 @@ void compute_E(tp_ctx* c);  // d_E, d_Ef from d_xphys
 int fine_blocks(const tp_ctx* c);
 
 // level 0 (matrix-free hex8 stencil)
-template <typename T> void fine_apply(tp_ctx* c, const T* E, const T* in, T* out);
-template <typename T> int fine_apply_dot(tp_ctx* c, const T* E, const T* in, T* out);  // + <in,out> partials; returns their count
-template <typename T> void fine_jacobi(tp_ctx* c, const T* E, const T* invD, const T* b, const T* u, T* unew, T omega);
-template <typename T> void fine_resid(tp_ctx* c, const T* E, const T* b, const T* u, T* d);
+// nr: right-hand sides stored as consecutive columns of ndof(0) (E and invD are shared)
+template <typename T> void fine_apply(tp_ctx* c, const T* E, const T* in, T* out, int nr = 1);
+template <typename T> int fine_apply_dot(tp_ctx* c, const T* E, const T* in, T* out, int nr = 1);  // + <in,out> partials per column; returns their count per column
+template <typename T> void fine_jacobi(tp_ctx* c, const T* E, const T* invD, const T* b, const T* u, T* unew, T omega, int nr = 1);
+template <typename T> void fine_resid(tp_ctx* c, const T* E, const T* b, const T* u, T* d, int nr = 1);
 void fine_inv_diag(tp_ctx* c, double* invD);
 // element-centric form (tp_kernels_fine_ec.cu): returns the number of CTAs
 // launched, or -1 when the plan or the pointers rule it out
 bool set_fine_kz(const double* ke0, double* kz_out);
 bool ec_plan(tp_ctx* c, int nzg, int ncx, EcPlan* p);
 void ec_default_plans(tp_ctx* c);
-template <typename T> int fine_ec(tp_ctx* c, int mode, const T* E, const T* in, T* out, const T* b, const T* invD, T omega);
+template <typename T> int fine_ec(tp_ctx* c, int mode, const T* E, const T* in, T* out, const T* b, const T* invD, T omega, int nr = 1);
 
 // levels >= 1 (assembled block stencils)
 template <typename T> void assemble_stencil(tp_ctx* c, int l, const T* E, const T* ke, T* st, double* invD, int masked);
-template <typename T> void stencil_apply(tp_ctx* c, int l, const T* st, const T* in, T* out);
-template <typename T> void stencil_jacobi(tp_ctx* c, int l, const T* st, const T* invD, const T* b, const T* u, T* unew, T omega);
-template <typename T> void stencil_resid(tp_ctx* c, int l, const T* st, const T* b, const T* u, T* d);
+template <typename T> void stencil_apply(tp_ctx* c, int l, const T* st, const T* in, T* out, int nr = 1);
+template <typename T> void stencil_jacobi(tp_ctx* c, int l, const T* st, const T* invD, const T* b, const T* u, T* unew, T omega, int nr = 1);
+template <typename T> void stencil_resid(tp_ctx* c, int l, const T* st, const T* b, const T* u, T* d, int nr = 1);
 
 // grid transfer
-template <typename T> void restrict_fw(tp_ctx* c, int l, const T* fine, T* coarse);
-template <typename T> void prolong_add(tp_ctx* c, int l, const T* coarse, T* fine);
-template <typename T> void prolong_set(tp_ctx* c, int l, const T* coarse, T* fine);
+template <typename T> void restrict_fw(tp_ctx* c, int l, const T* fine, T* coarse, int nr = 1);
+template <typename T> void prolong_add(tp_ctx* c, int l, const T* coarse, T* fine, int nr = 1);
+template <typename T> void prolong_set(tp_ctx* c, int l, const T* coarse, T* fine, int nr = 1);
 
 // vectors
-template <typename T> void vscale(tp_ctx* c, long n, const T* a, const T* b, T* out, T omega);  // out = omega*a*b
-void dot_partials(tp_ctx* c, long n, const double* a, const double* b, int* nblocks);
-void finish_sum(tp_ctx* c, int nblocks, int slot, int op);  // sum partials into d_scal[slot]
+template <typename T> void vscale(tp_ctx* c, long n, const T* a, const T* b, T* out, T omega, int nr = 1);  // out = omega*a*b
+void dot_partials(tp_ctx* c, long n, const double* a, const double* b, int* nblocks, int nr = 1);
+void finish_sum(tp_ctx* c, int nblocks, int slot, int op, int nr = 1);  // column r: partials -> d_scal[r*S_COUNT + slot]
 void cast_d2f(tp_ctx* c, long n, const double* a, float* b);
 void cast_f2d(tp_ctx* c, long n, const float* a, double* b);
-void cg_pupdate(tp_ctx* c, long n, const double* z, double* p, int first);
-void cg_xr_update(tp_ctx* c, long n, double* u, double* r, const double* p, const double* q, int* nblocks);
-void cg_scalars(tp_ctx* c, int what);
+void cg_pupdate(tp_ctx* c, long n, const double* z, double* p, int first, int nr = 1);
+void cg_xr_update(tp_ctx* c, long n, double* u, double* r, const double* p, const double* q, int* nblocks, int nr = 1);
+void cg_scalars(tp_ctx* c, int what, int nr = 1, double tol = 0.0, int iter = 0);
+void cg_reset(tp_ctx* c, int nr);
 
 // coarsest level (tp_cholesky.cu)
 void coarse_alloc(tp_ctx* c);
 void coarse_free(tp_ctx* c);
 void coarse_assemble(tp_ctx* c);  // from the FP64 stencil of level nl-1
 void coarse_factor(tp_ctx* c);
-void coarse_solve(tp_ctx* c, const double* rhs, double* x);
+void coarse_solve(tp_ctx* c, const double* rhs, double* x, int nr = 1);  // nr columns of ndof(nl-1)
 
 // design-variable ops (tp_kernels_design.cu)
-void compliance(tp_ctx* c, const double* u, double* dc, int* nblocks);
+void compliance(tp_ctx* c, const double* u, double* dc, int* nblocks, int nr = 1);  // sums over the nr load cases
 void filter_hs(tp_ctx* c, double* hs);
 void filter_fwd(tp_ctx* c, const double* x, double* out);
 void filter_adj(tp_ctx* c, double* v, double* tmp);
@@ -233,6 +246,12 @@ void vec_sum(tp_ctx* c, long n, const double* v, int slot);
 void element_sens(tp_ctx* c, const double* u, const double* w, double* out);
 int filter_fwd_blocks(const tp_ctx* c);
 void set_design_ke(const double* ke0_host);
+
+// PCG pieces (tp_api.cu) and the graph-captured solve (tp_api_batch.cu)
+void pcg_prologue(tp_ctx* c, const double* b, const double* u, int nr);
+void pcg_iteration(tp_ctx* c, double* u, int iter, int nr);
+tp_status pcg_graph(tp_ctx* c, int* iters, double* relres);
+void graph_free(tp_ctx* c);
 
 // error helpers
 bool cuda_ok(tp_ctx* c, cudaError_t e, const char* what);

@@ -124,63 +124,101 @@ template void assemble_stencil<float>(tp_ctx*, int, const float*, const float*, 
 
 enum { S_APPLY = 0, S_JACOBI = 1, S_RESID = 2 };
 
-template <typename T, int MODE>
+// NR right-hand sides (columns 3*nnodes apart) share each coefficient load.
+template <typename T, int MODE, int NR>
 __global__ void stencil_kernel(CGeom g, const T* __restrict__ st, const T* __restrict__ in,
                                T* __restrict__ out, const T* __restrict__ b,
                                const T* __restrict__ invD, T omega) {
   const long n = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (n >= g.nnodes) return;
+  const long vs = 3 * g.nnodes;
   const int j = n % g.ny;
   const int k = (n / g.ny) % g.nz;
   const int i = n / ((long)g.ny * g.nz);
-  T y[3] = {T(0), T(0), T(0)};
+  T y[NR][3];
+#pragma unroll
+  for (int r = 0; r < NR; r++) y[r][0] = y[r][1] = y[r][2] = T(0);
 #pragma unroll
   for (int m = 0; m < 27; m++) {
     const int mx = m / 9 - 1, mz = (m / 3) % 3 - 1, my = m % 3 - 1;
     const int mi = i + mx, mk = k + mz, mj = j + my;
     if (mi < 0 || mi >= g.nx || mk < 0 || mk >= g.nz || mj < 0 || mj >= g.ny) continue;
     const long nm = ((long)mi * g.nz + mk) * g.ny + mj;
-    const T u0 = in[3 * nm], u1 = in[3 * nm + 1], u2 = in[3 * nm + 2];
     const T* A = st + (long)m * 9 * g.nnodes + n;
+    T a[9];
 #pragma unroll
-    for (int c = 0; c < 3; c++)
-      y[c] += A[(3 * c) * g.nnodes] * u0 + A[(3 * c + 1) * g.nnodes] * u1 + A[(3 * c + 2) * g.nnodes] * u2;
+    for (int q = 0; q < 9; q++) a[q] = A[q * g.nnodes];
+#pragma unroll
+    for (int r = 0; r < NR; r++) {
+      const T u0 = in[r * vs + 3 * nm], u1 = in[r * vs + 3 * nm + 1], u2 = in[r * vs + 3 * nm + 2];
+#pragma unroll
+      for (int c = 0; c < 3; c++) y[r][c] += a[3 * c] * u0 + a[3 * c + 1] * u1 + a[3 * c + 2] * u2;
+    }
   }
 #pragma unroll
-  for (int c = 0; c < 3; c++) {
-    if (MODE == S_APPLY) out[3 * n + c] = y[c];
-    if (MODE == S_JACOBI) out[3 * n + c] = in[3 * n + c] + omega * invD[3 * n + c] * (b[3 * n + c] - y[c]);
-    if (MODE == S_RESID) out[3 * n + c] = b[3 * n + c] - y[c];
+  for (int r = 0; r < NR; r++)
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const long o = r * vs + 3 * n + c;
+      if (MODE == S_APPLY) out[o] = y[r][c];
+      if (MODE == S_JACOBI) out[o] = in[o] + omega * invD[3 * n + c] * (b[o] - y[r][c]);
+      if (MODE == S_RESID) out[o] = b[o] - y[r][c];
+    }
+}
+
+// nr columns in chunks of 8, 4, 2, 1 (each chunk reads the stencil once)
+template <typename T, int MODE>
+static void stencil_launch(tp_ctx* c, int l, const T* st, const T* in, T* out, const T* b, const T* invD, T omega,
+                           int nr) {
+  const CGeom g = cgeom(c, l);
+  const long vs = 3 * g.nnodes;
+  const unsigned grid = grid_for(g.nnodes, 128);
+  for (int r0 = 0; r0 < nr;) {
+    const int left = nr - r0;
+    const long o = r0 * vs;
+    const T* bb = b ? b + o : nullptr;
+    if (left >= 8) {
+      stencil_kernel<T, MODE, 8><<<grid, 128, 0, c->s>>>(g, st, in + o, out + o, bb, invD, omega);
+      r0 += 8;
+    } else if (left >= 4) {
+      stencil_kernel<T, MODE, 4><<<grid, 128, 0, c->s>>>(g, st, in + o, out + o, bb, invD, omega);
+      r0 += 4;
+    } else if (left >= 2) {
+      stencil_kernel<T, MODE, 2><<<grid, 128, 0, c->s>>>(g, st, in + o, out + o, bb, invD, omega);
+      r0 += 2;
+    } else {
+      stencil_kernel<T, MODE, 1><<<grid, 128, 0, c->s>>>(g, st, in + o, out + o, bb, invD, omega);
+      r0 += 1;
+    }
   }
 }
 
 template <typename T>
-void stencil_apply(tp_ctx* c, int l, const T* st, const T* in, T* out) {
+void stencil_apply(tp_ctx* c, int l, const T* st, const T* in, T* out, int nr) {
   ProfScope ps(c, P_STENCIL);
-  const CGeom g = cgeom(c, l);
-  stencil_kernel<T, S_APPLY><<<grid_for(g.nnodes, 128), 128, 0, c->s>>>(g, st, in, out, nullptr, nullptr, T(0));
+  stencil_launch<T, S_APPLY>(c, l, st, in, out, nullptr, nullptr, T(0), nr);
   TP_CHECK_LAUNCH(c, "stencil_apply");
 }
 template <typename T>
-void stencil_jacobi(tp_ctx* c, int l, const T* st, const T* invD, const T* b, const T* u, T* unew, T omega) {
+void stencil_jacobi(tp_ctx* c, int l, const T* st, const T* invD, const T* b, const T* u, T* unew, T omega, int nr) {
   ProfScope ps(c, P_STENCIL);
-  const CGeom g = cgeom(c, l);
-  stencil_kernel<T, S_JACOBI><<<grid_for(g.nnodes, 128), 128, 0, c->s>>>(g, st, u, unew, b, invD, omega);
+  stencil_launch<T, S_JACOBI>(c, l, st, u, unew, b, invD, omega, nr);
   TP_CHECK_LAUNCH(c, "stencil_jacobi");
 }
 template <typename T>
-void stencil_resid(tp_ctx* c, int l, const T* st, const T* b, const T* u, T* d) {
+void stencil_resid(tp_ctx* c, int l, const T* st, const T* b, const T* u, T* d, int nr) {
   ProfScope ps(c, P_STENCIL);
-  const CGeom g = cgeom(c, l);
-  stencil_kernel<T, S_RESID><<<grid_for(g.nnodes, 128), 128, 0, c->s>>>(g, st, u, d, b, nullptr, T(0));
+  stencil_launch<T, S_RESID>(c, l, st, u, d, b, nullptr, T(0), nr);
   TP_CHECK_LAUNCH(c, "stencil_resid");
 }
-template void stencil_apply<double>(tp_ctx*, int, const double*, const double*, double*);
-template void stencil_apply<float>(tp_ctx*, int, const float*, const float*, float*);
-template void stencil_jacobi<double>(tp_ctx*, int, const double*, const double*, const double*, const double*, double*, double);
-template void stencil_jacobi<float>(tp_ctx*, int, const float*, const float*, const float*, const float*, float*, float);
-template void stencil_resid<double>(tp_ctx*, int, const double*, const double*, const double*, double*);
-template void stencil_resid<float>(tp_ctx*, int, const float*, const float*, const float*, float*);
+template void stencil_apply<double>(tp_ctx*, int, const double*, const double*, double*, int);
+template void stencil_apply<float>(tp_ctx*, int, const float*, const float*, float*, int);
+template void stencil_jacobi<double>(tp_ctx*, int, const double*, const double*, const double*, const double*, double*,
+                                     double, int);
+template void stencil_jacobi<float>(tp_ctx*, int, const float*, const float*, const float*, const float*, float*, float,
+                                    int);
+template void stencil_resid<double>(tp_ctx*, int, const double*, const double*, const double*, double*, int);
+template void stencil_resid<float>(tp_ctx*, int, const float*, const float*, const float*, float*, int);
 
 // ---------------------------------------------------------------------------
 // Full-weighting restriction, level l+1 <- level l (stencil_methods.c:595-688):
@@ -191,6 +229,8 @@ template <typename T>
 __global__ void restrict_kernel(CGeom f, CGeom cg, const T* __restrict__ fine, T* __restrict__ coarse) {
   const long n = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (n >= cg.nnodes) return;
+  fine += blockIdx.y * 3 * f.nnodes;  // column of this right-hand side
+  coarse += blockIdx.y * 3 * cg.nnodes;
   const int jc = n % cg.ny;
   const int kc = (n / cg.ny) % cg.nz;
   const int ic = n / ((long)cg.ny * cg.nz);
@@ -220,6 +260,8 @@ template <typename T, bool ADD>
 __global__ void prolong_kernel(CGeom f, CGeom cg, const T* __restrict__ coarse, T* __restrict__ fine) {
   const long n = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (n >= f.nnodes) return;
+  fine += blockIdx.y * 3 * f.nnodes;
+  coarse += blockIdx.y * 3 * cg.nnodes;
   const int j = n % f.ny;
   const int k = (n / f.ny) % f.nz;
   const int i = n / ((long)f.ny * f.nz);
@@ -241,31 +283,31 @@ __global__ void prolong_kernel(CGeom f, CGeom cg, const T* __restrict__ coarse, 
 }
 
 template <typename T>
-void restrict_fw(tp_ctx* c, int l, const T* fine, T* coarse) {
+void restrict_fw(tp_ctx* c, int l, const T* fine, T* coarse, int nr) {
   ProfScope ps(c, P_TRANSFER);
   const CGeom f = cgeom(c, l), cg = cgeom(c, l + 1);
-  restrict_kernel<T><<<grid_for(cg.nnodes, 128), 128, 0, c->s>>>(f, cg, fine, coarse);
+  restrict_kernel<T><<<dim3(grid_for(cg.nnodes, 128), nr), 128, 0, c->s>>>(f, cg, fine, coarse);
   TP_CHECK_LAUNCH(c, "restrict");
 }
 template <typename T>
-void prolong_add(tp_ctx* c, int l, const T* coarse, T* fine) {
+void prolong_add(tp_ctx* c, int l, const T* coarse, T* fine, int nr) {
   ProfScope ps(c, P_TRANSFER);
   const CGeom f = cgeom(c, l), cg = cgeom(c, l + 1);
-  prolong_kernel<T, true><<<grid_for(f.nnodes, 128), 128, 0, c->s>>>(f, cg, coarse, fine);
+  prolong_kernel<T, true><<<dim3(grid_for(f.nnodes, 128), nr), 128, 0, c->s>>>(f, cg, coarse, fine);
   TP_CHECK_LAUNCH(c, "prolong_add");
 }
 template <typename T>
-void prolong_set(tp_ctx* c, int l, const T* coarse, T* fine) {
+void prolong_set(tp_ctx* c, int l, const T* coarse, T* fine, int nr) {
   ProfScope ps(c, P_TRANSFER);
   const CGeom f = cgeom(c, l), cg = cgeom(c, l + 1);
-  prolong_kernel<T, false><<<grid_for(f.nnodes, 128), 128, 0, c->s>>>(f, cg, coarse, fine);
+  prolong_kernel<T, false><<<dim3(grid_for(f.nnodes, 128), nr), 128, 0, c->s>>>(f, cg, coarse, fine);
   TP_CHECK_LAUNCH(c, "prolong_set");
 }
-template void restrict_fw<double>(tp_ctx*, int, const double*, double*);
-template void restrict_fw<float>(tp_ctx*, int, const float*, float*);
-template void prolong_add<double>(tp_ctx*, int, const double*, double*);
-template void prolong_add<float>(tp_ctx*, int, const float*, float*);
-template void prolong_set<double>(tp_ctx*, int, const double*, double*);
-template void prolong_set<float>(tp_ctx*, int, const float*, float*);
+template void restrict_fw<double>(tp_ctx*, int, const double*, double*, int);
+template void restrict_fw<float>(tp_ctx*, int, const float*, float*, int);
+template void prolong_add<double>(tp_ctx*, int, const double*, double*, int);
+template void prolong_add<float>(tp_ctx*, int, const float*, float*, int);
+template void prolong_set<double>(tp_ctx*, int, const double*, double*, int);
+template void prolong_set<float>(tp_ctx*, int, const float*, float*, int);
 
 }  // namespace tp

@@ -53,11 +53,13 @@ static DGeom dgeom(const tp_ctx* c) {
 constexpr int kMaxBlocks = 4096;
 
 // out_e = -3 (E0-Emin) x_e^2 w_e^T KE u_e (penalty 3, stencil_methods.c:855-858);
-// with w = u, also the compliance partials sum_e E_e u_e^T KE u_e.
+// with w = u, also the compliance partials sum_e E_e u_e^T KE u_e. With nr
+// load cases (columns vs apart) the compliance and its sensitivity are the
+// sums over the cases.
 template <bool COMPLIANCE>
 __global__ void sens_kernel(DGeom g, const double* __restrict__ x, const double* __restrict__ u,
                             const double* __restrict__ w, double* __restrict__ out,
-                            double* __restrict__ partials) {
+                            double* __restrict__ partials, int nr, long vs) {
   const long ne = (long)g.ex * g.ey * g.ez;
   const double Ed = 1.0 - 1e-6;
   double csum = 0.0;
@@ -65,30 +67,32 @@ __global__ void sens_kernel(DGeom g, const double* __restrict__ x, const double*
     const int j = e % g.ey;
     const int k = (e / g.ey) % g.ez;
     const int i = e / ((long)g.ey * g.ez);
-    double ue[24], we[24];
-#pragma unroll
-    for (int q = 0; q < 8; q++) {
-      const long n = ((long)(i + dloc_dx(q)) * g.nz + (k + dloc_dz(q))) * g.ny + (j + dloc_dy(q));
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        ue[3 * q + c] = u[3 * n + c];
-        we[3 * q + c] = COMPLIANCE ? ue[3 * q + c] : w[3 * n + c];
-      }
-    }
     const double xe = x[e];
     double d = 0.0;
+    for (int r = 0; r < nr; r++) {
+      double ue[24], we[24];
 #pragma unroll
-    for (int ii = 0; ii < 8; ii++) {
-      double cl = 0.0;
+      for (int q = 0; q < 8; q++) {
+        const long n = ((long)(i + dloc_dx(q)) * g.nz + (k + dloc_dz(q))) * g.ny + (j + dloc_dy(q));
 #pragma unroll
-      for (int a = 0; a < 3; a++) {
-        double t = 0.0;
-#pragma unroll
-        for (int b = 0; b < 24; b++) t += c_ke0_design[(ii * 3 + a) * 24 + b] * ue[b];
-        cl += we[3 * ii + a] * t;
+        for (int c = 0; c < 3; c++) {
+          ue[3 * q + c] = u[r * vs + 3 * n + c];
+          we[3 * q + c] = COMPLIANCE ? ue[3 * q + c] : w[3 * n + c];
+        }
       }
-      if (COMPLIANCE) csum += cl * (1e-6 + xe * xe * xe * Ed);
-      d += cl * (-3.0 * Ed * xe * xe);
+#pragma unroll
+      for (int ii = 0; ii < 8; ii++) {
+        double cl = 0.0;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+          double t = 0.0;
+#pragma unroll
+          for (int b = 0; b < 24; b++) t += c_ke0_design[(ii * 3 + a) * 24 + b] * ue[b];
+          cl += we[3 * ii + a] * t;
+        }
+        if (COMPLIANCE) csum += cl * (1e-6 + xe * xe * xe * Ed);
+        d += cl * (-3.0 * Ed * xe * xe);
+      }
     }
     out[e] = d;
   }
@@ -105,12 +109,12 @@ static int blocks_for(long n) {
   return (int)b;
 }
 
-void compliance(tp_ctx* c, const double* u, double* dc, int* nblocks) {
+void compliance(tp_ctx* c, const double* u, double* dc, int* nblocks, int nr) {
   ProfScope ps(c, P_DESIGN);
   const DGeom g = dgeom(c);
   const long ne = (long)g.ex * g.ey * g.ez;
   const int nb = blocks_for(ne);
-  sens_kernel<true><<<nb, 256, 0, c->s>>>(g, c->d_xphys, u, nullptr, dc, c->d_red);
+  sens_kernel<true><<<nb, 256, 0, c->s>>>(g, c->d_xphys, u, nullptr, dc, c->d_red, nr, c->L[0].ndof);
   TP_CHECK_LAUNCH(c, "compliance");
   *nblocks = nb;
 }
@@ -119,7 +123,7 @@ void element_sens(tp_ctx* c, const double* u, const double* w, double* out) {
   ProfScope ps(c, P_DESIGN);
   const DGeom g = dgeom(c);
   const long ne = (long)g.ex * g.ey * g.ez;
-  sens_kernel<false><<<blocks_for(ne), 256, 0, c->s>>>(g, c->d_xphys, u, w, out, nullptr);
+  sens_kernel<false><<<blocks_for(ne), 256, 0, c->s>>>(g, c->d_xphys, u, w, out, nullptr, 1, 0);
   TP_CHECK_LAUNCH(c, "element_sens");
 }
 

@@ -170,39 +170,47 @@ static dim3 fine_grid(const tp_ctx* c) {
 // has a plan for; this node-centric kernel covers the rest (y extents above
 // 256 elements, unaligned vectors) and serves as its cross-check.
 template <typename T>
-void fine_apply(tp_ctx* c, const T* E, const T* in, T* out) {
+void fine_apply(tp_ctx* c, const T* E, const T* in, T* out, int nr) {
   ProfScope ps(c, sizeof(T) == 8 ? P_FINE_APPLY_F64 : P_FINE_APPLY_F32);
-  if (c->fine_variant == 0 && fine_ec<T>(c, FM_APPLY, E, in, out, nullptr, nullptr, T(0)) >= 0) return;
-  fine_kernel<T, M_APPLY><<<fine_grid(c), dim3(TY, TZ, TX), 0, c->s>>>(geom(c), E, in, out, nullptr,
-                                                                       nullptr, T(0), nullptr);
+  if (c->fine_variant == 0 && fine_ec<T>(c, FM_APPLY, E, in, out, nullptr, nullptr, T(0), nr) >= 0) return;
+  const long vs = c->L[0].ndof;
+  for (int r = 0; r < nr; r++)
+    fine_kernel<T, M_APPLY><<<fine_grid(c), dim3(TY, TZ, TX), 0, c->s>>>(geom(c), E, in + r * vs, out + r * vs,
+                                                                         nullptr, nullptr, T(0), nullptr);
   TP_CHECK_LAUNCH(c, "fine_apply");
 }
 template <typename T>
-int fine_apply_dot(tp_ctx* c, const T* E, const T* in, T* out) {
+int fine_apply_dot(tp_ctx* c, const T* E, const T* in, T* out, int nr) {
   ProfScope ps(c, sizeof(T) == 8 ? P_FINE_APPLY_F64 : P_FINE_APPLY_F32);
   if (c->fine_variant == 0) {
-    const int nb = fine_ec<T>(c, FM_APPLY_DOT, E, in, out, nullptr, nullptr, T(0));
+    const int nb = fine_ec<T>(c, FM_APPLY_DOT, E, in, out, nullptr, nullptr, T(0), nr);
     if (nb >= 0) return nb;
   }
-  fine_kernel<T, M_APPLY_DOT><<<fine_grid(c), dim3(TY, TZ, TX), 0, c->s>>>(
-      geom(c), E, in, out, nullptr, nullptr, T(0), c->d_red);
+  const long vs = c->L[0].ndof;
+  for (int r = 0; r < nr; r++)
+    fine_kernel<T, M_APPLY_DOT><<<fine_grid(c), dim3(TY, TZ, TX), 0, c->s>>>(
+        geom(c), E, in + r * vs, out + r * vs, nullptr, nullptr, T(0), c->d_red + (long)r * fine_blocks(c));
   TP_CHECK_LAUNCH(c, "fine_apply_dot");
   return fine_blocks(c);
 }
 template <typename T>
-void fine_jacobi(tp_ctx* c, const T* E, const T* invD, const T* b, const T* u, T* unew, T omega) {
+void fine_jacobi(tp_ctx* c, const T* E, const T* invD, const T* b, const T* u, T* unew, T omega, int nr) {
   ProfScope ps(c, sizeof(T) == 8 ? P_FINE_JACOBI_F64 : P_FINE_JACOBI_F32);
-  if (c->fine_variant == 0 && fine_ec<T>(c, FM_JACOBI, E, u, unew, b, invD, omega) >= 0) return;
-  fine_kernel<T, M_JACOBI><<<fine_grid(c), dim3(TY, TZ, TX), 0, c->s>>>(geom(c), E, u, unew, b, invD,
-                                                                        omega, nullptr);
+  if (c->fine_variant == 0 && fine_ec<T>(c, FM_JACOBI, E, u, unew, b, invD, omega, nr) >= 0) return;
+  const long vs = c->L[0].ndof;
+  for (int r = 0; r < nr; r++)
+    fine_kernel<T, M_JACOBI><<<fine_grid(c), dim3(TY, TZ, TX), 0, c->s>>>(geom(c), E, u + r * vs, unew + r * vs,
+                                                                          b + r * vs, invD, omega, nullptr);
   TP_CHECK_LAUNCH(c, "fine_jacobi");
 }
 template <typename T>
-void fine_resid(tp_ctx* c, const T* E, const T* b, const T* u, T* d) {
+void fine_resid(tp_ctx* c, const T* E, const T* b, const T* u, T* d, int nr) {
   ProfScope ps(c, sizeof(T) == 8 ? P_FINE_RESID_F64 : P_FINE_RESID_F32);
-  if (c->fine_variant == 0 && fine_ec<T>(c, FM_RESID, E, u, d, b, nullptr, T(0)) >= 0) return;
-  fine_kernel<T, M_RESID><<<fine_grid(c), dim3(TY, TZ, TX), 0, c->s>>>(geom(c), E, u, d, b, nullptr,
-                                                                       T(0), nullptr);
+  if (c->fine_variant == 0 && fine_ec<T>(c, FM_RESID, E, u, d, b, nullptr, T(0), nr) >= 0) return;
+  const long vs = c->L[0].ndof;
+  for (int r = 0; r < nr; r++)
+    fine_kernel<T, M_RESID><<<fine_grid(c), dim3(TY, TZ, TX), 0, c->s>>>(geom(c), E, u + r * vs, d + r * vs,
+                                                                         b + r * vs, nullptr, T(0), nullptr);
   TP_CHECK_LAUNCH(c, "fine_resid");
 }
 
@@ -211,13 +219,14 @@ int fine_blocks(const tp_ctx* c) {
   return (int)(g.x * g.y * g.z);
 }
 
-template void fine_apply<double>(tp_ctx*, const double*, const double*, double*);
-template void fine_apply<float>(tp_ctx*, const float*, const float*, float*);
-template int fine_apply_dot<double>(tp_ctx*, const double*, const double*, double*);
-template void fine_jacobi<double>(tp_ctx*, const double*, const double*, const double*, const double*, double*, double);
-template void fine_jacobi<float>(tp_ctx*, const float*, const float*, const float*, const float*, float*, float);
-template void fine_resid<double>(tp_ctx*, const double*, const double*, const double*, double*);
-template void fine_resid<float>(tp_ctx*, const float*, const float*, const float*, float*);
+template void fine_apply<double>(tp_ctx*, const double*, const double*, double*, int);
+template void fine_apply<float>(tp_ctx*, const float*, const float*, float*, int);
+template int fine_apply_dot<double>(tp_ctx*, const double*, const double*, double*, int);
+template void fine_jacobi<double>(tp_ctx*, const double*, const double*, const double*, const double*, double*, double,
+                                  int);
+template void fine_jacobi<float>(tp_ctx*, const float*, const float*, const float*, const float*, float*, float, int);
+template void fine_resid<double>(tp_ctx*, const double*, const double*, const double*, double*, int);
+template void fine_resid<float>(tp_ctx*, const float*, const float*, const float*, float*, int);
 
 // inverse Jacobi diagonal of level 0: 1 / sum_e E_e KE[r][r], 1 at fixed DOFs
 __global__ void fine_diag_kernel(FineGeom g, const double* __restrict__ E, double* __restrict__ invD) {

@@ -569,7 +569,7 @@ static int ec_launch(tp_ctx* c, const EcPlan& p, const T* E, const T* in, T* out
   const dim3 grid((unsigned)((p.ngz + p.nzg - 1) / p.nzg), (unsigned)p.ncx, (unsigned)nrhs);
   kern<<<grid, dim3(p.nyt, p.nzg), smem, c->s>>>(g, E, in, out, b, invD, omega, c->d_red);
   TP_CHECK_LAUNCH(c, "fine_ec");
-  return (int)(grid.x * grid.y * grid.z);
+  return (int)(grid.x * grid.y);  // partials per right-hand side
 }
 
 template <typename T>
@@ -579,21 +579,26 @@ const EcPlan& ec_plan_for(const tp_ctx* c, int mode) {
 
 static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
+// nr right-hand sides, consecutive columns of ndof(0). Only the first column
+// needs a 16-byte aligned base: the staging of a later column may start up to
+// 15 bytes early, inside the column before it.
 template <typename T>
-int fine_ec(tp_ctx* c, int mode, const T* E, const T* in, T* out, const T* b, const T* invD, T omega) {
+int fine_ec(tp_ctx* c, int mode, const T* E, const T* in, T* out, const T* b, const T* invD, T omega, int nr) {
   const EcPlan& p = ec_plan_for<T>(c, mode);
+  const long vs = c->L[0].ndof;
   if (!p.ok || !aligned16(in) || (b && !aligned16(b)) || (invD && !aligned16(invD))) return -1;
   switch (mode) {
-    case EC_APPLY: return ec_launch<T, EC_APPLY>(c, p, E, in, out, b, invD, omega, 1, 0);
-    case EC_APPLY_DOT: return ec_launch<T, EC_APPLY_DOT>(c, p, E, in, out, b, invD, omega, 1, 0);
-    case EC_JACOBI: return ec_launch<T, EC_JACOBI>(c, p, E, in, out, b, invD, omega, 1, 0);
-    default: return ec_launch<T, EC_RESID>(c, p, E, in, out, b, invD, omega, 1, 0);
+    case EC_APPLY: return ec_launch<T, EC_APPLY>(c, p, E, in, out, b, invD, omega, nr, vs);
+    case EC_APPLY_DOT: return ec_launch<T, EC_APPLY_DOT>(c, p, E, in, out, b, invD, omega, nr, vs);
+    case EC_JACOBI: return ec_launch<T, EC_JACOBI>(c, p, E, in, out, b, invD, omega, nr, vs);
+    default: return ec_launch<T, EC_RESID>(c, p, E, in, out, b, invD, omega, nr, vs);
   }
 }
 
 template int fine_ec<double>(tp_ctx*, int, const double*, const double*, double*, const double*, const double*,
-                             double);
-template int fine_ec<float>(tp_ctx*, int, const float*, const float*, float*, const float*, const float*, float);
+                             double, int);
+template int fine_ec<float>(tp_ctx*, int, const float*, const float*, float*, const float*, const float*, float,
+                            int);
 
 }  // namespace tp
 
@@ -665,6 +670,7 @@ extern "C" tp_status tp_autotune(tp_ctx* c, double* ms_out) {
   if (ms_out)
     for (int i = 0; i < 8; i++) ms_out[i] = 0.0;
   if (!c->ec_ok || !c->ec_f64[0].ok) return TP_OK;
+  graph_free(c);  // a captured CG loop keeps the launch shapes it was recorded with
   int sms = 148;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
   ec_tune<double>(c, c->ec_f64, c->d_E, c->d_p, c->d_q, c->d_r, c->invD[0], sms, ms_out ? ms_out + 4 : nullptr);

@@ -2,7 +2,13 @@
 // stencil_solvers.h:36-58). Every reduction is two-pass and order-fixed:
 // blocks write partial sums, one block adds them in index order, so results
 // are bit-reproducible from run to run. The CG scalars (rho, alpha, beta,
-// relres) stay in device memory; the host reads relres once per iteration.
+// relres) stay in device memory.
+//
+// Several right-hand sides (load cases sharing one operator) are handled as
+// nr columns of length n stored one after the other; column r keeps its own
+// scalars at d_scal[r * S_COUNT + slot] and its own reduction partials. A
+// column whose relative residual has dropped below the tolerance is frozen
+// (alpha = beta = 0), so the columns still iterating do not disturb it.
 #include "tp_internal.h"
 
 namespace tp {
@@ -32,29 +38,37 @@ __device__ __forceinline__ double block_sum256(double v) {
 
 constexpr int kDotBlocks = 2048;
 
-// grid-stride dot with a fixed number of blocks -> partials[0..gridDim)
-__global__ void dot_kernel(long n, const double* __restrict__ a, const double* __restrict__ b,
-                           double* __restrict__ partials) {
-  double s = 0.0;
-  for (long i = blockIdx.x * 256L + threadIdx.x; i < n; i += (long)gridDim.x * 256) s += a[i] * b[i];
-  s = block_sum256(s);
-  if (threadIdx.x == 0) partials[blockIdx.x] = s;
-}
-
-void dot_partials(tp_ctx* c, long n, const double* a, const double* b, int* nblocks) {
-  ProfScope ps(c, P_VECTOR);
+static int dot_blocks(long n) {
   int nb = (int)((n + 255) / 256);
   if (nb > kDotBlocks) nb = kDotBlocks;
   if (nb < 1) nb = 1;
-  dot_kernel<<<nb, 256, 0, c->s>>>(n, a, b, c->d_red);
+  return nb;
+}
+
+// grid-stride dot per column with a fixed number of blocks -> partials[r * gridDim.x + block]
+__global__ void dot_kernel(long n, const double* __restrict__ a, const double* __restrict__ b,
+                           double* __restrict__ partials) {
+  const long off = (long)blockIdx.y * n;
+  double s = 0.0;
+  for (long i = blockIdx.x * 256L + threadIdx.x; i < n; i += (long)gridDim.x * 256) s += a[off + i] * b[off + i];
+  s = block_sum256(s);
+  if (threadIdx.x == 0) partials[(long)blockIdx.y * gridDim.x + blockIdx.x] = s;
+}
+
+void dot_partials(tp_ctx* c, long n, const double* a, const double* b, int* nblocks, int nr) {
+  ProfScope ps(c, P_VECTOR);
+  const int nb = dot_blocks(n);
+  dot_kernel<<<dim3(nb, nr), 256, 0, c->s>>>(n, a, b, c->d_red);
   TP_CHECK_LAUNCH(c, "dot");
   *nblocks = nb;
 }
 
-// op 0: sum; op 1: max
+// op 0: sum; op 1: max. Column r (blockIdx.x) folds partials[r*nb .. r*nb + nb)
+// into out[r * S_COUNT].
 __global__ void finish_kernel(const double* __restrict__ partials, int nb, double* __restrict__ out, int op) {
   __shared__ double sh[256];
-  double s = (op == 1) ? 0.0 : 0.0;
+  partials += (long)blockIdx.x * nb;
+  double s = 0.0;
   // each thread folds a contiguous chunk, in order
   const int per = (nb + 255) / 256;
   const int b0 = threadIdx.x * per;
@@ -64,13 +78,13 @@ __global__ void finish_kernel(const double* __restrict__ partials, int nb, doubl
   if (threadIdx.x == 0) {
     double t = sh[0];
     for (int i = 1; i < 256; i++) t = (op == 1) ? fmax(t, sh[i]) : t + sh[i];
-    *out = t;
+    out[(long)blockIdx.x * S_COUNT] = t;
   }
 }
 
-void finish_sum(tp_ctx* c, int nblocks, int slot, int op) {
+void finish_sum(tp_ctx* c, int nblocks, int slot, int op, int nr) {
   ProfScope ps(c, P_VECTOR);
-  finish_kernel<<<1, 256, 0, c->s>>>(c->d_red, nblocks, c->d_scal + slot, op);
+  finish_kernel<<<nr, 256, 0, c->s>>>(c->d_red, nblocks, c->d_scal + slot, op);
   TP_CHECK_LAUNCH(c, "finish");
 }
 
@@ -91,76 +105,114 @@ void cast_f2d(tp_ctx* c, long n, const float* a, double* b) {
 }
 
 // out = omega * a * b (the first Jacobi sweep from a zero initial guess:
-// K*0 = 0, so u1 = omega*invD*b exactly)
+// K*0 = 0, so u1 = omega*invD*b exactly); a (invD) has one column, b and out nr
 template <typename T>
-__global__ void vscale_kernel(long n, const T* __restrict__ a, const T* __restrict__ b, T* __restrict__ out, T omega) {
+__global__ void vscale_kernel(long n, long ntot, const T* __restrict__ a, const T* __restrict__ b,
+                              T* __restrict__ out, T omega) {
   const long i = blockIdx.x * 256L + threadIdx.x;
-  if (i < n) out[i] = omega * a[i] * (b[i] - T(0));
+  if (i < ntot) out[i] = omega * a[i % n] * (b[i] - T(0));
 }
 template <typename T>
-void vscale(tp_ctx* c, long n, const T* a, const T* b, T* out, T omega) {
+void vscale(tp_ctx* c, long n, const T* a, const T* b, T* out, T omega, int nr) {
   ProfScope ps(c, P_VECTOR);
-  vscale_kernel<T><<<grid_for(n, 256), 256, 0, c->s>>>(n, a, b, out, omega);
+  vscale_kernel<T><<<grid_for(n * nr, 256), 256, 0, c->s>>>(n, n * nr, a, b, out, omega);
   TP_CHECK_LAUNCH(c, "vscale");
 }
-template void vscale<double>(tp_ctx*, long, const double*, const double*, double*, double);
-template void vscale<float>(tp_ctx*, long, const float*, const float*, float*, float);
+template void vscale<double>(tp_ctx*, long, const double*, const double*, double*, double, int);
+template void vscale<float>(tp_ctx*, long, const float*, const float*, float*, float, int);
 
-// p = z (first iteration) or p = beta*p + z, beta = rho/rhoold from the device
-__global__ void pupdate_kernel(long n, const double* __restrict__ z, double* __restrict__ p,
+// p = z (first iteration) or p = beta*p + z, beta of the column from the
+// device; first = -1: the first iteration is the device counter's zero
+__global__ void pupdate_kernel(long n, long ntot, const double* __restrict__ z, double* __restrict__ p,
                                const double* __restrict__ scal, int first) {
   const long i = blockIdx.x * 256L + threadIdx.x;
-  if (i >= n) return;
+  if (i >= ntot) return;
+  if (first < 0) first = scal[S_IT] == 0.0;
   if (first)
     p[i] = z[i];
   else
-    p[i] = scal[S_BETA] * p[i] + z[i];
+    p[i] = scal[(i / n) * S_COUNT + S_BETA] * p[i] + z[i];
 }
-void cg_pupdate(tp_ctx* c, long n, const double* z, double* p, int first) {
+void cg_pupdate(tp_ctx* c, long n, const double* z, double* p, int first, int nr) {
   ProfScope ps(c, P_VECTOR);
-  pupdate_kernel<<<grid_for(n, 256), 256, 0, c->s>>>(n, z, p, c->d_scal, first);
+  pupdate_kernel<<<grid_for(n * nr, 256), 256, 0, c->s>>>(n, n * nr, z, p, c->d_scal, first);
   TP_CHECK_LAUNCH(c, "cg_pupdate");
 }
 
-// u += alpha p ; r -= alpha q ; partials of <r, r>
+// u += alpha p ; r -= alpha q ; partials of <r, r>, per column
 __global__ void xr_kernel(long n, double* __restrict__ u, double* __restrict__ r,
                           const double* __restrict__ p, const double* __restrict__ q,
                           const double* __restrict__ scal, double* __restrict__ partials) {
-  const double alpha = scal[S_ALPHA];
+  const long off = (long)blockIdx.y * n;
+  const double alpha = scal[blockIdx.y * S_COUNT + S_ALPHA];
   double s = 0.0;
-  for (long i = blockIdx.x * 256L + threadIdx.x; i < n; i += (long)gridDim.x * 256) {
+  for (long i = off + blockIdx.x * 256L + threadIdx.x; i < off + n; i += (long)gridDim.x * 256) {
     u[i] += alpha * p[i];
     const double ri = r[i] - alpha * q[i];
     r[i] = ri;
     s += ri * ri;
   }
   s = block_sum256(s);
-  if (threadIdx.x == 0) partials[blockIdx.x] = s;
+  if (threadIdx.x == 0) partials[(long)blockIdx.y * gridDim.x + blockIdx.x] = s;
 }
-void cg_xr_update(tp_ctx* c, long n, double* u, double* r, const double* p, const double* q, int* nblocks) {
+void cg_xr_update(tp_ctx* c, long n, double* u, double* r, const double* p, const double* q, int* nblocks, int nr) {
   ProfScope ps(c, P_VECTOR);
-  int nb = (int)((n + 255) / 256);
-  if (nb > kDotBlocks) nb = kDotBlocks;
-  xr_kernel<<<nb, 256, 0, c->s>>>(n, u, r, p, q, c->d_scal, c->d_red);
+  const int nb = dot_blocks(n);
+  xr_kernel<<<dim3(nb, nr), 256, 0, c->s>>>(n, u, r, p, q, c->d_scal, c->d_red);
   TP_CHECK_LAUNCH(c, "cg_xr_update");
   *nblocks = nb;
 }
 
-// what 0: beta = rho/rhoold (before the p update)
-// what 1: alpha = rho/dpr, rhoold = rho
-// what 2: relres = sqrt(rnorm2)/sqrt(bnorm2)
-__global__ void scalars_kernel(double* s, int what) {
-  if (what == 0) s[S_BETA] = s[S_RHO] / s[S_RHOOLD];
-  if (what == 1) {
-    s[S_ALPHA] = s[S_RHO] / s[S_DPR];
-    s[S_RHOOLD] = s[S_RHO];
+// Per column r (thread r):
+// what 0: beta = rho/rhoold (before the p update), 0 once converged
+// what 1: alpha = rho/dpr, rhoold = rho; 0 once converged
+// what 2: relres = sqrt(rnorm2)/sqrt(bnorm2) (0 for a zero load); a column
+//         below tol is marked converged at iteration `iter`. Thread 0 also
+//         keeps the largest relres of the columns in S_MAXRR of column 0.
+__global__ void scalars_kernel(double* scal, int what, int nr, double tol, int iter) {
+  const int r = threadIdx.x;
+  if (iter < 0) iter = (int)scal[S_IT];
+  if (r < nr) {
+    double* s = scal + (long)r * S_COUNT;
+    const bool done = s[S_CONV] > 0.0;
+    if (what == 0) s[S_BETA] = done ? 0.0 : s[S_RHO] / s[S_RHOOLD];
+    if (what == 1) {
+      s[S_ALPHA] = done ? 0.0 : s[S_RHO] / s[S_DPR];
+      s[S_RHOOLD] = s[S_RHO];
+    }
+    if (what == 2 && !done) {
+      s[S_RELRES] = s[S_BNORM2] > 0.0 ? sqrt(s[S_RNORM2]) / sqrt(s[S_BNORM2]) : 0.0;
+      if (s[S_RELRES] < tol) {
+        s[S_CONV] = 1.0;
+        s[S_ITER] = iter;
+      }
+    }
   }
-  if (what == 2) s[S_RELRES] = sqrt(s[S_RNORM2]) / sqrt(s[S_BNORM2]);
+  __syncwarp();
+  if (what == 2 && r == 0) {
+    double m = 0.0;
+    for (int q = 0; q < nr; q++) m = fmax(m, scal[(long)q * S_COUNT + S_RELRES]);
+    scal[S_MAXRR] = m;
+  }
 }
-void cg_scalars(tp_ctx* c, int what) {
+void cg_scalars(tp_ctx* c, int what, int nr, double tol, int iter) {
   ProfScope ps(c, P_VECTOR);
-  scalars_kernel<<<1, 1, 0, c->s>>>(c->d_scal, what);
+  scalars_kernel<<<1, 32, 0, c->s>>>(c->d_scal, what, nr, tol, iter);
   TP_CHECK_LAUNCH(c, "cg_scalars");
+}
+
+// clears the converged marks of the nr columns before a solve
+__global__ void cg_reset_kernel(double* scal, int nr) {
+  const int r = threadIdx.x;
+  if (r < nr) {
+    scal[(long)r * S_COUNT + S_CONV] = 0.0;
+    scal[(long)r * S_COUNT + S_ITER] = -1.0;
+    scal[(long)r * S_COUNT + S_RELRES] = 0.0;
+  }
+}
+void cg_reset(tp_ctx* c, int nr) {
+  cg_reset_kernel<<<1, 32, 0, c->s>>>(c->d_scal, nr);
+  TP_CHECK_LAUNCH(c, "cg_reset");
 }
 
 }  // namespace tp

@@ -23,7 +23,7 @@ static cudaEvent_t take_event(tp_ctx* c) {
 }
 
 ProfScope::ProfScope(tp_ctx* ctx, int i) : c(ctx), id(i) {
-  if (!c->prof) return;
+  if (!c->prof || c->capturing) return;  // nothing is timed inside a graph capture
   e1 = take_event(c);
   cudaEventRecord(e1, c->s);
 }

@@ -98,11 +98,26 @@ def load():
     L.tp_set_cg.argtypes = [V, D, I, I, D]
     L.tp_set_fine_variant.argtypes = [V, I]
     L.tp_autotune.argtypes = [V, P]
+    L.tp_multiload.argtypes = [I, I, I, I, I, ctypes.c_ulonglong, P]
+    L.tp_set_graph_solve.argtypes = [V, I]
+    L.tp_solve_columns.argtypes = [V, P, P]
     L.tp_set_rmin.argtypes = [V, D]
     L.tp_design_iteration.argtypes = [V, ctypes.POINTER(TpIterInfo)]
     L.tp_run.argtypes = [V, I, ctypes.POINTER(TpIterInfo), ctypes.POINTER(I)]
     _lib = L
     return L
+
+
+def multiload(nelx, nely, nelz, ncase, nload, seed=0):
+    """ncase load cases of nload unit nodal forces on the end face x = nelx
+    (tp_multiload), as an (ncase, ndof) float64 array."""
+    L = load()
+    ndof = 3 * (nelx + 1) * (nely + 1) * (nelz + 1)
+    F = np.zeros((ncase, ndof))
+    st = L.tp_multiload(nelx, nely, nelz, ncase, nload, seed, F.ctypes.data)
+    if st != 0:
+        raise TopOptError(st, "tp_multiload")
+    return F
 
 
 def _ptr(t):
@@ -113,7 +128,7 @@ class TopOpt:
     """One device context: grid, multigrid hierarchy, design state."""
 
     def __init__(self, nelx, nely, nelz, nl, precision=TP_FP64, volfrac=None, rmin=1.5,
-                 cgtol=None, cgmax=1000, nswp=4, omega=0.6, device=0):
+                 cgtol=None, cgmax=1000, nswp=4, omega=0.6, device=0, nrhs=1):
         self.L = load()
         p = TpParams()
         self.L.tp_default_params(ctypes.byref(p))
@@ -126,6 +141,8 @@ class TopOpt:
         p.cgmax, p.nswp, p.omega = cgmax, nswp, omega
         p.precision = precision
         p.device = device
+        p.nrhs = nrhs
+        self.nrhs = nrhs
         self.params = p
         self.ctx = ctypes.c_void_p()
         st = self.L.tp_create(ctypes.byref(p), ctypes.byref(self.ctx))
@@ -167,7 +184,7 @@ class TopOpt:
         self._check(self.L.tp_upload(self.ctx, FIELDS[name], a.ctypes.data_as(ctypes.c_void_p), a.size))
 
     def download(self, name):
-        n = self.nelem() if name not in ("F", "U") else self.ndof(0)
+        n = self.nelem() if name not in ("F", "U") else self.ndof(0) * self.nrhs
         out = np.zeros(n)
         self._check(self.L.tp_download(self.ctx, FIELDS[name], out.ctypes.data_as(ctypes.c_void_p), n))
         return out
@@ -194,6 +211,17 @@ class TopOpt:
     def set_fine_variant(self, variant):
         """0: element-centric level-0 kernel where it applies; 1: node-centric stencil."""
         self._check(self.L.tp_set_fine_variant(self.ctx, variant))
+
+    def solve_columns(self):
+        """(iteration index, relres) of each load case in the last solve."""
+        it = np.zeros(self.nrhs, np.int32)
+        rr = np.zeros(self.nrhs)
+        self._check(self.L.tp_solve_columns(self.ctx, it.ctypes.data, rr.ctypes.data))
+        return it, rr
+
+    def set_graph_solve(self, on):
+        """1: the CG loop runs as one CUDA graph launch also for a single load."""
+        self._check(self.L.tp_set_graph_solve(self.ctx, int(on)))
 
     def autotune(self):
         """Tunes the level-0 launch shapes; returns the best ms per (f32, f64) x mode."""

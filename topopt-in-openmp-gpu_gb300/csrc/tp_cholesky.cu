@@ -408,7 +408,8 @@ __device__ __forceinline__ double wsum(double s) {
   return s;
 }
 
-__global__ void fwd_rows_kernel(const double* __restrict__ Lrow, long bw, long n, int nbs, int blk, int nr,
+template <int NR>
+__global__ void fwd_rows_kernel(const double* __restrict__ Lrow, long bw, long n, int nbs, int blk,
                                 const double* __restrict__ b, const double* __restrict__ y,
                                 double* __restrict__ t) {
   const long b0 = (long)blk * nbs;
@@ -418,44 +419,46 @@ __global__ void fwd_rows_kernel(const double* __restrict__ Lrow, long bw, long n
   const long tlo = lmax(lmax(0L, bw - b0), (long)i);  // columns >= 0 and inside the band
   const double* L = Lrow + ((long)blk * nbs + i) * bw;
   const double* yy = y + (b0 - bw);
-  double s[kSolveCols] = {};
+  double s[NR] = {};
   for (long q = tlo + lane; q < bw; q += 32) {
     const double l = L[q];
 #pragma unroll
-    for (int v = 0; v < kSolveCols; v++)
-      if (v < nr) s[v] += l * yy[v * n + q];
+    for (int v = 0; v < NR; v++)
+      s[v] += l * yy[v * n + q];
   }
 #pragma unroll
-  for (int v = 0; v < kSolveCols; v++)
-    if (v < nr) {
+  for (int v = 0; v < NR; v++)
+    {
       const double sv = wsum(s[v]);
       if (lane == 0) t[v * n + r] = b[v * n + r] - sv;
     }
 }
 
-__global__ void fwd_diag_kernel(const double* __restrict__ D, long n, int nbs, int blk, int nr,
+template <int NR>
+__global__ void fwd_diag_kernel(const double* __restrict__ D, long n, int nbs, int blk,
                                 const double* __restrict__ t, double* __restrict__ y) {
   const long b0 = (long)blk * nbs;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (i >= nbs || b0 + i >= n) return;
   const double* Dr = D + ((long)blk * nbs + i) * nbs;
   const double* tt = t + b0;
-  double s[kSolveCols] = {};
+  double s[NR] = {};
   for (int j = lane; j <= i; j += 32) {
     const double d = Dr[j];
 #pragma unroll
-    for (int v = 0; v < kSolveCols; v++)
-      if (v < nr) s[v] += d * tt[v * n + j];
+    for (int v = 0; v < NR; v++)
+      s[v] += d * tt[v * n + j];
   }
 #pragma unroll
-  for (int v = 0; v < kSolveCols; v++)
-    if (v < nr) {
+  for (int v = 0; v < NR; v++)
+    {
       const double sv = wsum(s[v]);
       if (lane == 0) y[v * n + b0 + i] = sv;
     }
 }
 
-__global__ void bwd_rows_kernel(const double* __restrict__ B, long bw, long n, int nbs, int blk, int nr,
+template <int NR>
+__global__ void bwd_rows_kernel(const double* __restrict__ B, long bw, long n, int nbs, int blk,
                                 const double* __restrict__ y, const double* __restrict__ x,
                                 double* __restrict__ t) {
   const long b0 = (long)blk * nbs, b1 = lmin(n, b0 + nbs);
@@ -463,22 +466,23 @@ __global__ void bwd_rows_kernel(const double* __restrict__ B, long bw, long n, i
   const long r = b0 + i;
   if (i >= nbs || r >= n) return;
   const long c1 = lmin(n - 1, r + bw);
-  double s[kSolveCols] = {};
+  double s[NR] = {};
   for (long cc = b1 + lane; cc <= c1; cc += 32) {
     const double l = B[r * bw + cc];
 #pragma unroll
-    for (int v = 0; v < kSolveCols; v++)
-      if (v < nr) s[v] += l * x[v * n + cc];
+    for (int v = 0; v < NR; v++)
+      s[v] += l * x[v * n + cc];
   }
 #pragma unroll
-  for (int v = 0; v < kSolveCols; v++)
-    if (v < nr) {
+  for (int v = 0; v < NR; v++)
+    {
       const double sv = wsum(s[v]);
       if (lane == 0) t[v * n + r] = y[v * n + r] - sv;
     }
 }
 
-__global__ void bwd_diag_kernel(const double* __restrict__ DT, long n, int nbs, int blk, int nr,
+template <int NR>
+__global__ void bwd_diag_kernel(const double* __restrict__ DT, long n, int nbs, int blk,
                                 const double* __restrict__ t, double* __restrict__ x) {
   const long b0 = (long)blk * nbs;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
@@ -486,41 +490,42 @@ __global__ void bwd_diag_kernel(const double* __restrict__ DT, long n, int nbs, 
   const int s = (int)lmin((long)nbs, n - b0);
   const double* Dr = DT + ((long)blk * nbs + i) * nbs;
   const double* tt = t + b0;
-  double acc[kSolveCols] = {};
+  double acc[NR] = {};
   for (int j = i + lane; j < s; j += 32) {
     const double d = Dr[j];
 #pragma unroll
-    for (int v = 0; v < kSolveCols; v++)
-      if (v < nr) acc[v] += d * tt[v * n + j];
+    for (int v = 0; v < NR; v++)
+      acc[v] += d * tt[v * n + j];
   }
 #pragma unroll
-  for (int v = 0; v < kSolveCols; v++)
-    if (v < nr) {
+  for (int v = 0; v < NR; v++)
+    {
       const double sv = wsum(acc[v]);
       if (lane == 0) x[v * n + b0 + i] = sv;
     }
 }
 
-// the launch sequence of one solve of nr columns from rhs into sol (y and t
+// the launch sequence of one solve of NR columns from rhs into sol (y and t
 // are work columns of the same count)
-static void coarse_solve_launches(tp_ctx* c, const double* rhs, double* sol, double* y, double* t, int nr) {
+template <int NR>
+static void coarse_solve_launches(tp_ctx* c, const double* rhs, double* sol, double* y, double* t) {
   Coarse& C = c->coarse;
   const unsigned g = (unsigned)((C.nbs + 7) / 8);  // 8 warps per CTA, one row per warp
   for (int b = 0; b < C.nblk; b++) {
     const double* tin = rhs;
     if (b > 0) {
-      fwd_rows_kernel<<<g, 256, 0, c->s>>>(C.lrow, C.bw, C.n, C.nbs, b, nr, rhs, y, t);
+      fwd_rows_kernel<NR><<<g, 256, 0, c->s>>>(C.lrow, C.bw, C.n, C.nbs, b, rhs, y, t);
       tin = t;
     }
-    fwd_diag_kernel<<<g, 256, 0, c->s>>>(C.dinv, C.n, C.nbs, b, nr, tin, y);
+    fwd_diag_kernel<NR><<<g, 256, 0, c->s>>>(C.dinv, C.n, C.nbs, b, tin, y);
   }
   for (int b = C.nblk - 1; b >= 0; b--) {
     const double* tin = y;
     if (b < C.nblk - 1) {
-      bwd_rows_kernel<<<g, 256, 0, c->s>>>(C.band, C.bw, C.n, C.nbs, b, nr, y, sol, t);
+      bwd_rows_kernel<NR><<<g, 256, 0, c->s>>>(C.band, C.bw, C.n, C.nbs, b, y, sol, t);
       tin = t;
     }
-    bwd_diag_kernel<<<g, 256, 0, c->s>>>(C.dinvT, C.n, C.nbs, b, nr, tin, sol);
+    bwd_diag_kernel<NR><<<g, 256, 0, c->s>>>(C.dinvT, C.n, C.nbs, b, tin, sol);
   }
 }
 
@@ -533,9 +538,24 @@ void coarse_solve(tp_ctx* c, const double* rhs, double* x, int nr) {
   ProfScope ps(c, P_COARSE_SOLVE);
   Coarse& C = c->coarse;
   if (nr > 1 || c->capturing) {
-    for (int r0 = 0; r0 < nr; r0 += kSolveCols) {
-      const int k = std::min(kSolveCols, nr - r0);
-      coarse_solve_launches(c, rhs + (long)r0 * C.n, x + (long)r0 * C.n, C.vec, C.vec + (long)kSolveCols * C.n, k);
+    double *y = C.vec, *t = C.vec + (long)kSolveCols * C.n;
+    for (int r0 = 0; r0 < nr;) {
+      const double* b = rhs + (long)r0 * C.n;
+      double* xx = x + (long)r0 * C.n;
+      const int left = nr - r0;
+      if (left >= 8) {
+        coarse_solve_launches<8>(c, b, xx, y, t);
+        r0 += 8;
+      } else if (left >= 4) {
+        coarse_solve_launches<4>(c, b, xx, y, t);
+        r0 += 4;
+      } else if (left >= 2) {
+        coarse_solve_launches<2>(c, b, xx, y, t);
+        r0 += 2;
+      } else {
+        coarse_solve_launches<1>(c, b, xx, y, t);
+        r0 += 1;
+      }
     }
     TP_CHECK_LAUNCH(c, "coarse_solve");
     return;
@@ -544,7 +564,7 @@ void coarse_solve(tp_ctx* c, const double* rhs, double* x, int nr) {
   if (!C.graph_exec) {
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-      coarse_solve_launches(c, C.rhs, C.sol, C.vec, C.vec + C.n, 1);
+      coarse_solve_launches<1>(c, C.rhs, C.sol, C.vec, C.vec + C.n);
       if (cudaStreamEndCapture(c->s, &g) == cudaSuccess && g) {
         if (cudaGraphInstantiate(&C.graph_exec, g, 0) != cudaSuccess) C.graph_exec = nullptr;
         cudaGraphDestroy(g);
@@ -555,7 +575,7 @@ void coarse_solve(tp_ctx* c, const double* rhs, double* x, int nr) {
   if (C.graph_exec)
     cudaGraphLaunch(C.graph_exec, c->s);
   else
-    coarse_solve_launches(c, C.rhs, C.sol, C.vec, C.vec + C.n, 1);
+    coarse_solve_launches<1>(c, C.rhs, C.sol, C.vec, C.vec + C.n);
   cudaMemcpyAsync(x, C.sol, sizeof(double) * C.n, cudaMemcpyDeviceToDevice, c->s);
   TP_CHECK_LAUNCH(c, "coarse_solve");
 }

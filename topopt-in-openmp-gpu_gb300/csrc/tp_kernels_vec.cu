@@ -107,15 +107,16 @@ void cast_f2d(tp_ctx* c, long n, const float* a, double* b) {
 // out = omega * a * b (the first Jacobi sweep from a zero initial guess:
 // K*0 = 0, so u1 = omega*invD*b exactly); a (invD) has one column, b and out nr
 template <typename T>
-__global__ void vscale_kernel(long n, long ntot, const T* __restrict__ a, const T* __restrict__ b,
-                              T* __restrict__ out, T omega) {
+__global__ void vscale_kernel(long n, const T* __restrict__ a, const T* __restrict__ b, T* __restrict__ out,
+                              T omega) {
   const long i = blockIdx.x * 256L + threadIdx.x;
-  if (i < ntot) out[i] = omega * a[i % n] * (b[i] - T(0));
+  const long o = (long)blockIdx.y * n;  // column
+  if (i < n) out[o + i] = omega * a[i] * (b[o + i] - T(0));
 }
 template <typename T>
 void vscale(tp_ctx* c, long n, const T* a, const T* b, T* out, T omega, int nr) {
   ProfScope ps(c, P_VECTOR);
-  vscale_kernel<T><<<grid_for(n * nr, 256), 256, 0, c->s>>>(n, n * nr, a, b, out, omega);
+  vscale_kernel<T><<<dim3(grid_for(n, 256), nr), 256, 0, c->s>>>(n, a, b, out, omega);
   TP_CHECK_LAUNCH(c, "vscale");
 }
 template void vscale<double>(tp_ctx*, long, const double*, const double*, double*, double, int);
@@ -123,19 +124,20 @@ template void vscale<float>(tp_ctx*, long, const float*, const float*, float*, f
 
 // p = z (first iteration) or p = beta*p + z, beta of the column from the
 // device; first = -1: the first iteration is the device counter's zero
-__global__ void pupdate_kernel(long n, long ntot, const double* __restrict__ z, double* __restrict__ p,
+__global__ void pupdate_kernel(long n, const double* __restrict__ z, double* __restrict__ p,
                                const double* __restrict__ scal, int first) {
   const long i = blockIdx.x * 256L + threadIdx.x;
-  if (i >= ntot) return;
+  if (i >= n) return;
+  const long o = (long)blockIdx.y * n;  // column
   if (first < 0) first = scal[S_IT] == 0.0;
   if (first)
-    p[i] = z[i];
+    p[o + i] = z[o + i];
   else
-    p[i] = scal[(i / n) * S_COUNT + S_BETA] * p[i] + z[i];
+    p[o + i] = scal[blockIdx.y * S_COUNT + S_BETA] * p[o + i] + z[o + i];
 }
 void cg_pupdate(tp_ctx* c, long n, const double* z, double* p, int first, int nr) {
   ProfScope ps(c, P_VECTOR);
-  pupdate_kernel<<<grid_for(n * nr, 256), 256, 0, c->s>>>(n, n * nr, z, p, c->d_scal, first);
+  pupdate_kernel<<<dim3(grid_for(n, 256), nr), 256, 0, c->s>>>(n, z, p, c->d_scal, first);
   TP_CHECK_LAUNCH(c, "cg_pupdate");
 }
 

@@ -49,7 +49,10 @@ def args_parse():
     ap.add_argument("--nl", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison pass")
-    ap.add_argument("--passes", default="ABC", help="GPU passes to run (A resident, B e2e, C FP64)")
+    ap.add_argument("--passes", default="ABCD",
+                    help="GPU passes to run (A resident, B e2e, C FP64, D batched multi-load)")
+    ap.add_argument("--batched-shape", default="384x192x192")
+    ap.add_argument("--batched-cases", type=int, default=8)
     ap.add_argument("--cpu-budget", type=float, default=150.0, help="seconds of CPU work for the reference arm")
     ap.add_argument("--cpu-sample", default=None, help=argparse.SUPPRESS)  # internal: child process mode
     return ap.parse_args()
@@ -275,6 +278,66 @@ def design_pass(tp, torch, shape, nl, precision, W, K, profile=False, e2e=False,
     return hist + timed, timed, ms_events, wall, prof
 
 
+def batched_pass(tp, torch, shape, nl, nrhs, nload, W, K, hbm):
+    """Several load cases sharing one operator: nrhs seeded multi-load cases
+    (nload unit nodal forces each on the end face), mixed precision, summed
+    compliance; every state solve is one multi-column PCG whose CG loop is a
+    single CUDA graph launch."""
+    import ctypes
+    ctx = tp.TopOpt(shape[0], shape[1], shape[2], nl, precision=tp.TP_MIXED, nrhs=nrhs)
+    ctx.autotune()
+    F = tp.multiload(shape[0], shape[1], shape[2], nrhs, nload, seed=0)
+    ctx.upload("F", F.ravel())
+    del F
+    ctx.init_design()
+    for _ in range(W):
+        ctx.design_iteration()
+    ctx.L.tp_profile_enable(ctx.ctx, 1)
+    ctx.L.tp_profile_reset(ctx.ctx)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    timed = [ctx.design_iteration() for _ in range(K)]
+    ev1.record()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    ctx.L.tp_profile_enable(ctx.ctx, 0)
+    # per-kernel times: one more design iteration with the CG loop driven from
+    # the host (kernels inside a graph launch are not timed one by one)
+    ctx.set_graph_solve(2)
+    ctx.L.tp_profile_enable(ctx.ctx, 1)
+    ctx.L.tp_profile_reset(ctx.ctx)
+    ctx.design_iteration()
+    nm, la, pms = ctypes.c_char_p(), ctypes.c_long(), ctypes.c_double()
+    ctx.L.tp_profile_get.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
+                                     ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_double)]
+    prof = {}
+    for i in range(ctx.L.tp_profile_classes()):
+        ctx.L.tp_profile_get(ctx.ctx, i, ctypes.byref(nm), ctypes.byref(la), ctypes.byref(pms))
+        prof[nm.value.decode()] = (la.value, pms.value)
+    ctx.L.tp_profile_enable(ctx.ctx, 0)
+    mem = ctx.L.tp_device_bytes(ctx.ctx)
+    ctx.close()
+    nn = (shape[0] + 1) * (shape[1] + 1) * (shape[2] + 1)
+    ne = shape[0] * shape[1] * shape[2]
+    out = {"workload": "%d load cases x %dx%dx%d -l %d, %d unit nodal loads per case on the end face (seed 0), "
+                       "mixed precision, summed compliance, CG loop as one CUDA graph launch" %
+                       ((nrhs,) + tuple(shape) + (nl, nload)),
+           "value": K / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms / K, "steps": K, "warmup": W,
+           "dofs_per_case": 3 * nn, "device_bytes": mem,
+           "cg_iters": [h.cgiters for h in timed], "compliance": [h.c for h in timed]}
+    total = sum(v[1] for v in prof.values()) or 1.0
+    out["kernels"] = {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / total, 4)}
+                      for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1]) if v[0]}
+    for k, b in (("fine_apply_f64", nrhs * 48 * nn + 8 * ne), ("fine_jacobi_f32", nrhs * 48 * nn + 4 * ne)):
+        if k in prof and prof[k][0]:
+            avg = prof[k][1] / prof[k][0] / 1000.0
+            out["kernels"][k].update({"columns": nrhs, "algorithmic_bytes": b, "gbs": round(b / avg / 1e9, 1),
+                                      "hbm_frac": round(b / avg / 1e9 / hbm, 4)})
+    return out
+
+
 def main():
     a = args_parse()
     if a.cpu_sample:
@@ -381,6 +444,9 @@ def main():
         "clocks": clk,
         "cg_iters": [h.cgiters for h in timed_a],
     }
+    if "D" in a.passes:
+        bshape = tuple(int(v) for v in a.batched_shape.split("x"))
+        line["batched"] = batched_pass(tp, torch, bshape, a.nl, a.batched_cases, 8, 1, 2, hbm)
     if rank == 0 and world == 1 and not a.no_cpu:
         cores = cpu_cores()
         s = cpu_sample(shape, a.nl, 1, cores)

@@ -183,9 +183,11 @@ tp_status tp_autotune(tp_ctx* c, double* ms_out);
  * loop then minimises the summed compliance of the cases. */
 tp_status tp_multiload(int nelx, int nely, int nelz, int ncase, int nload, unsigned long long seed,
                        double* F_host);
-/* on = 1: tp_solve runs the CG loop as one CUDA graph launch (a conditional
- * while node over the captured iteration) also for a single load; contexts
- * with nrhs > 1 always do. No counterpart in the reference. */
+/* How tp_solve drives the CG loop (no counterpart in the reference):
+ * on = 0 (default) one CUDA graph launch (a conditional while node over the
+ * captured iteration) for contexts with nrhs > 1, the host-driven loop of the
+ * reference for one load; 1 = the graph launch always; 2 = the host-driven
+ * loop always (every kernel then shows in the tp_profile_* timings). */
 tp_status tp_set_graph_solve(tp_ctx* c, int on);
 /* Per load case of the last tp_solve: iters[r] = index of the CG iteration at
  * which case r met the tolerance (-1 if it did not), relres[r] its relative

@@ -324,7 +324,7 @@ static void destroy_buffers(tp_ctx* c) {
     F(c->mgf_r[l]); F(c->mgf_z[l]); F(c->mgf_d[l]); F(c->mgf_t[l]);
     F(c->invD[l]); F(c->invDf[l]); F(c->st[l]); F(c->stf[l]); F(c->st_sub[l]);
   }
-  F(c->d_x); F(c->d_xphys); F(c->d_xnew); F(c->d_dc); F(c->d_dv); F(c->d_hs);
+  F(c->d_x); F(c->d_xphys); F(c->d_xnew); F(c->d_dc); F(c->d_dv); F(c->d_hs); F(c->d_ocb);
   F(c->d_E); F(c->d_Ef); F(c->d_F); F(c->d_U);
   F(c->d_r); F(c->d_z); F(c->d_p); F(c->d_q);
   F(c->d_red); F(c->d_scal); F(c->d_flag); F(c->scratch_invD); F(c->d_fw);
@@ -379,6 +379,7 @@ tp_status tp_create(const tp_params* p, tp_ctx** out) {
   ok = ok && (c->d_x = dalloc<double>(c, ne)) && (c->d_xphys = dalloc<double>(c, ne)) &&
        (c->d_xnew = dalloc<double>(c, ne)) && (c->d_dc = dalloc<double>(c, ne)) &&
        (c->d_dv = dalloc<double>(c, ne)) && (c->d_hs = dalloc<double>(c, ne)) &&
+       (c->d_ocb = dalloc<double>(c, ne)) && ((c->ocb_n = ne) > 0) &&
        (c->d_E = dalloc<double>(c, ne)) && (c->d_Ef = dalloc<float>(c, ne)) &&
        (c->d_F = dalloc<double>(c, nv)) && (c->d_U = dalloc<double>(c, nv)) &&
        (c->d_r = dalloc<double>(c, nv)) && (c->d_z = dalloc<double>(c, nv)) &&
@@ -616,7 +617,10 @@ tp_status tp_solve(tp_ctx* c, int* iters, double* relres) {
   if (st != TP_OK) return st;
   int it = 0;
   double rr = 0;
-  st = (c->p.nrhs > 1 || c->graph_solve) ? pcg_graph(c, &it, &rr) : pcg(c, c->d_F, c->d_U, &it, &rr);
+  // graph_solve: 0 the captured loop for several loads, host-driven for one;
+  // 1 always the captured loop; 2 always host-driven
+  const bool graph = c->graph_solve == 1 || (c->graph_solve == 0 && c->p.nrhs > 1);
+  st = graph ? pcg_graph(c, &it, &rr) : pcg(c, c->d_F, c->d_U, &it, &rr, c->p.nrhs);
   if (iters) *iters = it;
   if (relres) *relres = rr;
   return st;

@@ -175,7 +175,7 @@ extern "C" tp_status tp_solve_columns(tp_ctx* c, int* iters, double* relres) {
 }
 
 extern "C" tp_status tp_set_graph_solve(tp_ctx* c, int on) {
-  if (!c || on < 0 || on > 1) return TP_ERR_ARG;
+  if (!c || on < 0 || on > 2) return TP_ERR_ARG;
   c->graph_solve = on;
   return TP_OK;
 }

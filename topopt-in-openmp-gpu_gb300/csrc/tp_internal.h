@@ -110,6 +110,8 @@ struct tp_ctx {
          *d_dv = nullptr, *d_hs = nullptr;
   double* d_E = nullptr;  // E(xPhys) per fine element
   double* d_fw = nullptr; // filter weights per offset, (2*ceil(rmin))^3
+  double* d_ocb = nullptr;  // OC scratch: x sqrt(-dc/dv) per element
+  long ocb_n = 0;
   float* d_Ef = nullptr;
 
   // state: load and displacement (FP64), nrhs columns, column-contiguous

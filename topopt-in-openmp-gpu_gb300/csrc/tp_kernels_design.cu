@@ -267,16 +267,39 @@ __device__ __forceinline__ double oc_xnew(double x, double dc, double dv, double
   return (0.0 > cc) ? 0.0 : cc;                      // MAX(0.0, cc)
 }
 
-// one bisection step: partial sums of dv*(xnew - x) at lmid = (l1 + l2)/2
+// The bisection steps only need the volume change sum_e dv_e (xnew_e - x_e)
+// at each trial lmid. x sqrt(-dc/(dv lmid)) = B / sqrt(lmid) with
+// B = x sqrt(-dc/dv) formed once per update, which takes the division and the
+// square root of every element out of the ~50 steps (they agree with the
+// reference's expression to a few ulp; the final pass below evaluates the
+// reference's expression itself at the chosen lmid).
+__global__ void oc_prep_kernel(long n, const double* __restrict__ x, const double* __restrict__ dc,
+                               const double* __restrict__ dv, double* __restrict__ B) {
+  const long e = blockIdx.x * 256L + threadIdx.x;
+  if (e < n) B[e] = x[e] * sqrt(-dc[e] / dv[e]);
+}
+
+__device__ __forceinline__ double oc_clamp(double x, double xs) {
+  const double move = 0.2;
+  const double a = (x + move > xs) ? xs : x + move;
+  const double b = (1.0 > a) ? a : 1.0;
+  const double cc = (x - move > b) ? x - move : b;
+  return (0.0 > cc) ? 0.0 : cc;
+}
+
+// one bisection step: partial sums of dv*(xnew - x) at lmid = (l1 + l2)/2;
+// B = nullptr evaluates the reference's expression per element instead
 __global__ void oc_step_kernel(long n, const double* __restrict__ x, const double* __restrict__ dc,
-                               const double* __restrict__ dv, double* __restrict__ scal,
-                               double* __restrict__ partials) {
+                               const double* __restrict__ dv, const double* __restrict__ B,
+                               double* __restrict__ scal, double* __restrict__ partials) {
   if (scal[S_OCDONE] != 0.0) return;
   const double lmid = 0.5 * (scal[S_L2] + scal[S_L1]);
+  const double rl = 1.0 / sqrt(lmid);
   double s = 0.0;
   for (long e = blockIdx.x * 256L + threadIdx.x; e < n; e += (long)gridDim.x * 256) {
-    const double xn = oc_xnew(x[e], dc[e], dv[e], lmid);
-    s += dv[e] * (xn - x[e]);
+    const double xe = x[e];
+    const double xn = B ? oc_clamp(xe, B[e] * rl) : oc_xnew(xe, dc[e], dv[e], lmid);
+    s += dv[e] * (xn - xe);
   }
   s = bsum256(s);
   if (threadIdx.x == 0) partials[blockIdx.x] = s;
@@ -345,11 +368,16 @@ int oc_bisect(tp_ctx* c, long ne, double* x, double* xnew, const double* dc, con
   ProfScope ps(c, P_DESIGN);
   const int nb = blocks_for(ne);
   oc_init_kernel<<<1, 1, 0, c->s>>>(c->d_scal);
+  const double* B = nullptr;
+  if (c->d_ocb && ne <= c->ocb_n) {
+    oc_prep_kernel<<<grid_for(ne, 256), 256, 0, c->s>>>(ne, x, dc, dv, c->d_ocb);
+    B = c->d_ocb;
+  }
   const int kBatch = 24, kMaxSteps = 240;
   int taken = 0;
   for (;;) {
     for (int q = 0; q < kBatch; q++) {
-      oc_step_kernel<<<nb, 256, 0, c->s>>>(ne, x, dc, dv, c->d_scal, c->d_red);
+      oc_step_kernel<<<nb, 256, 0, c->s>>>(ne, x, dc, dv, B, c->d_scal, c->d_red);
       oc_finish_kernel<<<1, 256, 0, c->s>>>(c->d_red, nb, c->d_scal, g);
     }
     taken += kBatch;

@@ -73,6 +73,7 @@ struct Coarse {
 struct EcPlan {
   bool ok = false;
   int nyt = 0, nzg = 1, ngz = 0, zbase = 0, zextra = 0, ncx = 1, cx = 0;
+  int own = 0;  // sweep/residual: stage b and invD in shared memory too
 };
 struct EcGeom {
   int nx, ny, nz, ex, ey, ez, lim;

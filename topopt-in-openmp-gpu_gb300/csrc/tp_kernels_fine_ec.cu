@@ -146,6 +146,9 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
                                                       const T* __restrict__ invD, T omega,
                                                       double* __restrict__ partials) {
   constexpr int NST = 3;  // slab stages: planes L, L+1 in use, L+2 in flight
+  // the items of the columns shared by warps, (ey/32 + 1) * rows * 3, fit one
+  // per thread of a group when 3 * RMAX <= 16
+  static_assert(3 * RMAX <= 16, "one shared-column item per thread");
   constexpr bool HASB = (MODE == EC_JACOBI || MODE == EC_RESID);
   constexpr bool HASD = (MODE == EC_JACOBI);
   extern __shared__ __align__(16) unsigned char smem[];
@@ -199,25 +202,35 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
   for (int q = tid; q < nzg * (nwy + 1) * RMAX * 3; q += nthr) carry_b[q] = T(0);
 
   double dot = 0.0;
-  // one output component of plane P, node row kr, column j
-  auto epi = [&](const T* uP, const T* bP, const T* dP, int P, int kr, int j, int c, T y) {
+  // output components [c0, c1) of plane P, node row kr, column j
+  auto epi = [&](const T* uP, const T* bP, const T* dP, int P, int kr, int j, int c0, int c1, const T* y) {
     if (P < i0) return;
-    const long li = (long)(kr - kmin) * row3 + 3 * j + c;
-    const long n3 = ((long)P * nz + kr) * row3 + 3 * j + c;
-    const T u = uP[li];
-    if (P == 0 && (j < g.lim || j >= ny - g.lim)) y = u;  // fixed DOF: identity row
-    if (MODE == EC_APPLY || MODE == EC_APPLY_DOT) out[n3] = y;
-    if (MODE == EC_APPLY_DOT) dot += (double)u * (double)y;
-    if (HASB) {
-      const long lo = (long)(kr - K0) * row3 + 3 * j + c;
-      const T b = stage_own ? bP[lo] : bv[n3];
-      if (MODE == EC_RESID) out[n3] = b - y;
-      if (MODE == EC_JACOBI) {
-        const T d = stage_own ? dP[lo] : invD[n3];
-        out[n3] = u + omega * d * (b - y);
+    const long li = (long)(kr - kmin) * row3 + 3 * j;
+    const long n3 = ((long)P * nz + kr) * row3 + 3 * j;
+    const long lo = (long)(kr - K0) * row3 + 3 * j;
+    const bool fixed = P == 0 && (j < g.lim || j >= ny - g.lim);  // identity rows
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      if (c < c0 || c >= c1) continue;
+      const T u = uP[li + c];
+      const T yc = fixed ? u : y[c];
+      if (MODE == EC_APPLY || MODE == EC_APPLY_DOT) out[n3 + c] = yc;
+      if (MODE == EC_APPLY_DOT) dot += (double)u * (double)yc;
+      if (HASB) {
+        const T b = stage_own ? bP[lo + c] : bv[n3 + c];
+        if (MODE == EC_RESID) out[n3 + c] = b - yc;
+        if (MODE == EC_JACOBI) {
+          const T d = stage_own ? dP[lo + c] : invD[n3 + c];
+          out[n3 + c] = u + omega * d * (b - yc);
+        }
       }
     }
   };
+  // the columns shared by two warps (0, 32, 64, ...): one (column, row,
+  // component) item per thread of the group, fixed for the whole launch
+  const int ncb = ey / 32 + 1;
+  const bool tail = gact && t < ncb * nrow * 3;
+  const int tc = tail ? t % 3 : 0, tr = tail ? (t / 3) % nrow : 0, tcb = tail ? t / (3 * nrow) : 0;
   auto own_at = [&](unsigned char* base, const T* v, int p) -> const T* {
     if (!stage_own) return nullptr;
     return ec_view<T>(base + (p & 1) * g.own_bytes, own_src(v, p));
@@ -235,10 +248,11 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
 
   for (int L = Ls; L < Le; ++L) {
     T Ev[RMAX + 1];
+    const T* EL = E + ((long)L * ez + (k0 - 1)) * ey + t;
 #pragma unroll
     for (int q = 0; q <= RMAX; q++) {
       const int ek = k0 - 1 + q;
-      Ev[q] = (lact && q <= nrow && ek >= 0 && ek < ez) ? E[((long)L * ez + ek) * g.ey + t] : T(0);
+      Ev[q] = (lact && q <= nrow && ek >= 0 && ek < ez) ? EL[(long)q * ey] : T(0);
     }
     if (L + 2 <= Le) issue_slab(L + 2);
     if (L + 1 <= Le) issue_own(L + 1);
@@ -398,12 +412,13 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
               bnd_own[bo + 3 + c] = own1[c];
             }
           } else if (lact) {
+            T y[3];
 #pragma unroll
             for (int c = 0; c < 3; c++) {
-              const T y = carry[r][c] + own0[c] + rv0[c];
+              y[c] = carry[r][c] + own0[c] + rv0[c];
               carry[r][c] = own1[c] + rv1[c];
-              epi(u0, bL, dL, L, k0 + r, t + 1, c, y);
             }
+            epi(u0, bL, dL, L, k0 + r, t + 1, 0, 3, y);
           }
         }
 #pragma unroll
@@ -416,27 +431,24 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
     __syncthreads();
     // columns 0, 32, 64, ...: the own share of lane 31 of the warp on the
     // left plus the share of lane 0 of the warp on the right
-    if (gact) {
-      const int ncb = ey / 32 + 1;
-      for (int it = t; it < ncb * nrow * 3; it += nyt) {
-        const int c = it % 3, r = (it / 3) % nrow, cb = it / (3 * nrow);
-        const int j = 32 * cb;
-        T o0 = T(0), o1 = T(0), n0 = T(0), n1 = T(0);
-        if (cb >= 1) {
-          const int bo = ((tz * nwy + cb - 1) * RMAX + r) * 6;
-          o0 = bnd_own[bo + c];
-          o1 = bnd_own[bo + 3 + c];
-        }
-        if (j < ey) {
-          const int bo = ((tz * nwy + cb) * RMAX + r) * 6;
-          n0 = bnd_nb[bo + c];
-          n1 = bnd_nb[bo + 3 + c];
-        }
-        T& cr = carry_b[((tz * (nwy + 1) + cb) * RMAX + r) * 3 + c];
-        const T y = cr + o0 + n0;
-        cr = o1 + n1;
-        epi(u0, bL, dL, L, k0 + r, j, c, y);
+    if (tail) {
+      const int j = 32 * tcb;
+      T o0 = T(0), o1 = T(0), n0 = T(0), n1 = T(0);
+      if (tcb >= 1) {
+        const int bo = ((tz * nwy + tcb - 1) * RMAX + tr) * 6;
+        o0 = bnd_own[bo + tc];
+        o1 = bnd_own[bo + 3 + tc];
       }
+      if (j < ey) {
+        const int bo = ((tz * nwy + tcb) * RMAX + tr) * 6;
+        n0 = bnd_nb[bo + tc];
+        n1 = bnd_nb[bo + 3 + tc];
+      }
+      T& cr = carry_b[((tz * (nwy + 1) + tcb) * RMAX + tr) * 3 + tc];
+      const T v = cr + o0 + n0;
+      cr = o1 + n1;
+      const T y[3] = {v, v, v};  // only component tc is stored
+      epi(u0, bL, dL, L, k0 + tr, j, tc, tc + 1, y);
     }
     __syncthreads();
   }
@@ -451,14 +463,12 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
     if (lact && lane != 31) {
 #pragma unroll
       for (int r = 0; r < RMAX; r++)
-        if (r < nrow)
-#pragma unroll
-          for (int c = 0; c < 3; c++) epi(uP, bP, dP, P, k0 + r, t + 1, c, carry[r][c]);
+        if (r < nrow) epi(uP, bP, dP, P, k0 + r, t + 1, 0, 3, carry[r]);
     }
-    const int ncb = ey / 32 + 1;
-    for (int it = t; it < ncb * nrow * 3; it += nyt) {
-      const int c = it % 3, r = (it / 3) % nrow, cb = it / (3 * nrow);
-      epi(uP, bP, dP, P, k0 + r, 32 * cb, c, carry_b[((tz * (nwy + 1) + cb) * RMAX + r) * 3 + c]);
+    if (tail) {
+      const T v = carry_b[((tz * (nwy + 1) + tcb) * RMAX + tr) * 3 + tc];
+      const T y[3] = {v, v, v};
+      epi(uP, bP, dP, P, k0 + tr, 32 * tcb, tc, tc + 1, y);
     }
   }
   if (MODE == EC_APPLY_DOT) {
@@ -554,13 +564,14 @@ static size_t ec_smem(const EcGeom& g, const EcPlan& p, size_t tsize) {
 template <typename T, int MODE>
 static int ec_launch(tp_ctx* c, const EcPlan& p, const T* E, const T* in, T* out, const T* b, const T* invD,
                      T omega, int nrhs, long vstride) {
-  const bool own = (MODE == EC_JACOBI || MODE == EC_RESID) && sizeof(T) == 4;
+  const bool own = (MODE == EC_JACOBI || MODE == EC_RESID) && p.own;
   const EcGeom g = ec_geom(c, p, sizeof(T), own, vstride);
   const size_t smem = ec_smem(g, p, sizeof(T));
   auto kern = fine_ec_kernel<T, MODE, kEcRmax>;
   static size_t set_for = 0;  // largest size the attribute was raised to
   if (smem > 48 * 1024 && smem > set_for) {
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+      cudaGetLastError();  // not sticky: the error is reported through c->err
       c->err = "fine_ec: shared memory request of " + std::to_string(smem) + " bytes refused";
       return 0;
     }
@@ -611,6 +622,10 @@ template <typename T>
 float ec_time(tp_ctx* c, int mode, const tp::EcPlan& p, const T* E, const T* in, T* out, const T* b,
               const T* d) {
   using namespace tp;
+  int smax = 0;
+  cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+  const bool own = (mode == FM_JACOBI || mode == FM_RESID) && p.own;
+  if (ec_smem(ec_geom(c, p, sizeof(T), own, 0), p, sizeof(T)) > (size_t)smax) return 1e30f;  // does not fit
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -650,10 +665,14 @@ void ec_tune(tp_ctx* c, tp::EcPlan* plans, const T* E, const T* in, T* out, cons
       for (int mult = 1; mult <= 6; mult++) {
         if (!ec_plan(c, nzg, (mult * sms + zctas - 1) / zctas, &p) || p.ncx == last_ncx) continue;
         last_ncx = p.ncx;
-        const float ms = ec_time<T>(c, mode, p, E, in, out, b, d);
-        if (ms < tbest) {
-          tbest = ms;
-          best = p;
+        const int nown = (mode == FM_JACOBI || mode == FM_RESID) ? 2 : 1;
+        for (int own = 0; own < nown; own++) {
+          p.own = own;
+          const float ms = ec_time<T>(c, mode, p, E, in, out, b, d);
+          if (ms < tbest) {
+            tbest = ms;
+            best = p;
+          }
         }
       }
     }

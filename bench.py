@@ -176,6 +176,20 @@ def dist():
     return world, rank, local
 
 
+def whole_job(times, K, world, device="cuda"):
+    """Replicas: every rank runs the same K design iterations on its own GPU,
+    with no data exchange. The job's time is the slowest rank's (max over
+    ranks, one all-reduce) and its throughput counts every rank's
+    iterations: world * K / max time."""
+    if world > 1:
+        import torch
+        import torch.distributed as td
+        t = torch.tensor(times, device=device, dtype=torch.float64)
+        td.all_reduce(t, op=td.ReduceOp.MAX)
+        times = [float(v) for v in t]
+    return times, [world * K / v for v in times]
+
+
 def run_reference(a):
     world, rank, _ = dist()
     if rank != 0:
@@ -387,14 +401,7 @@ def main():
                 "cg_iters_fp64": [h.cgiters for h in timed_c], "cg_iters_mixed": [h.cgiters for h in timed_a]}
 
     # whole-job numbers: max time over ranks, units summed over ranks
-    t_a, t_b = ms_a / 1000.0, wall_b
-    if world > 1:
-        import torch.distributed as td
-        t = torch.tensor([t_a, t_b], device="cuda", dtype=torch.float64)
-        td.all_reduce(t, op=td.ReduceOp.MAX)
-        t_a, t_b = float(t[0]), float(t[1])
-    value = world * K / t_a
-    e2e_value = world * K / t_b
+    (t_a, t_b), (value, e2e_value) = whole_job([ms_a / 1000.0, wall_b], K, world)
 
     nbytes, flops = fine_bytes(shape)
     hbm, peak_kind = peaks()

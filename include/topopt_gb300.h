@@ -189,6 +189,18 @@ tp_status tp_multiload(int nelx, int nely, int nelz, int ncase, int nload, unsig
  * reference for one load; 1 = the graph launch always; 2 = the host-driven
  * loop always (every kernel then shows in the tp_profile_* timings). */
 tp_status tp_set_graph_solve(tp_ctx* c, int on);
+
+/* Checkpoint/restart of the loop state (no counterpart in the reference):
+ * x, xPhys, U and F (all load cases) with the grid, level count, load-case
+ * count, precision, volfrac, rmin and the caller's design-iteration number,
+ * in one binary file with an FNV-1a checksum (layout in tp_checkpoint.cpp),
+ * written to <path>.tmp and renamed. Load requires the same grid and nrhs;
+ * it rejects a missing, truncated or corrupt file with TP_ERR_ARG.
+ * tp_checkpoint_info reads and checks a file without a context: info[7] =
+ * {nelx, nely, nelz, nl, nrhs, precision, loop}. */
+tp_status tp_checkpoint_save(tp_ctx* c, const char* path, int loop);
+tp_status tp_checkpoint_load(tp_ctx* c, const char* path, int* loop);
+tp_status tp_checkpoint_info(const char* path, int* info);
 /* Per load case of the last tp_solve: iters[r] = index of the CG iteration at
  * which case r met the tolerance (-1 if it did not), relres[r] its relative
  * residual then (nrhs entries each). */

@@ -101,11 +101,24 @@ def load():
     L.tp_multiload.argtypes = [I, I, I, I, I, ctypes.c_ulonglong, P]
     L.tp_set_graph_solve.argtypes = [V, I]
     L.tp_solve_columns.argtypes = [V, P, P]
+    L.tp_checkpoint_save.argtypes = [V, ctypes.c_char_p, I]
+    L.tp_checkpoint_load.argtypes = [V, ctypes.c_char_p, ctypes.POINTER(I)]
+    L.tp_checkpoint_info.argtypes = [ctypes.c_char_p, P]
     L.tp_set_rmin.argtypes = [V, D]
     L.tp_design_iteration.argtypes = [V, ctypes.POINTER(TpIterInfo)]
     L.tp_run.argtypes = [V, I, ctypes.POINTER(TpIterInfo), ctypes.POINTER(I)]
     _lib = L
     return L
+
+
+def checkpoint_info(path):
+    """(nelx, nely, nelz, nl, nrhs, precision, loop) of a checkpoint file, or
+    TopOptError if it is missing, truncated or corrupt."""
+    info = np.zeros(7, np.int32)
+    st = load().tp_checkpoint_info(os.fsencode(path), info.ctypes.data)
+    if st != 0:
+        raise TopOptError(st, "checkpoint " + str(path))
+    return tuple(int(v) for v in info)
 
 
 def multiload(nelx, nely, nelz, ncase, nload, seed=0):
@@ -211,6 +224,15 @@ class TopOpt:
     def set_fine_variant(self, variant):
         """0: element-centric level-0 kernel where it applies; 1: node-centric stencil."""
         self._check(self.L.tp_set_fine_variant(self.ctx, variant))
+
+    def checkpoint_save(self, path, loop):
+        self._check(self.L.tp_checkpoint_save(self.ctx, os.fsencode(path), loop))
+
+    def checkpoint_load(self, path):
+        """Restores x, xPhys, U, F; returns the saved design-iteration number."""
+        loop = ctypes.c_int(0)
+        self._check(self.L.tp_checkpoint_load(self.ctx, os.fsencode(path), ctypes.byref(loop)))
+        return loop.value
 
     def solve_columns(self):
         """(iteration index, relres) of each load case in the last solve."""

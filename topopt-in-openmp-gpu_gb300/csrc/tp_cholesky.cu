@@ -9,7 +9,7 @@
 // column-major block.
 //   factor : right-looking blocked band Cholesky, panel width NB:
 //            POTRF of the NB x NB diagonal block (one CTA), TRSM of the panel
-//            below it (one thread per row), SYRK update of the trailing band
+//            below it (one warp per row), SYRK update of the trailing band
 //            triangle (32x32 tiles). A non-positive pivot sets *info and is
 //            replaced by 1 so the factor completes; the host reports
 //            TP_ERR_NOT_SPD.
@@ -75,7 +75,13 @@ void coarse_alloc(tp_ctx* c) {
   C.rhs = C.vec + 16 * C.n;
   C.sol = C.vec + 17 * C.n;
   cudaMalloc(&C.info, sizeof(int));
-  cudaMalloc(&C.linv, NB * NB * sizeof(double));
+  cudaMalloc(&C.linv, (NB * NB + NB) * sizeof(double));  // current diagonal block of L and 1/L(j,j)
+  cudaStreamCreateWithFlags(&C.s2, cudaStreamNonBlocking);
+  int lo = 0, hi = 0;
+  cudaDeviceGetStreamPriorityRange(&lo, &hi);
+  C.prio_high = hi;
+  cudaEventCreateWithFlags(&C.ev_panel, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&C.ev_rest, cudaEventDisableTiming);
   c->mem_bytes += (long)(C.band_elems + 2 * dsz + lsz + C.n * 18) * 8;
 }
 
@@ -90,6 +96,9 @@ void coarse_free(tp_ctx* c) {
   if (C.factor_exec) cudaGraphExecDestroy(C.factor_exec);
   cudaFree(C.info);
   cudaFree(C.linv);
+  if (C.s2) cudaStreamDestroy(C.s2);
+  if (C.ev_panel) cudaEventDestroy(C.ev_panel);
+  if (C.ev_rest) cudaEventDestroy(C.ev_rest);
   C = Coarse();
 }
 
@@ -107,9 +116,9 @@ void coarse_assemble(tp_ctx* c) {
 // ----------------------------------------------------------------------------
 // Factor the nb x nb diagonal block held (updated, lower part, zero above the
 // diagonal) in S with the 256 threads of the CTA: L into S and into the band,
-// and L^{-1} into Inv and linv_out (row-major 32x32, zero above the
-// diagonal). A non-positive pivot sets *info (first column + 1) and is
-// replaced by 1 so that the factor completes.
+// and into lblk_out (row-major 32x32, zero above the diagonal, followed by
+// the 32 reciprocals 1/L(j,j)). A non-positive pivot sets *info (first
+// column + 1) and is replaced by 1 so that the factor completes.
 //
 // This block lies on the factorisation's critical path (one per 32 columns),
 // and FP64 issue per SM is scarce on this part, so the work is spread over
@@ -117,8 +126,9 @@ void coarse_assemble(tp_ctx* c) {
 // one reciprocal square root: thread (i, g) owns row i, columns g, g+8, g+16,
 // g+24; column j is updated unscaled (with 1/L(j,j)^2) and scaled one step
 // later; the owner of (j+1, j+1) forms the next pivot right after its last
-// update. L^{-1} follows by recursive doubling over diagonal blocks,
-// Inv_BA = -Inv_BB (L_BA Inv_AA), with Tm as scratch.
+// update. (No inverse is formed: the panel solve below substitutes with L
+// directly, which keeps this block -- the part of each 32-column step that
+// no other CTA can share -- short.)
 __device__ __forceinline__ void diag_pivot(double (*S)[NB + 1], double* rp, int j, long k, int* info) {
   double d = S[j][j];
   if (!(d > 0.0)) {
@@ -127,19 +137,19 @@ __device__ __forceinline__ void diag_pivot(double (*S)[NB + 1], double* rp, int 
   }
   const double r = rsqrt(d);
   rp[j] = r;
+  rp[NB + j] = r * r;  // 1/d for the unscaled column update
   S[j][j] = d * r;
 }
 
 __device__ void factor_diag_block(double* __restrict__ B, long bw, long k, int nb, double (*S)[NB + 1],
-                                  double (*Inv)[NB + 1], double (*Tm)[NB + 1], double* __restrict__ linv_out,
-                                  int* info) {
-  __shared__ double rp[NB];
+                                  double* __restrict__ lblk_out, int* info) {
+  __shared__ double rp[2 * NB];  // 1/L(j,j), then 1/L(j,j)^2
   const int tid = threadIdx.x;
   const int i = tid >> 3, g = tid & 7;
   if (tid == 0) diag_pivot(S, rp, 0, k, info);
   __syncthreads();
   for (int j = 0; j < nb; j++) {
-    const double r2 = rp[j] * rp[j];
+    const double r2 = rp[NB + j];
     if (j >= 1 && g == 0 && i >= j && i < nb) S[i][j - 1] *= rp[j - 1];
     if (i > j && i < nb) {
       const double sij = S[i][j] * r2;
@@ -152,78 +162,69 @@ __device__ void factor_diag_block(double* __restrict__ B, long bw, long k, int n
     if (j + 1 < nb && i == j + 1 && g == ((j + 1) & 7)) diag_pivot(S, rp, j + 1, k, info);
     __syncthreads();
   }
-  for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
-    const int r = idx / NB, cc = idx % NB;
-    Inv[r][cc] = (r == cc && r < nb) ? rp[r] : 0.0;
-  }
-  __syncthreads();
-  for (int s = 1; s < NB; s *= 2) {
-    const int ent = (NB / (2 * s)) * s * s;  // entries of all L_BA Inv_AA products
-    for (int e = tid; e < ent; e += blockDim.x) {
-      const int p = (e / (s * s)) * 2 * s, a = (e % (s * s)) / s, b = e % s;
-      double v = 0.0;
-      for (int m = b; m < s; m++) v += S[p + s + a][p + m] * Inv[p + m][p + b];
-      Tm[p + s + a][p + b] = v;
-    }
-    __syncthreads();
-    for (int e = tid; e < ent; e += blockDim.x) {
-      const int p = (e / (s * s)) * 2 * s, a = (e % (s * s)) / s, b = e % s;
-      double v = 0.0;
-      for (int m = 0; m <= a; m++) v += Inv[p + s + a][p + s + m] * Tm[p + s + m][p + b];
-      Inv[p + s + a][p + b] = -v;
-    }
-    __syncthreads();
-  }
   for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
     const int r = idx % NB, cc = idx / NB;
-    if (r < nb && cc < nb && r >= cc && r - cc <= bw) B[(k + cc) * bw + (k + r)] = S[r][cc];
-    linv_out[r * NB + cc] = Inv[r][cc];
+    const bool in = r < nb && cc < nb && r >= cc;
+    if (in && r - cc <= bw) B[(k + cc) * bw + (k + r)] = S[r][cc];
+    lblk_out[r * NB + cc] = in ? S[r][cc] : 0.0;
   }
+  if (threadIdx.x < NB) lblk_out[NB * NB + threadIdx.x] = threadIdx.x < nb ? rp[threadIdx.x] : 0.0;
 }
 
 // the first diagonal block (later ones are factored inside syrk_kernel)
 __global__ void potrf_kernel(double* __restrict__ B, long bw, long k, int nb, double* __restrict__ linv, int* info) {
-  __shared__ double S[NB][NB + 1], Inv[NB][NB + 1], Tm[NB][NB + 1];
+  __shared__ double S[NB][NB + 1];
   for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
     const int r = idx % NB, cc = idx / NB;
     S[r][cc] = (r < nb && cc < nb && r >= cc) ? bget(B, bw, k + r, k + cc) : 0.0;
   }
   __syncthreads();
-  factor_diag_block(B, bw, k, nb, S, Inv, Tm, linv, info);
+  factor_diag_block(B, bw, k, nb, S, linv, info);
 }
 
-// panel rows R0..R1 of columns k..k+nb-1: L(r, k+t) = sum_{t'<=t} A(r, k+t') Linv(t, t');
-// one warp per row, lane t computes output t
+// panel rows R0..R1 of columns k..k+nb-1: solve x L_kk^T = a for each row,
+// one warp per row, lane t holding x_t: at step p lane p finishes
+// x_p = acc_p / L(p,p) and broadcasts it, lanes t > p subtract L(t,p) x_p
 __global__ void trsm_kernel(double* __restrict__ B, long bw, long k, int nb, long R0, long R1,
-                            const double* __restrict__ linv) {
-  __shared__ double Li[NB][NB + 1];
-  for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) Li[idx / NB][idx % NB] = linv[idx];
+                            const double* __restrict__ lblk) {
+  __shared__ double Lb[NB][NB + 1], rp[NB];
+  for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) Lb[idx / NB][idx % NB] = lblk[idx];
+  if (threadIdx.x < NB) rp[threadIdx.x] = lblk[NB * NB + threadIdx.x];
   __syncthreads();
   const int w = threadIdx.x >> 5, t = threadIdx.x & 31;
   const long r = R0 + (long)blockIdx.x * (blockDim.x >> 5) + w;
   if (r > R1) return;
-  const double a = (t < nb) ? bget(B, bw, r, k + t) : 0.0;
+  double acc = (t < nb) ? bget(B, bw, r, k + t) : 0.0;
   double x = 0.0;
 #pragma unroll
-  for (int tp = 0; tp < NB; tp++) {
-    const double at = __shfl_sync(0xffffffffu, a, tp);
-    if (tp <= t) x += at * Li[t][tp];
+  for (int p = 0; p < NB; p++) {
+    const double xp = __shfl_sync(0xffffffffu, acc * rp[p], p);
+    if (t == p) x = xp;
+    if (t > p) acc -= Lb[t][p] * xp;
   }
   if (t < nb && r - (k + t) <= bw) B[(k + t) * bw + r] = x;
 }
 
-// A(r,c) -= sum_t L(r,k+t) L(c,k+t), R0 <= c <= r <= R1, 32x32 tiles. The CTA of
-// tile (0,0) -- the next diagonal block -- then factors it for the next step.
+// A(r,c) -= sum_t L(r,k+t) L(c,k+t), R0 <= c <= r <= R1, 32x32 tiles (tr, tc)
+// of the trailing triangle. part 1: the first tile column only (tc = 0, the
+// next panel), whose tile (0,0) -- the next diagonal block -- is then
+// factored by its CTA for the next step; part 2: the other tiles (tc >= 1).
 __global__ void syrk_kernel(double* __restrict__ B, long bw, long n, long k, int nb, long R0, long R1,
-                            double* __restrict__ linv, int* info) {
+                            double* __restrict__ linv, int* info, int part) {
   __shared__ double Lr[NB][33], Lc[NB][33];
-  __shared__ double S[NB][NB + 1], Inv[NB][NB + 1];
-  // blockIdx.x -> lower-triangular tile (tr, tc)
-  const long b = blockIdx.x;
-  long tr = (long)((sqrt(8.0 * (double)b + 1.0) - 1.0) / 2.0);
-  while ((tr + 1) * (tr + 2) / 2 <= b) tr++;
-  while (tr * (tr + 1) / 2 > b) tr--;
-  const long tc = b - tr * (tr + 1) / 2;
+  __shared__ double S[NB][NB + 1];
+  long tr, tc;
+  if (part == 1) {
+    tr = blockIdx.x;
+    tc = 0;
+  } else {  // blockIdx.x -> lower-triangular tile among those with tc >= 1
+    const long b = blockIdx.x;
+    long q = (long)((sqrt(8.0 * (double)b + 1.0) - 1.0) / 2.0);
+    while ((q + 1) * (q + 2) / 2 <= b) q++;
+    while (q * (q + 1) / 2 > b) q--;
+    tr = q + 1;
+    tc = b - q * (q + 1) / 2 + 1;
+  }
   const long rb = R0 + tr * 32, cb = R0 + tc * 32;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 256 threads
   for (int t = ty; t < NB; t += 8) {
@@ -232,7 +233,7 @@ __global__ void syrk_kernel(double* __restrict__ B, long bw, long n, long k, int
     Lc[t][tx] = (t < nb && cc <= R1) ? bget(B, bw, cc, k + t) : 0.0;
   }
   __syncthreads();
-  const bool diag_next = (b == 0);
+  const bool diag_next = part == 1 && tr == 0;
   const long r = rb + tx;
 #pragma unroll
   for (int q = 0; q < 4; q++) {
@@ -253,7 +254,7 @@ __global__ void syrk_kernel(double* __restrict__ B, long bw, long n, long k, int
   if (diag_next) {
     __syncthreads();
     const int nb2 = (int)lmin((long)NB, n - R0);
-    factor_diag_block(B, bw, R0, nb2, S, Inv, Lr, linv, info);
+    factor_diag_block(B, bw, R0, nb2, S, linv, info);
   }
 }
 
@@ -352,20 +353,55 @@ __global__ void lrow_kernel(const double* __restrict__ B, long bw, long n, int n
   }
 }
 
+// Lookahead over two streams. Per 32-column step k: the panel solve T_k, then
+// on the main stream the update of the next panel's tile column with the
+// factorisation of the next diagonal block (the chain every step waits on),
+// and on the second stream the rest of the trailing update, which overlaps
+// that chain and the next step's panel solve. The next step's first-column
+// update waits for this step's rest, which writes the same tiles.
 static void coarse_factor_launches(tp_ctx* c, size_t dinv_smem) {
   Coarse& C = c->coarse;
-  cudaMemsetAsync(C.info, 0, sizeof(int), c->s);
-  potrf_kernel<<<1, 256, 0, c->s>>>(C.band, C.bw, 0, (int)std::min((long)NB, C.n), C.linv, C.info);
+  cudaStream_t s = c->s, s2 = C.s2;
+  cudaMemsetAsync(C.info, 0, sizeof(int), s);
+  potrf_kernel<<<1, 256, 0, s>>>(C.band, C.bw, 0, (int)std::min((long)NB, C.n), C.linv, C.info);
+  bool rest_pending = false;
   for (long k = 0; k < C.n; k += NB) {
     const int nb = (int)std::min((long)NB, C.n - k);
     const long R0 = k + nb, R1 = std::min(C.n - 1, k + nb - 1 + C.bw);
     if (R0 <= R1) {
       const long m = R1 - R0 + 1;
-      trsm_kernel<<<(unsigned)((m + 7) / 8), 256, 0, c->s>>>(C.band, C.bw, k, nb, R0, R1, C.linv);
+      // the chain's kernels run at the highest priority, so that their CTAs
+      // take the SMs first as the trailing update's CTAs retire
+      cudaLaunchAttribute pri[1];
+      pri[0].id = cudaLaunchAttributePriority;
+      pri[0].val.priority = C.prio_high;
+      cudaLaunchConfig_t cfg = {};
+      cfg.blockDim = dim3(256);
+      cfg.stream = s;
+      cfg.attrs = pri;
+      cfg.numAttrs = 1;
+      cfg.gridDim = dim3((unsigned)((m + 7) / 8));
+      double* band = C.band;
+      const long bw = C.bw, n = C.n;
+      const double* lc = C.linv;
+      cudaLaunchKernelEx(&cfg, trsm_kernel, band, bw, k, nb, R0, R1, lc);
       const long T = (m + 31) / 32;
-      syrk_kernel<<<(unsigned)(T * (T + 1) / 2), 256, 0, c->s>>>(C.band, C.bw, C.n, k, nb, R0, R1, C.linv, C.info);
+      if (T > 1) {
+        cudaEventRecord(C.ev_panel, s);
+        cudaStreamWaitEvent(s2, C.ev_panel, 0);
+      }
+      if (rest_pending) cudaStreamWaitEvent(s, C.ev_rest, 0);
+      cfg.gridDim = dim3((unsigned)T);
+      cudaLaunchKernelEx(&cfg, syrk_kernel, band, bw, n, k, nb, R0, R1, C.linv, C.info, 1);
+      rest_pending = false;
+      if (T > 1) {
+        syrk_kernel<<<(unsigned)(T * (T - 1) / 2), 256, 0, s2>>>(C.band, C.bw, C.n, k, nb, R0, R1, C.linv, C.info, 2);
+        cudaEventRecord(C.ev_rest, s2);
+        rest_pending = true;
+      }
     }
   }
+  if (rest_pending) cudaStreamWaitEvent(s, C.ev_rest, 0);
   dinv_kernel<<<dim3(C.nbs / 32, C.nblk), kDinvThreads, dinv_smem, c->s>>>(C.band, C.bw, C.n, C.nbs, C.dinv, C.dinvT);
   lrow_kernel<<<dim3((unsigned)((C.bw + 31) / 32), C.nbs / 32, C.nblk), dim3(32, 8), 0, c->s>>>(C.band, C.bw, C.n,
                                                                                                C.nbs, C.lrow);
@@ -383,7 +419,8 @@ void coarse_factor(tp_ctx* c) {
     if (cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
       coarse_factor_launches(c, smem);
       if (cudaStreamEndCapture(c->s, &g) == cudaSuccess && g) {
-        if (cudaGraphInstantiate(&C.factor_exec, g, 0) != cudaSuccess) C.factor_exec = nullptr;
+        if (cudaGraphInstantiate(&C.factor_exec, g, cudaGraphInstantiateFlagUseNodePriority) != cudaSuccess)
+          C.factor_exec = nullptr;
         cudaGraphDestroy(g);
       }
     }

@@ -62,9 +62,12 @@ struct Coarse {
   double* rhs = nullptr;
   double* sol = nullptr;
   int* info = nullptr;          // device status: first non-positive pivot + 1, 0 if none
-  double* linv = nullptr;       // inverse of the current 32x32 diagonal block of the factor
+  double* linv = nullptr;       // current 32x32 diagonal block of L (row-major) and its 32 reciprocal pivots
   cudaGraphExec_t graph_exec = nullptr;   // the captured block-solve sequence
   cudaGraphExec_t factor_exec = nullptr;  // the captured factorisation sequence
+  cudaStream_t s2 = nullptr;    // second stream of the factorisation's lookahead
+  cudaEvent_t ev_panel = nullptr, ev_rest = nullptr;
+  int prio_high = 0;            // highest stream priority of the device (the lookahead chain)
 };
 
 // Launch plan of the element-centric level-0 kernel (tp_kernels_fine_ec.cu):

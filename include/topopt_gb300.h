@@ -168,6 +168,19 @@ tp_status tp_set_cg(tp_ctx* c, double cgtol, int cgmax, int nswp, double omega);
  * applies (nely <= 256, 16-byte aligned vectors), else the node-centric
  * stencil; variant 1 = the node-centric stencil everywhere. */
 tp_status tp_set_fine_variant(tp_ctx* c, int variant);
+/* Coarsest-level solve selection (no counterpart in the reference, whose
+ * coarse solve is cholmod_solve2, stencil_assembly.c:476-484): variant 0 =
+ * both triangular sweeps as one cooperative launch with grid barriers
+ * between the block steps, wherever its launch plan applies; variant 1 = two
+ * launches per block step. Each variant sums in a fixed order, so repeated
+ * solves agree bit for bit; the two variants agree to rounding. */
+tp_status tp_set_coarse_solve_variant(tp_ctx* c, int variant);
+/* Failure detection of the single-launch coarse solve (host-side fault
+ * injection, for tests): each grid-barrier wait gives up after spin polls
+ * (0 = the default, about a second) and, with missing = 1, waits for one
+ * arrival that never comes, so every wait runs out. The solve then reports
+ * TP_ERR_TIMEOUT and the context stays usable; (0, 0) restores the defaults. */
+tp_status tp_fault_coarse_barrier(tp_ctx* c, long spin, int missing);
 /* Times the element-centric kernel's launch shapes (z groups per CTA, x
  * chunks) for each precision and fused mode on the context's grid and keeps
  * the fastest. It overwrites the solver work vectors (not F, U, x, xPhys):

@@ -248,6 +248,7 @@ static tp_status pcg(tp_ctx* c, const double* b, double* u, int* iters, double* 
     if (!std::isfinite(rr)) {
       *iters = it;
       *relres = rr;
+      if (coarse_status(c) != TP_OK) return TP_ERR_TIMEOUT;
       c->err = "CG: non-finite residual";
       return TP_ERR_NONFINITE;
     }
@@ -259,6 +260,8 @@ static tp_status pcg(tp_ctx* c, const double* b, double* u, int* iters, double* 
   *iters = it;
   *relres = (double)(float)rr;  // the reference reports it through a float
   tp_status st = check(c);
+  if (st != TP_OK) return st;
+  st = coarse_status(c);
   if (st != TP_OK) return st;
   return converged ? TP_OK : TP_ERR_NOT_CONVERGED;
 }
@@ -300,7 +303,10 @@ const char* tp_status_string(tp_status s) {
   return "unknown status";
 }
 
-const char* tp_error_message(const tp_ctx* c) { return c ? c->err.c_str() : "null context"; }
+const char* tp_error_message(const tp_ctx* c) {
+  if (!c) return "null context";
+  return c->err.empty() ? c->note.c_str() : c->err.c_str();
+}
 
 long tp_ndof(const tp_ctx* c, int level) {
   if (!c || level < 0 || level >= c->nl) return -1;
@@ -598,7 +604,8 @@ tp_status tp_coarse_solve(tp_ctx* c, const double* rhs, double* x) {
     if (st != TP_OK) return st;
   }
   coarse_solve(c, rhs, x);
-  return sync_check(c);
+  tp_status st = sync_check(c);
+  return st != TP_OK ? st : coarse_status(c);
 }
 
 tp_status tp_vcycle(tp_ctx* c, const double* r, double* z) {

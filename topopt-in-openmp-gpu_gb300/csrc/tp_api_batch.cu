@@ -94,6 +94,7 @@ tp_status pcg_graph(tp_ctx* c, int* iters, double* relres) {
     return TP_ERR_CUDA;
   }
   if (!c->err.empty()) return TP_ERR_CUDA;
+  if (coarse_status(c) != TP_OK) return TP_ERR_TIMEOUT;
   const double* s = c->h_scal;
   const double rr = s[S_MAXRR];
   *iters = (int)s[S_IT] - 1;  // index of the last iteration, as the reference reports it

@@ -69,6 +69,31 @@ tp_status tp_set_fine_variant(tp_ctx* c, int variant) {
   return TP_OK;
 }
 
+tp_status tp_set_coarse_solve_variant(tp_ctx* c, int variant) {
+  if (!c || variant < 0 || variant > 1) return TP_ERR_ARG;
+  Coarse& C = c->coarse;
+  C.solve_variant = variant;
+  if (C.graph_exec) {
+    cudaGraphExecDestroy(C.graph_exec);
+    C.graph_exec = nullptr;
+  }
+  graph_free(c);
+  return TP_OK;
+}
+
+tp_status tp_fault_coarse_barrier(tp_ctx* c, long spin, int missing) {
+  if (!c || spin < 0 || missing < 0 || missing > 1) return TP_ERR_ARG;
+  Coarse& C = c->coarse;
+  C.ps_spin = spin;
+  C.ps_missing = missing;
+  if (C.graph_exec) {  // the captured solve holds the old values
+    cudaGraphExecDestroy(C.graph_exec);
+    C.graph_exec = nullptr;
+  }
+  graph_free(c);
+  return TP_OK;
+}
+
 tp_status tp_apply_subspace(tp_ctx* c, int level, const double* in, double* out) {
   if (!c || level < 0 || level >= c->nl || !in || !out) return TP_ERR_ARG;
   if (level == 0) return tp_apply(c, 0, in, out);
@@ -152,7 +177,8 @@ tp_status tp_coarse_factor_csr(tp_ctx* c, long n, const int* rowptr, const int* 
 tp_status tp_coarse_solve_factored(tp_ctx* c, const double* rhs, double* x) {
   if (!c || !rhs || !x) return TP_ERR_ARG;
   coarse_solve(c, rhs, x);
-  return sync_status(c);
+  tp_status st = sync_status(c);
+  return st != TP_OK ? st : coarse_status(c);
 }
 
 tp_status tp_vec_sum(tp_ctx* c, long n, const double* v, double* out) {

@@ -15,7 +15,10 @@
 //            TP_ERR_NOT_SPD.
 //   solve  : L y = b and L^T x = y by blocks of NBS rows; the inverse of each
 //            diagonal block is formed once per factorisation, so each block
-//            step is two matrix-vector products.
+//            step is two matrix-vector products. Both sweeps run as one
+//            cooperative launch with grid barriers between the half steps
+//            (or, where that launch plan does not apply, as two launches per
+//            block step).
 #include <algorithm>
 
 #include "tp_internal.h"
@@ -32,6 +35,8 @@ __device__ __forceinline__ double bget(const double* B, long bw, long r, long c)
   const long d = r - c;
   return (d >= 0 && d <= bw) ? B[c * bw + r] : 0.0;
 }
+
+static void ps_plan(tp_ctx* c);
 
 // ----------------------------------------------------------------------------
 // band assembly from the coarsest FP64 stencil (BCs already applied there)
@@ -83,6 +88,13 @@ void coarse_alloc(tp_ctx* c) {
   cudaEventCreateWithFlags(&C.ev_panel, cudaEventDisableTiming);
   cudaEventCreateWithFlags(&C.ev_rest, cudaEventDisableTiming);
   c->mem_bytes += (long)(C.band_elems + 2 * dsz + lsz + C.n * 18) * 8;
+  int* flags = nullptr;  // barrier counter, status word, exit counter
+  if (cudaMalloc(&flags, 3 * sizeof(int)) == cudaSuccess) {
+    cudaMemsetAsync(flags, 0, 3 * sizeof(int), c->s);
+    C.bar = reinterpret_cast<unsigned*>(flags);
+    C.serr = flags + 1;
+  }
+  ps_plan(c);
 }
 
 void coarse_free(tp_ctx* c) {
@@ -99,6 +111,7 @@ void coarse_free(tp_ctx* c) {
   if (C.s2) cudaStreamDestroy(C.s2);
   if (C.ev_panel) cudaEventDestroy(C.ev_panel);
   if (C.ev_rest) cudaEventDestroy(C.ev_rest);
+  cudaFree(C.bar);  // C.serr shares its allocation
   C = Coarse();
 }
 
@@ -542,11 +555,302 @@ __global__ void bwd_diag_kernel(const double* __restrict__ DT, long n, int nbs, 
     }
 }
 
+// ----------------------------------------------------------------------------
+// The same block triangular solves as ONE cooperative launch: every half step
+// of the forward and the backward sweep (Lrow product, D_k product, L^T
+// product, D_k^T product) is a phase, and the CTAs meet at a grid barrier
+// between phases instead of at a kernel boundary. CTA b owns rows
+// b*R .. b*R+R-1 of every block; each row is split into P = 8/R fixed parts,
+// one warp each, so every sum is formed in the same order on every call.
+// While a CTA works on phase h (and waits at the barrier after it), the
+// matrix rows of phase h+1 -- constant during the solve -- arrive in shared
+// memory by cp.async; the vectors written by other CTAs are read through L2
+// (ld.global.cg). Each barrier wait is bounded: a CTA that gives up sets the
+// status word and every CTA leaves at its next barrier; the host reads (and
+// clears) the word after the solve and reports TP_ERR_TIMEOUT.
+constexpr int kPsWarps = 8;
+constexpr long kBarrierSpin = 1L << 22;  // polls of the barrier counter (about a second)
+
+struct PsArgs {
+  const double* lrow;
+  const double* band;
+  const double* D;
+  const double* DT;
+  long bw, n;
+  int nbs, nblk, R, P, seg;
+  const double* rhs;
+  double* y;
+  double* t;
+  double* x;
+  unsigned* bar;  // barrier counter; bar[2] counts the CTAs out
+  int* err;
+  long spin;         // polls before a barrier wait gives up
+  unsigned missing;  // arrivals each barrier waits for beyond the grid (0; 1 only in the failure test)
+};
+
+enum { PH_FA = 0, PH_FB, PH_BA, PH_BB };
+
+// phase h -> (kind, block): forward FB_0, FA_1, FB_1, ..., FB_{m-1}, then
+// backward BB_{m-1}, BA_{m-2}, BB_{m-2}, ..., BB_0 (m = nblk)
+__device__ __forceinline__ void ps_phase(const PsArgs& a, int h, int& kind, int& k) {
+  const int nf = 2 * a.nblk - 1;
+  if (h < nf) {
+    k = (h + 1) / 2;
+    kind = (h & 1) ? PH_FA : PH_FB;
+  } else {
+    const int q = h - nf;
+    k = a.nblk - 1 - (q + 1) / 2;
+    kind = (q & 1) ? PH_BA : PH_BB;
+  }
+}
+
+// Row i of block k in phase kind: the matrix entry at position e is m[e], the
+// vector entry of column v at vb[v*n + voff + e], for lo <= e < hi. This
+// warp's part of the row is [a0, a1).
+struct PsRow {
+  const double* m;
+  const double* vb;
+  long voff, a0, a1;
+};
+
+__device__ __forceinline__ bool ps_row(const PsArgs& a, int kind, int k, int i, int p, PsRow& r) {
+  const long b0 = (long)k * a.nbs;
+  const int s = (int)lmin((long)a.nbs, a.n - b0);
+  if (i >= s) return false;
+  long lo, hi;
+  if (kind == PH_FA) {  // t = b - Lrow_k y over columns b0-bw+e, e in [max(0, bw-b0, i), bw)
+    r.m = a.lrow + ((long)k * a.nbs + i) * a.bw;
+    r.vb = a.y;
+    r.voff = b0 - a.bw;
+    lo = lmax(lmax(0L, a.bw - b0), (long)i);
+    hi = a.bw;
+  } else if (kind == PH_FB) {  // y_k = D_k t_k, lower triangle
+    r.m = a.D + ((long)k * a.nbs + i) * a.nbs;
+    r.vb = k == 0 ? a.rhs : a.t;
+    r.voff = b0;
+    lo = 0;
+    hi = i + 1;
+  } else if (kind == PH_BA) {  // t = y - L(b1.., r)^T x: band column r is contiguous
+    const long rr = b0 + i, b1 = lmin(a.n, b0 + a.nbs);
+    r.m = a.band + rr * a.bw;
+    r.vb = a.x;
+    r.voff = 0;
+    lo = b1;
+    hi = lmin(a.n - 1, rr + a.bw) + 1;
+  } else {  // x_k = D_k^T t_k, upper triangle
+    r.m = a.DT + ((long)k * a.nbs + i) * a.nbs;
+    r.vb = k == a.nblk - 1 ? a.y : a.t;
+    r.voff = b0;
+    lo = i;
+    hi = s;
+  }
+  const long len = lmax(0L, hi - lo), cs = (len + a.P - 1) / a.P;  // cs <= seg
+  r.a0 = lo + p * cs;
+  r.a1 = lmin(hi, r.a0 + cs);
+  return true;
+}
+
+__device__ __forceinline__ void cp_async8(double* dst, const double* src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// stage this warp's part of phase h's matrix row; lane l copies (and later
+// reads) positions a0 + l, a0 + l + 32, ...
+__device__ __forceinline__ void ps_stage(const PsArgs& a, int h, double* wbuf, int i, int p, int lane) {
+  int kind, k;
+  ps_phase(a, h, kind, k);
+  PsRow r;
+  if (!ps_row(a, kind, k, i, p, r)) return;
+  for (long e = r.a0 + lane; e < r.a1; e += 32) cp_async8(wbuf + (e - r.a0), r.m + e);
+}
+
+// Grid barrier number h (targets h * gridDim.x arrivals), at most spin polls;
+// false if this or another CTA gave up.
+__device__ __forceinline__ bool ps_barrier(unsigned* bar, int* err, unsigned target, long spin) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    __threadfence();
+    atomicAdd(bar, 1u);
+    for (long it = 0;; it++) {
+      unsigned v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(bar) : "memory");
+      if (v >= target) break;
+      if (*(volatile int*)err != 0) {
+        ok = 0;
+        break;
+      }
+      if (it >= spin) {
+        atomicExch(err, 1);
+        ok = 0;
+        break;
+      }
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+template <int NR>
+__global__ void __launch_bounds__(kPsWarps * 32) ps_solve_kernel(PsArgs a) {
+  extern __shared__ double sm[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int rl = w / a.P, p = w % a.P;
+  const int i = blockIdx.x * a.R + rl;
+  auto buf = [&](int b) { return sm + (long)(b * kPsWarps + w) * a.seg; };  // stage b of this warp
+  double* part = sm + 2L * kPsWarps * a.seg;  // [warp][NR]
+  const int nph = 4 * a.nblk - 2;
+  ps_stage(a, 0, buf(0), i, p, lane);
+  cp_commit();
+  for (int h = 0; h < nph; h++) {
+    if (h + 1 < nph) {
+      ps_stage(a, h + 1, buf((h + 1) & 1), i, p, lane);
+      cp_commit();
+      cp_wait<1>();
+    } else {
+      cp_wait<0>();
+    }
+    int kind, k;
+    ps_phase(a, h, kind, k);
+    PsRow r;
+    double acc[NR];
+#pragma unroll
+    for (int v = 0; v < NR; v++) acc[v] = 0.0;
+    if (ps_row(a, kind, k, i, p, r)) {
+      const double* mb = buf(h & 1);
+      for (long e = r.a0 + lane; e < r.a1; e += 32) {
+        const double mv = mb[e - r.a0];
+        const long ve = r.voff + e;  // >= 0
+#pragma unroll
+        for (int v = 0; v < NR; v++) acc[v] += mv * __ldcg(r.vb + (v * a.n + ve));
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < NR; v++) {
+      const double sv = wsum(acc[v]);
+      if (lane == 0) part[w * NR + v] = sv;
+    }
+    __syncthreads();
+    if (threadIdx.x < a.R * NR) {
+      const int rr = threadIdx.x / NR, v = threadIdx.x % NR;
+      const long b0 = (long)k * a.nbs;
+      const long row = blockIdx.x * a.R + rr;
+      if (row < lmin((long)a.nbs, a.n - b0)) {
+        double sum = 0.0;
+        for (int q = 0; q < a.P; q++) sum += part[(rr * a.P + q) * NR + v];
+        const long o = v * a.n + b0 + row;
+        if (kind == PH_FA)
+          a.t[o] = a.rhs[o] - sum;
+        else if (kind == PH_FB)
+          a.y[o] = sum;
+        else if (kind == PH_BA)
+          a.t[o] = __ldcg(a.y + o) - sum;
+        else
+          a.x[o] = sum;
+      }
+    }
+    if (h + 1 < nph && !ps_barrier(a.bar, a.err, (unsigned)(h + 1) * gridDim.x + a.missing, a.spin)) break;
+  }
+  cp_wait<0>();
+  // every CTA, on every path, counts itself out; the last one puts the
+  // barrier counter (and the exit counter) back to zero for the next launch
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned* done = a.bar + 2;
+    __threadfence();
+    if (atomicAdd(done, 1u) == gridDim.x - 1) {
+      atomicExch(a.bar, 0u);
+      atomicExch(done, 0u);
+    }
+  }
+}
+
+// Launch plan: R rows per CTA (1, 2, 4 or 8), the fewest that keep one CTA
+// per SM; P = 8/R warps per row; shared memory for two stages of every
+// warp's longest part. No plan (ps_grid = 0) if the stages do not fit or
+// the grid cannot be co-resident.
+static void ps_plan(tp_ctx* c) {
+  Coarse& C = c->coarse;
+  C.ps_grid = 0;
+  if (!C.bar || C.nblk < 1) return;
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  int R = 1;
+  while (R < kPsWarps && (C.nbs + R - 1) / R > nsm) R *= 2;
+  const int P = kPsWarps / R;
+  const int grid = (C.nbs + R - 1) / R;
+  if (grid > nsm) return;
+  const long seg = std::max((C.bw + P - 1) / P, (long)(C.nbs + P - 1) / P);
+  const size_t smem = (size_t)(2 * kPsWarps * seg + kPsWarps * 8) * sizeof(double);
+  if (smem > 200 * 1024) return;
+  auto fits = [&](const void* f) {
+    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return false;
+    int per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, kPsWarps * 32, smem) != cudaSuccess) return false;
+    return per >= 1;
+  };
+  const bool ok = fits((const void*)ps_solve_kernel<1>) && fits((const void*)ps_solve_kernel<2>) &&
+                  fits((const void*)ps_solve_kernel<4>) && fits((const void*)ps_solve_kernel<8>);
+  cudaGetLastError();
+  if (!ok) return;
+  C.ps_R = R;
+  C.ps_P = P;
+  C.ps_seg = (int)seg;
+  C.ps_smem = smem;
+  C.ps_grid = grid;
+}
+
+template <int NR>
+static void ps_launch(tp_ctx* c, const double* rhs, double* sol, double* y, double* t) {
+  Coarse& C = c->coarse;
+  PsArgs a{C.lrow, C.band, C.dinv, C.dinvT, C.bw, C.n, C.nbs, C.nblk, C.ps_R, C.ps_P, C.ps_seg,
+           rhs, y, t, sol, C.bar, C.serr, C.ps_spin > 0 ? C.ps_spin : kBarrierSpin, (unsigned)C.ps_missing};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)C.ps_grid);
+  cfg.blockDim = dim3(kPsWarps * 32);
+  cfg.dynamicSmemBytes = C.ps_smem;
+  cfg.stream = c->s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, ps_solve_kernel<NR>, a);
+}
+
+tp_status coarse_status(tp_ctx* c) {
+  Coarse& C = c->coarse;
+  if (!C.serr) return TP_OK;
+  int e = 0;
+  cudaMemcpyAsync(&e, C.serr, sizeof(int), cudaMemcpyDeviceToHost, c->s);
+  if (cudaStreamSynchronize(c->s) != cudaSuccess) return TP_OK;  // the caller's own check reports it
+  if (e != 0) {
+    cudaMemsetAsync(C.serr, 0, sizeof(int), c->s);  // the context stays usable
+    cudaStreamSynchronize(c->s);
+    c->note = "coarse solve: a grid barrier wait gave up";
+    return TP_ERR_TIMEOUT;
+  }
+  return TP_OK;
+}
+
 // the launch sequence of one solve of NR columns from rhs into sol (y and t
 // are work columns of the same count)
 template <int NR>
 static void coarse_solve_launches(tp_ctx* c, const double* rhs, double* sol, double* y, double* t) {
   Coarse& C = c->coarse;
+  if (C.solve_variant == 0 && C.ps_grid > 0) {
+    ps_launch<NR>(c, rhs, sol, y, t);
+    return;
+  }
   const unsigned g = (unsigned)((C.nbs + 7) / 8);  // 8 warps per CTA, one row per warp
   for (int b = 0; b < C.nblk; b++) {
     const double* tin = rhs;

@@ -68,6 +68,14 @@ struct Coarse {
   cudaStream_t s2 = nullptr;    // second stream of the factorisation's lookahead
   cudaEvent_t ev_panel = nullptr, ev_rest = nullptr;
   int prio_high = 0;            // highest stream priority of the device (the lookahead chain)
+  // single-launch solve (one cooperative kernel for all block steps)
+  unsigned* bar = nullptr;      // its grid-barrier counter, then the status word (serr) and the exit counter; zero between launches
+  int* serr = nullptr;          // its device status: 1 = a barrier wait gave up (until the host reads it)
+  int ps_grid = 0, ps_R = 0, ps_P = 0, ps_seg = 0;  // CTAs, rows per CTA, warps per row, staged doubles per warp
+  size_t ps_smem = 0;
+  long ps_spin = 0;             // polls before a barrier wait gives up (0: the default, about a second)
+  int ps_missing = 0;           // arrivals each barrier waits for beyond the grid (failure-detection test only)
+  int solve_variant = 0;        // 0: single launch where its plan applies; 1: block launches
 };
 
 // Launch plan of the element-centric level-0 kernel (tp_kernels_fine_ec.cu):
@@ -103,7 +111,8 @@ struct tp_ctx {
   tp::Level L[TP_MAXL];
   cudaStream_t s = nullptr;
   int device = 0;
-  std::string err;
+  std::string err;   // sticky: a CUDA error; every later call fails
+  std::string note;  // the last recoverable failure (a coarse-solve barrier wait that gave up)
 
   // element stiffness tables per level (576 * ncell^3), FP64 and FP32 copies
   double* d_ke[TP_MAXL] = {};
@@ -237,6 +246,9 @@ void coarse_free(tp_ctx* c);
 void coarse_assemble(tp_ctx* c);  // from the FP64 stencil of level nl-1
 void coarse_factor(tp_ctx* c);
 void coarse_solve(tp_ctx* c, const double* rhs, double* x, int nr = 1);  // nr columns of ndof(nl-1)
+// TP_ERR_TIMEOUT (with the message set) if a single-launch solve gave up at a
+// grid barrier; synchronises the context's stream
+tp_status coarse_status(tp_ctx* c);
 
 // design-variable ops (tp_kernels_design.cu)
 void compliance(tp_ctx* c, const double* u, double* dc, int* nblocks, int nr = 1);  // sums over the nr load cases

@@ -97,6 +97,8 @@ def load():
     L.tp_oc_update.argtypes = [V, D, ctypes.POINTER(D)]
     L.tp_set_cg.argtypes = [V, D, I, I, D]
     L.tp_set_fine_variant.argtypes = [V, I]
+    L.tp_set_coarse_solve_variant.argtypes = [V, I]
+    L.tp_fault_coarse_barrier.argtypes = [V, ctypes.c_long, I]
     L.tp_autotune.argtypes = [V, P]
     L.tp_multiload.argtypes = [I, I, I, I, I, ctypes.c_ulonglong, P]
     L.tp_set_graph_solve.argtypes = [V, I]
@@ -224,6 +226,14 @@ class TopOpt:
     def set_fine_variant(self, variant):
         """0: element-centric level-0 kernel where it applies; 1: node-centric stencil."""
         self._check(self.L.tp_set_fine_variant(self.ctx, variant))
+
+    def set_coarse_solve_variant(self, variant):
+        """0: coarse triangular sweeps in one cooperative launch; 1: two launches per block step."""
+        self._check(self.L.tp_set_coarse_solve_variant(self.ctx, variant))
+
+    def fault_coarse_barrier(self, spin, missing):
+        """Failure-detection hook: barrier waits give up after spin polls; missing=1 makes them run out."""
+        self._check(self.L.tp_fault_coarse_barrier(self.ctx, spin, missing))
 
     def checkpoint_save(self, path, loop):
         self._check(self.L.tp_checkpoint_save(self.ctx, os.fsencode(path), loop))

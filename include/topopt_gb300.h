@@ -168,12 +168,16 @@ tp_status tp_set_cg(tp_ctx* c, double cgtol, int cgmax, int nswp, double omega);
  * applies (nely <= 256, 16-byte aligned vectors), else the node-centric
  * stencil; variant 1 = the node-centric stencil everywhere. */
 tp_status tp_set_fine_variant(tp_ctx* c, int variant);
-/* Coarsest-level solve selection (no counterpart in the reference, whose
- * coarse solve is cholmod_solve2, stencil_assembly.c:476-484): variant 0 =
- * both triangular sweeps as one cooperative launch with grid barriers
- * between the block steps, wherever its launch plan applies; variant 1 = two
- * launches per block step. Each variant sums in a fixed order, so repeated
- * solves agree bit for bit; the two variants agree to rounding. */
+/* Coarsest-level direct solver selection (no counterpart in the reference,
+ * whose coarse factor and solve are CHOLMOD's, stencil_assembly.c:435-484):
+ * variant 0 = the band Cholesky as one cooperative launch (a chain CTA
+ * factoring the diagonal tiles, the other CTAs solving panel tiles and
+ * updating the trailing band, handing work over through flags) and both
+ * triangular sweeps as one cooperative launch with grid barriers between the
+ * block steps, wherever their launch plans apply; variant 1 = launches per
+ * 32-column factor step and two launches per solve block step. The factor is
+ * redone at the next solve. Each variant sums in a fixed order, so repeated
+ * runs agree bit for bit; the two variants agree to rounding. */
 tp_status tp_set_coarse_solve_variant(tp_ctx* c, int variant);
 /* Failure detection of the single-launch coarse solve (host-side fault
  * injection, for tests): each grid-barrier wait gives up after spin polls

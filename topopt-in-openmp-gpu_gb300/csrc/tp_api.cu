@@ -195,6 +195,11 @@ static tp_status assemble(tp_ctx* c) {
   if (st != TP_OK) return st;
   c->assembled = true;
   for (int l = 0; l < TP_MAXL; l++) c->st_sub_valid[l] = false;
+  if (info & kCoarseWaitGaveUp) {
+    c->assembled = false;
+    c->note = "coarse Cholesky: a bounded wait gave up";
+    return TP_ERR_TIMEOUT;
+  }
   if (info != 0) {
     c->err = "coarse Cholesky: non-positive pivot at column " + std::to_string(info - 1);
     return TP_ERR_NOT_SPD;

@@ -77,6 +77,11 @@ tp_status tp_set_coarse_solve_variant(tp_ctx* c, int variant) {
     cudaGraphExecDestroy(C.graph_exec);
     C.graph_exec = nullptr;
   }
+  if (C.factor_exec) {  // the factorisation is redone with the chosen launches at the next solve
+    cudaGraphExecDestroy(C.factor_exec);
+    C.factor_exec = nullptr;
+  }
+  c->assembled = false;
   graph_free(c);
   return TP_OK;
 }
@@ -166,6 +171,10 @@ tp_status tp_coarse_factor_csr(tp_ctx* c, long n, const int* rowptr, const int* 
   cudaMemcpyAsync(&info, C.info, sizeof(int), cudaMemcpyDeviceToHost, c->s);
   tp_status st = sync_status(c);
   if (st != TP_OK) return st;
+  if (info & kCoarseWaitGaveUp) {
+    c->note = "coarse Cholesky: a bounded wait gave up";
+    return TP_ERR_TIMEOUT;
+  }
   if (info != 0) {
     c->err = "coarse Cholesky: non-positive pivot at column " + std::to_string(info - 1);
     return TP_ERR_NOT_SPD;

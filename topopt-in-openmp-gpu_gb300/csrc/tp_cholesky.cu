@@ -27,6 +27,7 @@ namespace tp {
 
 constexpr int NB = 32;    // factor panel width
 constexpr int NBS = 512;  // solve block size (largest)
+constexpr long kBarrierSpin = 1L << 22;  // polls of a flag or barrier counter in global memory (about a second)
 
 __host__ __device__ __forceinline__ long lmax(long a, long b) { return a > b ? a : b; }
 __host__ __device__ __forceinline__ long lmin(long a, long b) { return a < b ? a : b; }
@@ -37,6 +38,23 @@ __device__ __forceinline__ double bget(const double* B, long bw, long r, long c)
 }
 
 static void ps_plan(tp_ctx* c);
+static void pf_plan(tp_ctx* c);
+
+// 8-byte asynchronous copies global -> shared (cp.async); the z form writes
+// zero instead when the source is outside the band
+__device__ __forceinline__ void cp_async8(double* dst, const double* src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8z(double* dst, const double* src, bool in) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(src), "r"(in ? 8 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
 
 // ----------------------------------------------------------------------------
 // band assembly from the coarsest FP64 stencil (BCs already applied there)
@@ -85,6 +103,9 @@ void coarse_alloc(tp_ctx* c) {
   int lo = 0, hi = 0;
   cudaDeviceGetStreamPriorityRange(&lo, &hi);
   C.prio_high = hi;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&C.nsm, cudaDevAttrMultiProcessorCount, dev);
   cudaEventCreateWithFlags(&C.ev_panel, cudaEventDisableTiming);
   cudaEventCreateWithFlags(&C.ev_rest, cudaEventDisableTiming);
   c->mem_bytes += (long)(C.band_elems + 2 * dsz + lsz + C.n * 18) * 8;
@@ -95,6 +116,7 @@ void coarse_alloc(tp_ctx* c) {
     C.serr = flags + 1;
   }
   ps_plan(c);
+  pf_plan(c);
 }
 
 void coarse_free(tp_ctx* c) {
@@ -112,6 +134,9 @@ void coarse_free(tp_ctx* c) {
   if (C.ev_panel) cudaEventDestroy(C.ev_panel);
   if (C.ev_rest) cudaEventDestroy(C.ev_rest);
   cudaFree(C.bar);  // C.serr shares its allocation
+  cudaFree(C.pf_flags);
+  cudaFree(C.pf_rpk);
+  cudaFree(C.pf_off);
   C = Coarse();
 }
 
@@ -133,48 +158,110 @@ void coarse_assemble(tp_ctx* c) {
 // the 32 reciprocals 1/L(j,j)). A non-positive pivot sets *info (first
 // column + 1) and is replaced by 1 so that the factor completes.
 //
-// This block lies on the factorisation's critical path (one per 32 columns),
-// and FP64 issue per SM is scarce on this part, so the work is spread over
-// all warps and the serial chain per column is kept to one multiply-add and
-// one reciprocal square root: thread (i, g) owns row i, columns g, g+8, g+16,
-// g+24; column j is updated unscaled (with 1/L(j,j)^2) and scaled one step
-// later; the owner of (j+1, j+1) forms the next pivot right after its last
-// update. (No inverse is formed: the panel solve below substitutes with L
-// directly, which keeps this block -- the part of each 32-column step that
-// no other CTA can share -- short.)
-__device__ __forceinline__ void diag_pivot(double (*S)[NB + 1], double* rp, int j, long k, int* info) {
-  double d = S[j][j];
-  if (!(d > 0.0)) {
-    atomicCAS(info, 0, (int)(k + j + 1));
-    d = 1.0;
+// This block lies on the factorisation's critical path (one per 32 columns).
+// On this part an FP64 warp instruction holds its SM sub-partition's FP64
+// unit for about 67 cycles whatever its active lanes, so the factor runs on
+// four warps, one per sub-partition, each instruction with a full column of
+// rows: warp w keeps columns w, w+4, ..., w+28 in registers (lane = row).
+// The owner of column j forms its pivot (reciprocal square root, one
+// multiply), writes L(:,j) to S and raises ready[j]; the others wait for the
+// flag and update their columns. The owner of column j+1 updates that column
+// first and defers its other updates until it has published pivot j+1, so
+// the chain from pivot to pivot is one multiply-add, the reciprocal square
+// root and one multiply. (No inverse is formed: the panel solve substitutes
+// with L directly.) Waits on the flags are bounded; one that gives up sets
+// kCoarseWaitGaveUp in *info.
+constexpr int kFlagSpin = 1 << 20;
+
+// A producer writes its column, fences, syncs its warp, then lane 0 raises
+// the flag; a consumer polls the flag and fences before reading the column.
+__device__ __forceinline__ void flag_wait(volatile int* flag, int* info) {
+  int it = 0;
+  while (!*flag && ++it < kFlagSpin) {
   }
-  const double r = rsqrt(d);
-  rp[j] = r;
-  rp[NB + j] = r * r;  // 1/d for the unscaled column update
-  S[j][j] = d * r;
+  if (it >= kFlagSpin) atomicOr(info, kCoarseWaitGaveUp);
+  __threadfence_block();
+}
+
+// The warp's columns are template parameters (W: the warp, FULL: nb == 32),
+// so after unrolling every column test is resolved at compile time and no
+// FP64 instruction is issued with all its lanes switched off (such an
+// instruction still holds the FP64 unit).
+template <int W, bool FULL>
+__device__ __forceinline__ void diag_columns(double (*S)[NB + 1], double* rp, volatile int* ready, int nb, long k,
+                                             int* info, int t) {
+  double v[8];  // v[q] = A(t, W + 4q), lower part
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const int c = W + 4 * q;
+    v[q] = ((FULL || c < nb) && t >= c && (FULL || t < nb)) ? S[t][c] : 0.0;
+  }
+#pragma unroll
+  for (int j = 0; j < NB; j++) {
+    if (!FULL && j >= nb) break;
+    if ((j & 3) == W) {  // pivot j: column j (v[j >> 2]) has all its updates
+      double d = __shfl_sync(0xffffffffu, v[j >> 2], j);
+      if (!(d > 0.0)) {
+        if (t == 0) atomicCAS(info, 0, (int)(k + j + 1));
+        d = 1.0;
+      }
+      const double r = rsqrt(d);
+      const double l = (t >= j) ? v[j >> 2] * r : 0.0;  // L(j,j) = d r
+      v[j >> 2] = l;
+      S[t][j] = l;
+      if (t == 0) rp[j] = r;
+      __threadfence_block();
+      __syncwarp();
+      if (t == 0) ready[j] = 1;
+      if (j >= 1) {  // the updates from pivot j-1 deferred in the last step
+        const double lt = S[t][j - 1];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          const int c = W + 4 * q;
+          if (c > j && (FULL || c < nb)) v[q] -= lt * S[c][j - 1];
+        }
+      }
+    } else {
+      flag_wait(&ready[j], info);
+    }
+    const double lt = S[t][j];
+    if (((j + 1) & 3) == W) {  // the next pivot's column first, the rest after it
+      if (j + 1 < NB && (FULL || j + 1 < nb)) v[((j + 1) >> 2) & 7] -= lt * S[(j + 1) & (NB - 1)][j];
+    } else {
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const int c = W + 4 * q;
+        if (c > j && (FULL || c < nb)) v[q] -= lt * S[c][j];
+      }
+    }
+  }
+}
+
+template <bool FULL>
+__device__ __forceinline__ void diag_columns_of(int w, double (*S)[NB + 1], double* rp, volatile int* ready, int nb,
+                                                long k, int* info, int t) {
+  switch (w) {
+    case 0: diag_columns<0, FULL>(S, rp, ready, nb, k, info, t); break;
+    case 1: diag_columns<1, FULL>(S, rp, ready, nb, k, info, t); break;
+    case 2: diag_columns<2, FULL>(S, rp, ready, nb, k, info, t); break;
+    default: diag_columns<3, FULL>(S, rp, ready, nb, k, info, t); break;
+  }
 }
 
 __device__ void factor_diag_block(double* __restrict__ B, long bw, long k, int nb, double (*S)[NB + 1],
                                   double* __restrict__ lblk_out, int* info) {
-  __shared__ double rp[2 * NB];  // 1/L(j,j), then 1/L(j,j)^2
-  const int tid = threadIdx.x;
-  const int i = tid >> 3, g = tid & 7;
-  if (tid == 0) diag_pivot(S, rp, 0, k, info);
+  __shared__ double rp[NB];       // 1/L(j,j)
+  __shared__ volatile int ready[NB];
+  const int tid = threadIdx.x, w = tid >> 5, t = tid & 31;
+  if (tid < NB) ready[tid] = 0;
   __syncthreads();
-  for (int j = 0; j < nb; j++) {
-    const double r2 = rp[NB + j];
-    if (j >= 1 && g == 0 && i >= j && i < nb) S[i][j - 1] *= rp[j - 1];
-    if (i > j && i < nb) {
-      const double sij = S[i][j] * r2;
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const int t = g + 8 * q;
-        if (t > j && t <= i) S[i][t] -= sij * S[t][j];
-      }
-    }
-    if (j + 1 < nb && i == j + 1 && g == ((j + 1) & 7)) diag_pivot(S, rp, j + 1, k, info);
-    __syncthreads();
+  if (w < 4) {
+    if (nb == NB)
+      diag_columns_of<true>(w, S, rp, ready, nb, k, info, t);
+    else
+      diag_columns_of<false>(w, S, rp, ready, nb, k, info, t);
   }
+  __syncthreads();
   for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
     const int r = idx % NB, cc = idx / NB;
     const bool in = r < nb && cc < nb && r >= cc;
@@ -184,7 +271,7 @@ __device__ void factor_diag_block(double* __restrict__ B, long bw, long k, int n
   if (threadIdx.x < NB) lblk_out[NB * NB + threadIdx.x] = threadIdx.x < nb ? rp[threadIdx.x] : 0.0;
 }
 
-// the first diagonal block (later ones are factored inside syrk_kernel)
+// the first diagonal block (later ones are factored inside syrk_panel_kernel)
 __global__ void potrf_kernel(double* __restrict__ B, long bw, long k, int nb, double* __restrict__ linv, int* info) {
   __shared__ double S[NB][NB + 1];
   for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
@@ -195,50 +282,126 @@ __global__ void potrf_kernel(double* __restrict__ B, long bw, long k, int nb, do
   factor_diag_block(B, bw, k, nb, S, linv, info);
 }
 
-// panel rows R0..R1 of columns k..k+nb-1: solve x L_kk^T = a for each row,
-// one warp per row, lane t holding x_t: at step p lane p finishes
-// x_p = acc_p / L(p,p) and broadcasts it, lanes t > p subtract L(t,p) x_p
-__global__ void trsm_kernel(double* __restrict__ B, long bw, long k, int nb, long R0, long R1,
-                            const double* __restrict__ lblk) {
-  __shared__ double Lb[NB][NB + 1], rp[NB];
-  for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) Lb[idx / NB][idx % NB] = lblk[idx];
-  if (threadIdx.x < NB) rp[threadIdx.x] = lblk[NB * NB + threadIdx.x];
-  __syncthreads();
-  const int w = threadIdx.x >> 5, t = threadIdx.x & 31;
-  const long r = R0 + (long)blockIdx.x * (blockDim.x >> 5) + w;
-  if (r > R1) return;
-  double acc = (t < nb) ? bget(B, bw, r, k + t) : 0.0;
-  double x = 0.0;
+// Panel rows R0..R1 of columns k..k+nb-1: solve X L_kk^T = A. One CTA of four
+// warps per 32-row tile, laid out as the diagonal factor (lane = row, warp w
+// holding columns w, w+4, ...): the owner of column p finishes
+// X(:,p) = acc(:,p) / L(p,p) with one multiply and raises ready[p]; the
+// others subtract X(:,p) L(c,p) from their columns c > p; the owner of p+1
+// updates that column first and defers the rest.
+constexpr int kTrsmThreads = 128;
+
+// warp W's columns W, W+4, ... of the tile (compile-time, as in diag_columns)
+// The tile A (row t, column c; 32 x 32 in shared memory) is solved in place;
+// a finished column is published in A itself (its other entries live in the
+// owner's registers until the end).
+template <int W, bool FULL>
+__device__ __forceinline__ void trsm_columns(double (*A)[NB + 1], int nb, const double (*Lb)[NB + 1],
+                                             const double* rp, volatile int* ready, int* info, int t) {
+  double (*X)[NB + 1] = A;
+  double v[8];
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const int c = W + 4 * q;
+    v[q] = (FULL || c < nb) ? A[t][c] : 0.0;
+  }
 #pragma unroll
   for (int p = 0; p < NB; p++) {
-    const double xp = __shfl_sync(0xffffffffu, acc * rp[p], p);
-    if (t == p) x = xp;
-    if (t > p) acc -= Lb[t][p] * xp;
+    if (!FULL && p >= nb) break;
+    if ((p & 3) == W) {
+      const double x = v[p >> 2] * rp[p];
+      v[p >> 2] = x;
+      X[t][p] = x;
+      __threadfence_block();
+      __syncwarp();
+      if (t == 0) ready[p] = 1;
+      if (p >= 1) {  // the updates from column p-1 deferred in the last step
+        const double xt = X[t][p - 1];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          const int c = W + 4 * q;
+          if (c > p && (FULL || c < nb)) v[q] -= xt * Lb[c][p - 1];
+        }
+      }
+    } else {
+      flag_wait(&ready[p], info);
+    }
+    const double xt = X[t][p];
+    if (((p + 1) & 3) == W) {
+      if (p + 1 < NB && (FULL || p + 1 < nb)) v[((p + 1) >> 2) & 7] -= xt * Lb[(p + 1) & (NB - 1)][p];
+    } else {
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const int c = W + 4 * q;
+        if (c > p && (FULL || c < nb)) v[q] -= xt * Lb[c][p];
+      }
+    }
   }
-  if (t < nb && r - (k + t) <= bw) B[(k + t) * bw + r] = x;
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const int c = W + 4 * q;
+    if (FULL || c < nb) A[t][c] = v[q];
+  }
 }
 
-// A(r,c) -= sum_t L(r,k+t) L(c,k+t), R0 <= c <= r <= R1, 32x32 tiles (tr, tc)
-// of the trailing triangle. part 1: the first tile column only (tc = 0, the
-// next panel), whose tile (0,0) -- the next diagonal block -- is then
-// factored by its CTA for the next step; part 2: the other tiles (tc >= 1).
-__global__ void syrk_kernel(double* __restrict__ B, long bw, long n, long k, int nb, long R0, long R1,
-                            double* __restrict__ linv, int* info, int part) {
+// solve the tile A in place with warps 0-3 (the caller syncs before and after)
+__device__ __forceinline__ void trsm_tile(double (*A)[NB + 1], int nb, const double (*Lb)[NB + 1], const double* rp,
+                                          volatile int* ready, int* info) {
+  const int w = threadIdx.x >> 5, t = threadIdx.x & 31;
+  if (w >= 4) return;
+  if (nb == NB) {
+    switch (w) {
+      case 0: trsm_columns<0, true>(A, nb, Lb, rp, ready, info, t); break;
+      case 1: trsm_columns<1, true>(A, nb, Lb, rp, ready, info, t); break;
+      case 2: trsm_columns<2, true>(A, nb, Lb, rp, ready, info, t); break;
+      default: trsm_columns<3, true>(A, nb, Lb, rp, ready, info, t); break;
+    }
+  } else {
+    switch (w) {
+      case 0: trsm_columns<0, false>(A, nb, Lb, rp, ready, info, t); break;
+      case 1: trsm_columns<1, false>(A, nb, Lb, rp, ready, info, t); break;
+      case 2: trsm_columns<2, false>(A, nb, Lb, rp, ready, info, t); break;
+      default: trsm_columns<3, false>(A, nb, Lb, rp, ready, info, t); break;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kTrsmThreads) trsm_kernel(double* __restrict__ B, long bw, long k, int nb, long R0,
+                                                            long R1, const double* __restrict__ lblk, int* info) {
+  __shared__ double Lb[NB][NB + 1], rp[NB], A[NB][NB + 1];
+  __shared__ volatile int ready[NB];
+  for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) Lb[idx / NB][idx % NB] = lblk[idx];
+  const long r0 = R0 + (long)blockIdx.x * 32;
+  for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
+    const int t = idx & 31, c = idx >> 5;  // consecutive threads: consecutive rows of one column
+    const long r = r0 + t;
+    A[t][c] = (r <= R1 && c < nb) ? bget(B, bw, r, k + c) : 0.0;
+  }
+  if (threadIdx.x < NB) {
+    rp[threadIdx.x] = lblk[NB * NB + threadIdx.x];
+    ready[threadIdx.x] = 0;
+  }
+  __syncthreads();
+  trsm_tile(A, nb, Lb, rp, ready, info);
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
+    const int t = idx & 31, c = idx >> 5;
+    const long r = r0 + t;
+    if (r <= R1 && c < nb && r - (k + c) <= bw) B[(k + c) * bw + r] = A[t][c];
+  }
+}
+
+// A(r,c) -= sum_t L(r,k+t) L(c,k+t), R0 <= c <= r <= R1, over 32x32 tiles
+// (tr, tc) of the trailing triangle. syrk_panel_kernel: the first tile column
+// (tc = 0, the next panel), one tile per CTA; CTA 0 then factors tile (0,0),
+// the next diagonal block, for the next step. syrk_rest_kernel: the tiles
+// with tc >= 1, as quarter tiles (32 rows x 8 columns) dealt round-robin to
+// two CTAs per SM, so every SM gets nearly the same FP64 work.
+__global__ void syrk_panel_kernel(double* __restrict__ B, long bw, long n, long k, int nb, long R0, long R1,
+                                  double* __restrict__ linv, int* info) {
   __shared__ double Lr[NB][33], Lc[NB][33];
   __shared__ double S[NB][NB + 1];
-  long tr, tc;
-  if (part == 1) {
-    tr = blockIdx.x;
-    tc = 0;
-  } else {  // blockIdx.x -> lower-triangular tile among those with tc >= 1
-    const long b = blockIdx.x;
-    long q = (long)((sqrt(8.0 * (double)b + 1.0) - 1.0) / 2.0);
-    while ((q + 1) * (q + 2) / 2 <= b) q++;
-    while (q * (q + 1) / 2 > b) q--;
-    tr = q + 1;
-    tc = b - q * (q + 1) / 2 + 1;
-  }
-  const long rb = R0 + tr * 32, cb = R0 + tc * 32;
+  const long tr = blockIdx.x;
+  const long rb = R0 + tr * 32, cb = R0;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 256 threads
   for (int t = ty; t < NB; t += 8) {
     const long r = rb + tx, cc = cb + tx;
@@ -246,7 +409,7 @@ __global__ void syrk_kernel(double* __restrict__ B, long bw, long n, long k, int
     Lc[t][tx] = (t < nb && cc <= R1) ? bget(B, bw, cc, k + t) : 0.0;
   }
   __syncthreads();
-  const bool diag_next = part == 1 && tr == 0;
+  const bool diag_next = tr == 0;
   const long r = rb + tx;
 #pragma unroll
   for (int q = 0; q < 4; q++) {
@@ -269,6 +432,285 @@ __global__ void syrk_kernel(double* __restrict__ B, long bw, long n, long k, int
     const int nb2 = (int)lmin((long)NB, n - R0);
     factor_diag_block(B, bw, R0, nb2, S, linv, info);
   }
+}
+
+// lower-triangular tile b among those with tc >= 1 -> (tr, tc)
+__device__ __forceinline__ void rest_tile(long b, long& tr, long& tc) {
+  long q = (long)((sqrt(8.0 * (double)b + 1.0) - 1.0) / 2.0);
+  while ((q + 1) * (q + 2) / 2 <= b) q++;
+  while (q * (q + 1) / 2 > b) q--;
+  tr = q + 1;
+  tc = b - q * (q + 1) / 2 + 1;
+}
+
+constexpr int kRestStage = 2 * NB * 33;  // doubles per stage: the row and the column panel blocks
+constexpr size_t kRestSmem = 2 * kRestStage * sizeof(double);
+
+// stage the panel blocks of tile b (rows rb.., columns cb.. of columns k..k+nb-1)
+__device__ __forceinline__ void rest_stage(const double* __restrict__ B, long bw, long k, int nb, long R0, long R1,
+                                           long b, double* st) {
+  long tr, tc;
+  rest_tile(b, tr, tc);
+  const long rb = R0 + tr * 32, cb = R0 + tc * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int t = ty; t < NB; t += 8) {
+    const long r = rb + tx, cc = cb + tx;
+    const bool ir = t < nb && r <= R1 && r - (k + t) <= bw, ic = t < nb && cc <= R1 && cc - (k + t) <= bw;
+    cp_async8z(st + t * 33 + tx, ir ? B + (k + t) * bw + r : B, ir);
+    cp_async8z(st + NB * 33 + t * 33 + tx, ic ? B + (k + t) * bw + cc : B, ic);
+  }
+}
+
+__global__ void __launch_bounds__(256) syrk_rest_kernel(double* __restrict__ B, long bw, long k, int nb, long R0,
+                                                        long R1, long ntiles) {
+  extern __shared__ double sm[];  // two stages
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  long b = blockIdx.x;
+  int s = 0;
+  if (b < ntiles) rest_stage(B, bw, k, nb, R0, R1, b, sm);
+  cp_commit();
+  for (; b < ntiles; b += gridDim.x, s ^= 1) {
+    if (b + gridDim.x < ntiles) rest_stage(B, bw, k, nb, R0, R1, b + gridDim.x, sm + (s ^ 1) * kRestStage);
+    cp_commit();
+    cp_wait<1>();
+    __syncthreads();
+    const double* Lr = sm + s * kRestStage;
+    const double* Lc = Lr + NB * 33;
+    long tr, tc;
+    rest_tile(b, tr, tc);
+    const long r = R0 + tr * 32 + tx;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int cy = ty + 8 * q;
+      const long cc = R0 + tc * 32 + cy;
+      double acc = 0.0;
+#pragma unroll
+      for (int t = 0; t < NB; t++) acc += Lr[t * 33 + tx] * Lc[t * 33 + cy];
+      if (r <= R1 && cc <= R1 && cc <= r && r - cc <= bw) B[cc * bw + r] -= acc;
+    }
+    __syncthreads();  // every read of stage s is done before it is refilled
+  }
+  cp_wait<0>();
+}
+
+// ----------------------------------------------------------------------------
+// The whole factorisation as ONE cooperative launch, one CTA per SM. Tiles
+// are the 32 x 32 blocks (I, J), I >= J, of the band; step k factors diagonal
+// tile k. CTA 0 runs the chain every step waits on: factor tile (k,k), solve
+// the panel tile (k+1,k), apply step k's update to tile (k+1,k+1) -- which it
+// keeps in shared memory and factors as step k+1. The other CTAs take, in
+// step order and round-robin, the rest of each step: the panel tiles (I,k),
+// I >= k+2, then the updates of the trailing band, column k+1 first (the
+// next step's panel) and tile (k+2,k+2) right after it (the chain's next
+// input). Each item waits, bounded, on flags for what it reads:
+//   fdone[k]        diagonal tile k factored (and its 1/L(j,j) in rpk[k])
+//   sdone[k][I-k]   panel tile (I,k) solved
+//   tver[J][I-J]    tile (I,J) holds the updates of steps < tver
+// A producer stores, syncs, fences and releases the flag; a consumer's
+// thread 0 acquires it, and the band is read through L2 (ld.global.cg).
+// Items only wait on items of earlier steps or on earlier items of their
+// own step, and every CTA takes its items in order, so the waits end.
+struct PfArgs {
+  double* B;
+  long bw, n;
+  int NT, TS;        // diagonal tiles; row stride of sdone and tver
+  double* rpk;       // [NT][NB]
+  int* fdone;        // [NT]
+  int* sdone;        // [NT][TS]
+  int* tver;         // [NT][TS]
+  const long* off;   // [NT+1]: bulk items before step k
+  int* info;
+  int* abort_flag;
+  long spin;
+};
+constexpr size_t kPfSmem = 120 * 1024;  // more than half an SM's shared memory: one CTA per SM
+
+// last tile row of step k's panel (k itself: no panel)
+__host__ __device__ __forceinline__ long pf_imax(long n, long bw, long k) {
+  if (32 * (k + 1) >= n) return k;
+  return lmin(n - 1, 32 * k + 31 + bw) / 32;
+}
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// every thread of the CTA: wait until *flag >= target; false if the
+// factorisation is being abandoned (this or another wait gave up)
+__device__ bool pf_wait(const PfArgs& a, const int* flag, int target) {
+  int ok = 1;
+  if (threadIdx.x == 0) {
+    for (long it = 0; ld_acquire(flag) < target; it++) {
+      if (*(volatile int*)a.abort_flag) {
+        ok = 0;
+        break;
+      }
+      if (it >= a.spin) {
+        atomicOr(a.info, kCoarseWaitGaveUp);
+        atomicExch(a.abort_flag, 1);
+        ok = 0;
+        break;
+      }
+    }
+  }
+  return __syncthreads_and(ok) != 0;
+}
+
+__device__ __forceinline__ void pf_release(int* flag, int v) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    asm volatile("st.release.gpu.global.s32 [%0], %1;\n" ::"l"(flag), "r"(v) : "memory");
+  }
+}
+
+// tile (I, J) into A[r][c] (TR: A[c][r]); zero outside the matrix, above the
+// diagonal and outside the band
+template <bool TR>
+__device__ void pf_load(const PfArgs& a, long I, long J, double (*A)[NB + 1]) {
+  for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
+    const int r = idx & 31, c = idx >> 5;
+    const long gr = 32 * I + r, gc = 32 * J + c;
+    const bool in = gr < a.n && gr >= gc && gr - gc <= a.bw;
+    const double v = in ? __ldcg(a.B + gc * a.bw + gr) : 0.0;
+    if (TR)
+      A[c][r] = v;
+    else
+      A[r][c] = v;
+  }
+}
+
+__device__ void pf_store(const PfArgs& a, long I, long J, const double (*A)[NB + 1]) {
+  for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
+    const int r = idx & 31, c = idx >> 5;
+    const long gr = 32 * I + r, gc = 32 * J + c;
+    if (gr < a.n && gr >= gc && gr - gc <= a.bw) a.B[gc * a.bw + gr] = A[r][c];
+  }
+}
+
+__device__ void pf_chain(const PfArgs& a, double* smem) {
+  double(*D)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(smem);  // diagonal tile, then L_kk
+  double(*X)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(smem + NB * (NB + 1));  // panel tile (k+1,k)
+  double* rp = smem + 2 * NB * (NB + 1);
+  volatile int* ready = reinterpret_cast<volatile int*>(rp + NB);
+  const int w = threadIdx.x >> 5, t = threadIdx.x & 31;
+  pf_load<false>(a, 0, 0, D);
+  for (long k = 0; k < a.NT; k++) {
+    const int nb = (int)lmin(NB, a.n - 32 * k);
+    if (threadIdx.x < NB) ready[threadIdx.x] = 0;
+    __syncthreads();
+    if (w < 4) {
+      if (nb == NB)
+        diag_columns_of<true>(w, D, rp, ready, nb, 32 * k, a.info, t);
+      else
+        diag_columns_of<false>(w, D, rp, ready, nb, 32 * k, a.info, t);
+    }
+    __syncthreads();
+    pf_store(a, k, k, D);
+    if (threadIdx.x < NB) a.rpk[k * NB + threadIdx.x] = threadIdx.x < nb ? rp[threadIdx.x] : 0.0;
+    pf_release(a.fdone + k, 1);
+    if (pf_imax(a.n, a.bw, k) < k + 1) break;
+    const bool prev = k >= 1 && k + 1 <= pf_imax(a.n, a.bw, k - 1);  // tiles (k+1, *) hold a step k-1 update
+    // panel tile (k+1, k)
+    if (prev && !pf_wait(a, a.tver + k * a.TS + 1, (int)k)) return;
+    pf_load<false>(a, k + 1, k, X);
+    if (threadIdx.x < NB) ready[threadIdx.x] = 0;
+    __syncthreads();
+    trsm_tile(X, NB, D, rp, ready, a.info);
+    __syncthreads();
+    pf_store(a, k + 1, k, X);
+    pf_release(a.sdone + k * a.TS + 1, 1);
+    // tile (k+1, k+1): step k-1's update (from the other CTAs), then step k's
+    if (prev && !pf_wait(a, a.tver + (k + 1) * a.TS, (int)k)) return;
+    pf_load<false>(a, k + 1, k + 1, D);
+    __syncthreads();
+    for (int e = threadIdx.x; e < NB * (NB + 1) / 2; e += blockDim.x) {  // the lower triangle, packed
+      int r = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+      while ((r + 1) * (r + 2) / 2 <= e) r++;
+      while (r * (r + 1) / 2 > e) r--;
+      const int c = e - r * (r + 1) / 2;
+      double s = 0.0;
+#pragma unroll
+      for (int q = 0; q < NB; q++) s += X[r][q] * X[c][q];
+      D[r][c] -= s;
+    }
+    __syncthreads();
+  }
+}
+
+__device__ void pf_bulk(const PfArgs& a, double* smem) {
+  double(*P)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(smem);  // panel tile / row panel block (transposed)
+  double(*Q)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(smem + NB * (NB + 1));  // L_kk / column panel block
+  double* rp = smem + 2 * NB * (NB + 1);
+  volatile int* ready = reinterpret_cast<volatile int*>(rp + NB);
+  const long nbulk = gridDim.x - 1, total = a.off[a.NT];
+  long k = 0;
+  for (long g = blockIdx.x - 1; g < total; g += nbulk) {
+    while (a.off[k + 1] <= g) k++;
+    const long idx = g - a.off[k];
+    const long T = pf_imax(a.n, a.bw, k) - k;
+    const long prev = k >= 1 ? pf_imax(a.n, a.bw, k - 1) : -1;  // tiles with I <= prev hold a step k-1 update
+    if (idx < T - 1) {  // panel tile (I, k)
+      const long I = k + 2 + idx;
+      if (!pf_wait(a, a.fdone + k, 1)) return;
+      if (I <= prev && !pf_wait(a, a.tver + k * a.TS + (I - k), (int)k)) return;
+      pf_load<false>(a, k, k, Q);
+      pf_load<false>(a, I, k, P);
+      if (threadIdx.x < NB) {
+        rp[threadIdx.x] = __ldcg(a.rpk + k * NB + threadIdx.x);
+        ready[threadIdx.x] = 0;
+      }
+      __syncthreads();
+      trsm_tile(P, NB, Q, rp, ready, a.info);
+      __syncthreads();
+      pf_store(a, I, k, P);
+      pf_release(a.sdone + k * a.TS + (I - k), 1);
+    } else {  // update of tile (I, J)
+      long u = idx - (T - 1), I, J;
+      if (u < T - 1) {
+        I = k + 2 + u;
+        J = k + 1;
+      } else {
+        u -= T - 1;
+        long q = (long)((sqrt(8.0 * (double)u + 1.0) - 1.0) / 2.0);
+        while ((q + 1) * (q + 2) / 2 <= u) q++;
+        while (q * (q + 1) / 2 > u) q--;
+        I = k + 2 + q;
+        J = k + 2 + (u - q * (q + 1) / 2);
+      }
+      if (!pf_wait(a, a.sdone + k * a.TS + (I - k), 1)) return;
+      if (J != I && !pf_wait(a, a.sdone + k * a.TS + (J - k), 1)) return;
+      if (I <= prev && !pf_wait(a, a.tver + J * a.TS + (I - J), (int)k)) return;
+      pf_load<true>(a, I, k, P);  // P[t][r] = L(32I + r, 32k + t)
+      pf_load<true>(a, J, k, Q);
+      __syncthreads();
+      const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+      const long gr = 32 * I + tx;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int cy = ty + 8 * q;
+        const long gc = 32 * J + cy;
+        double s = 0.0;
+#pragma unroll
+        for (int t = 0; t < NB; t++) s += P[t][tx] * Q[t][cy];
+        if (gr < a.n && gc <= gr && gr - gc <= a.bw) {
+          double* p = a.B + gc * a.bw + gr;
+          *p = __ldcg(p) - s;
+        }
+      }
+      pf_release(a.tver + J * a.TS + (I - J), (int)k + 1);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) pf_kernel(PfArgs a) {
+  extern __shared__ double sm[];
+  if (blockIdx.x == 0)
+    pf_chain(a, sm);
+  else
+    pf_bulk(a, sm);
 }
 
 // Inverse of each diagonal NBSxNBS block of L, one CTA per (block, 32-column
@@ -366,16 +808,17 @@ __global__ void lrow_kernel(const double* __restrict__ B, long bw, long n, int n
   }
 }
 
-// Lookahead over two streams. Per 32-column step k: the panel solve T_k, then
-// on the main stream the update of the next panel's tile column with the
-// factorisation of the next diagonal block (the chain every step waits on),
-// and on the second stream the rest of the trailing update, which overlaps
-// that chain and the next step's panel solve. The next step's first-column
-// update waits for this step's rest, which writes the same tiles.
-static void coarse_factor_launches(tp_ctx* c, size_t dinv_smem) {
+// The factorisation as launches per 32-column step (where the single launch
+// does not apply, and as its cross-check), with lookahead over two streams.
+// Per step k: the panel solve T_k, then on the main stream the update of the
+// next panel's tile column with the factorisation of the next diagonal block
+// (the chain every step waits on), and on the second stream the rest of the
+// trailing update, which overlaps that chain and the next step's panel
+// solve. The next step's first-column update waits for this step's rest,
+// which writes the same tiles.
+static void step_launches(tp_ctx* c) {
   Coarse& C = c->coarse;
   cudaStream_t s = c->s, s2 = C.s2;
-  cudaMemsetAsync(C.info, 0, sizeof(int), s);
   potrf_kernel<<<1, 256, 0, s>>>(C.band, C.bw, 0, (int)std::min((long)NB, C.n), C.linv, C.info);
   bool rest_pending = false;
   for (long k = 0; k < C.n; k += NB) {
@@ -388,33 +831,103 @@ static void coarse_factor_launches(tp_ctx* c, size_t dinv_smem) {
       cudaLaunchAttribute pri[1];
       pri[0].id = cudaLaunchAttributePriority;
       pri[0].val.priority = C.prio_high;
+      const long T = (m + 31) / 32;  // 32-row tiles of the panel
       cudaLaunchConfig_t cfg = {};
-      cfg.blockDim = dim3(256);
+      cfg.blockDim = dim3(kTrsmThreads);
       cfg.stream = s;
       cfg.attrs = pri;
       cfg.numAttrs = 1;
-      cfg.gridDim = dim3((unsigned)((m + 7) / 8));
+      cfg.gridDim = dim3((unsigned)T);
       double* band = C.band;
       const long bw = C.bw, n = C.n;
       const double* lc = C.linv;
-      cudaLaunchKernelEx(&cfg, trsm_kernel, band, bw, k, nb, R0, R1, lc);
-      const long T = (m + 31) / 32;
+      int* info = C.info;
+      cudaLaunchKernelEx(&cfg, trsm_kernel, band, bw, k, nb, R0, R1, lc, info);
       if (T > 1) {
         cudaEventRecord(C.ev_panel, s);
         cudaStreamWaitEvent(s2, C.ev_panel, 0);
       }
       if (rest_pending) cudaStreamWaitEvent(s, C.ev_rest, 0);
-      cfg.gridDim = dim3((unsigned)T);
-      cudaLaunchKernelEx(&cfg, syrk_kernel, band, bw, n, k, nb, R0, R1, C.linv, C.info, 1);
+      cfg.blockDim = dim3(256);
+      cudaLaunchKernelEx(&cfg, syrk_panel_kernel, band, bw, n, k, nb, R0, R1, C.linv, info);
       rest_pending = false;
       if (T > 1) {
-        syrk_kernel<<<(unsigned)(T * (T - 1) / 2), 256, 0, s2>>>(C.band, C.bw, C.n, k, nb, R0, R1, C.linv, C.info, 2);
+        const long tiles = T * (T - 1) / 2;
+        const unsigned g = (unsigned)std::min(tiles, (long)std::max(1, C.nsm));
+        syrk_rest_kernel<<<g, 256, kRestSmem, s2>>>(C.band, C.bw, k, nb, R0, R1, tiles);
         cudaEventRecord(C.ev_rest, s2);
         rest_pending = true;
       }
     }
   }
   if (rest_pending) cudaStreamWaitEvent(s, C.ev_rest, 0);
+}
+
+// Plan of the single-launch factorisation: the flag arrays and the count of
+// the other CTAs' work items per step (T-1 panel tiles and T(T+1)/2 - 1 tile
+// updates for a panel of T tile rows).
+static void pf_plan(tp_ctx* c) {
+  Coarse& C = c->coarse;
+  C.pf_ok = false;
+  const long NT = (C.n + 31) / 32;
+  if (NT < 2 || C.nsm < 2) return;
+  long TS = 2;
+  std::vector<long> off(NT + 1, 0);
+  for (long k = 0; k < NT; k++) {
+    const long T = pf_imax(C.n, C.bw, k) - k;
+    TS = std::max(TS, T + 2);
+    off[k + 1] = off[k] + (T >= 1 ? (T - 1) + T * (T + 1) / 2 - 1 : 0);
+  }
+  if (cudaFuncSetAttribute(pf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPfSmem) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  int per = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pf_kernel, 256, kPfSmem) != cudaSuccess || per < 1) {
+    cudaGetLastError();
+    return;
+  }
+  C.pf_NT = (int)NT;
+  C.pf_TS = (int)TS;
+  C.pf_flag_bytes = sizeof(int) * (size_t)(NT + 2 * NT * TS + 1);
+  if (cudaMalloc(&C.pf_flags, C.pf_flag_bytes) != cudaSuccess ||
+      cudaMalloc(&C.pf_rpk, sizeof(double) * NT * NB) != cudaSuccess ||
+      cudaMalloc(&C.pf_off, sizeof(long) * (NT + 1)) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  cudaMemcpy(C.pf_off, off.data(), sizeof(long) * (NT + 1), cudaMemcpyHostToDevice);
+  c->mem_bytes += (long)C.pf_flag_bytes + 8L * NT * NB + 8L * (NT + 1);
+  C.pf_ok = true;
+}
+
+static void pf_launch(tp_ctx* c) {
+  Coarse& C = c->coarse;
+  const long NT = C.pf_NT, TS = C.pf_TS;
+  int* f = C.pf_flags;
+  PfArgs a{C.band, C.bw, C.n, (int)NT, (int)TS, C.pf_rpk, f, f + NT, f + NT + NT * TS, C.pf_off, C.info,
+           f + NT + 2 * NT * TS, C.ps_spin > 0 ? C.ps_spin : kBarrierSpin};
+  cudaMemsetAsync(C.pf_flags, 0, C.pf_flag_bytes, c->s);
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)C.nsm);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = kPfSmem;
+  cfg.stream = c->s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, pf_kernel, a);
+}
+
+static void coarse_factor_launches(tp_ctx* c, size_t dinv_smem) {
+  Coarse& C = c->coarse;
+  cudaMemsetAsync(C.info, 0, sizeof(int), c->s);
+  if (C.solve_variant == 0 && C.pf_ok)
+    pf_launch(c);
+  else
+    step_launches(c);
   dinv_kernel<<<dim3(C.nbs / 32, C.nblk), kDinvThreads, dinv_smem, c->s>>>(C.band, C.bw, C.n, C.nbs, C.dinv, C.dinvT);
   lrow_kernel<<<dim3((unsigned)((C.bw + 31) / 32), C.nbs / 32, C.nblk), dim3(32, 8), 0, c->s>>>(C.band, C.bw, C.n,
                                                                                                C.nbs, C.lrow);
@@ -569,7 +1082,6 @@ __global__ void bwd_diag_kernel(const double* __restrict__ DT, long n, int nbs, 
 // status word and every CTA leaves at its next barrier; the host reads (and
 // clears) the word after the solve and reports TP_ERR_TIMEOUT.
 constexpr int kPsWarps = 8;
-constexpr long kBarrierSpin = 1L << 22;  // polls of the barrier counter (about a second)
 
 struct PsArgs {
   const double* lrow;
@@ -650,16 +1162,6 @@ __device__ __forceinline__ bool ps_row(const PsArgs& a, int kind, int k, int i, 
   return true;
 }
 
-__device__ __forceinline__ void cp_async8(double* dst, const double* src) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
 // stage this warp's part of phase h's matrix row; lane l copies (and later
 // reads) positions a0 + l, a0 + l + 32, ...
 __device__ __forceinline__ void ps_stage(const PsArgs& a, int h, double* wbuf, int i, int p, int lane) {
@@ -725,12 +1227,25 @@ __global__ void __launch_bounds__(kPsWarps * 32) ps_solve_kernel(PsArgs a) {
 #pragma unroll
     for (int v = 0; v < NR; v++) acc[v] = 0.0;
     if (ps_row(a, kind, k, i, p, r)) {
+      // U positions per lane per round: all their L2 loads are issued before
+      // the first multiply-add, so a round costs one L2 latency; the sum
+      // still runs over the positions in order
+      constexpr int U = NR == 1 ? 16 : (NR == 2 ? 8 : (NR == 4 ? 4 : 2));
       const double* mb = buf(h & 1);
-      for (long e = r.a0 + lane; e < r.a1; e += 32) {
-        const double mv = mb[e - r.a0];
-        const long ve = r.voff + e;  // >= 0
+      for (long e0 = r.a0 + lane; e0 < r.a1; e0 += 32L * U) {
+        double mv[U], vv[U][NR];
 #pragma unroll
-        for (int v = 0; v < NR; v++) acc[v] += mv * __ldcg(r.vb + (v * a.n + ve));
+        for (int u = 0; u < U; u++) {
+          const long e = e0 + 32L * u;
+          const bool in = e < r.a1;
+          mv[u] = in ? mb[e - r.a0] : 0.0;
+#pragma unroll
+          for (int v = 0; v < NR; v++) vv[u][v] = in ? __ldcg(r.vb + (v * a.n + r.voff + e)) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++)
+#pragma unroll
+          for (int v = 0; v < NR; v++) acc[v] += mv[u] * vv[u][v];
       }
     }
 #pragma unroll

@@ -50,6 +50,9 @@ enum Scalar {
 };
 
 // The coarsest-level direct solver: band Cholesky in FP64 (tp_cholesky.cu).
+// Its status word (Coarse::info) holds the first non-positive pivot's column
+// + 1, or'ed with kCoarseWaitGaveUp if a bounded wait inside the factor gave up.
+constexpr int kCoarseWaitGaveUp = 1 << 30;
 struct Coarse {
   long n = 0, bw = 0;           // order, half bandwidth
   double* band = nullptr;       // L(r,c) at c*bw + r, 0 <= r - c <= bw (column-major, ld = bw)
@@ -68,6 +71,7 @@ struct Coarse {
   cudaStream_t s2 = nullptr;    // second stream of the factorisation's lookahead
   cudaEvent_t ev_panel = nullptr, ev_rest = nullptr;
   int prio_high = 0;            // highest stream priority of the device (the lookahead chain)
+  int nsm = 0;                  // SMs of the device
   // single-launch solve (one cooperative kernel for all block steps)
   unsigned* bar = nullptr;      // its grid-barrier counter, then the status word (serr) and the exit counter; zero between launches
   int* serr = nullptr;          // its device status: 1 = a barrier wait gave up (until the host reads it)
@@ -75,7 +79,14 @@ struct Coarse {
   size_t ps_smem = 0;
   long ps_spin = 0;             // polls before a barrier wait gives up (0: the default, about a second)
   int ps_missing = 0;           // arrivals each barrier waits for beyond the grid (failure-detection test only)
-  int solve_variant = 0;        // 0: single launch where its plan applies; 1: block launches
+  int solve_variant = 0;        // 0: single launches (factor and solve) where their plans apply; 1: launches per step
+  // single-launch factor (one cooperative kernel for all 32-column steps)
+  bool pf_ok = false;
+  int pf_NT = 0, pf_TS = 0;     // diagonal tiles; row stride of its flag arrays
+  int* pf_flags = nullptr;      // fdone [NT], sdone [NT][TS], tver [NT][TS], abort [1]
+  size_t pf_flag_bytes = 0;
+  double* pf_rpk = nullptr;     // [NT][32] reciprocal pivots per diagonal tile
+  long* pf_off = nullptr;       // [NT+1] work items of the other CTAs before each step
 };
 
 // Launch plan of the element-centric level-0 kernel (tp_kernels_fine_ec.cu):

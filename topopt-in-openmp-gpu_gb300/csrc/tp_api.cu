@@ -382,7 +382,9 @@ tp_status tp_create(const tp_params* p, tp_ctx** out) {
     if (l == 0) {
       set_fine_ke(ke.data());
       set_design_ke(ke.data());
-      c->ec_ok = set_fine_kz(ke.data(), nullptr);
+      double kz45[45];
+      c->ec_ok = set_fine_kz(ke.data(), kz45);
+      if (c->ec_ok) set_design_kz(kz45);
     }
   }
   const bool mx = p->precision == TP_MIXED;
@@ -390,7 +392,7 @@ tp_status tp_create(const tp_params* p, tp_ctx** out) {
   ok = ok && (c->d_x = dalloc<double>(c, ne)) && (c->d_xphys = dalloc<double>(c, ne)) &&
        (c->d_xnew = dalloc<double>(c, ne)) && (c->d_dc = dalloc<double>(c, ne)) &&
        (c->d_dv = dalloc<double>(c, ne)) && (c->d_hs = dalloc<double>(c, ne)) &&
-       (c->d_ocb = dalloc<double>(c, ne)) && ((c->ocb_n = ne) > 0) &&
+       (c->d_ocb = dalloc<double>(c, 3 * ne)) && ((c->ocb_n = ne) > 0) &&
        (c->d_E = dalloc<double>(c, ne)) && (c->d_Ef = dalloc<float>(c, ne)) &&
        (c->d_F = dalloc<double>(c, nv)) && (c->d_U = dalloc<double>(c, nv)) &&
        (c->d_r = dalloc<double>(c, nv)) && (c->d_z = dalloc<double>(c, nv)) &&

@@ -640,68 +640,188 @@ __device__ void pf_chain(const PfArgs& a, double* smem) {
   }
 }
 
+// One work item of the non-chain CTAs: a panel tile (S: solve tile (I,k)
+// with L_kk) or a tile update (U: tile (I,J) -= L(I,k) L(J,k)^T), with the
+// flags it waits on.
+struct PfItem {
+  bool solve;
+  long k, I, J;
+  const int *f0, *f1, *f2;  // the first nf are used
+  int t0, t1, t2;
+  int nf;
+  __device__ void add(const int* f, int tg) {
+    if (nf == 0) f0 = f, t0 = tg;
+    else if (nf == 1) f1 = f, t1 = tg;
+    else f2 = f, t2 = tg;
+    nf++;
+  }
+  __device__ const int* flag(int i) const { return i == 0 ? f0 : (i == 1 ? f1 : f2); }
+  __device__ int target(int i) const { return i == 0 ? t0 : (i == 1 ? t1 : t2); }
+};
+
+// item g; k is the step of an earlier item and is advanced to g's step
+__device__ void pf_item(const PfArgs& a, long g, long& k, PfItem& it) {
+  while (a.off[k + 1] <= g) k++;
+  const long idx = g - a.off[k];
+  const long T = pf_imax(a.n, a.bw, k) - k;
+  const long prev = k >= 1 ? pf_imax(a.n, a.bw, k - 1) : -1;  // tiles with I <= prev hold a step k-1 update
+  it.k = k;
+  it.nf = 0;
+  if (idx < T - 1) {
+    it.solve = true;
+    it.I = k + 2 + idx;
+    it.J = k;
+    it.add(a.fdone + k, 1);
+    if (it.I <= prev) it.add(a.tver + k * a.TS + (it.I - k), (int)k);
+    return;
+  }
+  long u = idx - (T - 1);
+  it.solve = false;
+  if (u < T - 1) {
+    it.I = k + 2 + u;
+    it.J = k + 1;
+  } else {
+    u -= T - 1;
+    long q = (long)((sqrt(8.0 * (double)u + 1.0) - 1.0) / 2.0);
+    while ((q + 1) * (q + 2) / 2 <= u) q++;
+    while (q * (q + 1) / 2 > u) q--;
+    it.I = k + 2 + q;
+    it.J = k + 2 + (u - q * (q + 1) / 2);
+  }
+  it.add(a.sdone + k * a.TS + (it.I - k), 1);
+  if (it.J != it.I) it.add(a.sdone + k * a.TS + (it.J - k), 1);
+  if (it.I <= prev) it.add(a.tver + it.J * a.TS + (it.I - it.J), (int)k);
+}
+
+// threads 0..nf-1 each watch one flag (bounded); false if the factorisation
+// is being abandoned
+__device__ bool pf_wait_item(const PfArgs& a, const PfItem& it) {
+  int ok = 1;
+  if (threadIdx.x < it.nf) {
+    const int* f = it.flag(threadIdx.x);
+    const int tg = it.target(threadIdx.x);
+    for (long n = 0; ld_acquire(f) < tg; n++) {
+      if (*(volatile int*)a.abort_flag) {
+        ok = 0;
+        break;
+      }
+      if (n >= a.spin) {
+        atomicOr(a.info, kCoarseWaitGaveUp);
+        atomicExch(a.abort_flag, 1);
+        ok = 0;
+        break;
+      }
+    }
+  }
+  return __syncthreads_and(ok) != 0;
+}
+
+// are the item's inputs ready now? (one look, no wait)
+__device__ bool pf_ready(const PfItem& it) {
+  int ok = 1;
+  if (threadIdx.x < it.nf) ok = ld_acquire(it.flag(threadIdx.x)) >= it.target(threadIdx.x);
+  return __syncthreads_and(ok) != 0;
+}
+
+__device__ __forceinline__ double pf_elem(const PfArgs& a, long I, long J, int r, int c) {
+  const long gr = 32 * I + r, gc = 32 * J + c;
+  return (gr < a.n && gr >= gc && gr - gc <= a.bw) ? __ldcg(a.B + gc * a.bw + gr) : 0.0;
+}
+
+// the item's inputs into registers: element idx = threadIdx.x + 256 m of the
+// two tiles (S: tile (I,k) and L_kk; U: tiles (I,k) and (J,k)), and for S
+// the reciprocal pivots
+struct PfRegs {
+  double p[4], q[4], r;
+};
+
+__device__ __forceinline__ void pf_fetch(const PfArgs& a, const PfItem& it, PfRegs& R) {
+  const long qI = it.solve ? it.k : it.J;
+#pragma unroll
+  for (int m = 0; m < 4; m++) {
+    const int idx = threadIdx.x + 256 * m, r = idx & 31, c = idx >> 5;
+    R.p[m] = pf_elem(a, it.I, it.k, r, c);
+    R.q[m] = pf_elem(a, qI, it.k, r, c);
+  }
+  R.r = (it.solve && threadIdx.x < NB) ? __ldcg(a.rpk + it.k * NB + threadIdx.x) : 0.0;
+}
+
+// S: P, Q row-major (P solved in place); U: transposed, P[t][r] = L(32I + r, 32k + t)
+__device__ __forceinline__ void pf_put(const PfItem& it, const PfRegs& R, double (*P)[NB + 1],
+                                       double (*Q)[NB + 1], double* rp, volatile int* ready) {
+#pragma unroll
+  for (int m = 0; m < 4; m++) {
+    const int idx = threadIdx.x + 256 * m, r = idx & 31, c = idx >> 5;
+    if (it.solve) {
+      P[r][c] = R.p[m];
+      Q[r][c] = R.q[m];
+    } else {
+      P[c][r] = R.p[m];
+      Q[c][r] = R.q[m];
+    }
+  }
+  if (it.solve && threadIdx.x < NB) {
+    rp[threadIdx.x] = R.r;
+    ready[threadIdx.x] = 0;
+  }
+}
+
+// The non-chain CTAs take items g = blockIdx.x - 1 + m (gridDim.x - 1). While
+// one item is computed, the next item's inputs are loaded into registers if
+// its flags are already set (otherwise it waits for them when its turn comes).
 __device__ void pf_bulk(const PfArgs& a, double* smem) {
-  double(*P)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(smem);  // panel tile / row panel block (transposed)
-  double(*Q)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(smem + NB * (NB + 1));  // L_kk / column panel block
+  double(*P)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(smem);
+  double(*Q)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(smem + NB * (NB + 1));
   double* rp = smem + 2 * NB * (NB + 1);
   volatile int* ready = reinterpret_cast<volatile int*>(rp + NB);
   const long nbulk = gridDim.x - 1, total = a.off[a.NT];
-  long k = 0;
-  for (long g = blockIdx.x - 1; g < total; g += nbulk) {
-    while (a.off[k + 1] <= g) k++;
-    const long idx = g - a.off[k];
-    const long T = pf_imax(a.n, a.bw, k) - k;
-    const long prev = k >= 1 ? pf_imax(a.n, a.bw, k - 1) : -1;  // tiles with I <= prev hold a step k-1 update
-    if (idx < T - 1) {  // panel tile (I, k)
-      const long I = k + 2 + idx;
-      if (!pf_wait(a, a.fdone + k, 1)) return;
-      if (I <= prev && !pf_wait(a, a.tver + k * a.TS + (I - k), (int)k)) return;
-      pf_load<false>(a, k, k, Q);
-      pf_load<false>(a, I, k, P);
-      if (threadIdx.x < NB) {
-        rp[threadIdx.x] = __ldcg(a.rpk + k * NB + threadIdx.x);
-        ready[threadIdx.x] = 0;
+  long g = blockIdx.x - 1, kk = 0;
+  if (g >= total) return;
+  PfItem cur, nxt;
+  PfRegs R;
+  pf_item(a, g, kk, cur);
+  bool have = false;
+  for (; g < total; g += nbulk) {
+    if (!have) {
+      if (!pf_wait_item(a, cur)) return;
+      pf_fetch(a, cur, R);
+    }
+    pf_put(cur, R, P, Q, rp, ready);
+    __syncthreads();
+    have = false;
+    if (g + nbulk < total) {
+      pf_item(a, g + nbulk, kk, nxt);
+      if (pf_ready(nxt)) {
+        pf_fetch(a, nxt, R);  // in flight while this item is computed
+        have = true;
       }
-      __syncthreads();
+    }
+    if (cur.solve) {
       trsm_tile(P, NB, Q, rp, ready, a.info);
       __syncthreads();
-      pf_store(a, I, k, P);
-      pf_release(a.sdone + k * a.TS + (I - k), 1);
-    } else {  // update of tile (I, J)
-      long u = idx - (T - 1), I, J;
-      if (u < T - 1) {
-        I = k + 2 + u;
-        J = k + 1;
-      } else {
-        u -= T - 1;
-        long q = (long)((sqrt(8.0 * (double)u + 1.0) - 1.0) / 2.0);
-        while ((q + 1) * (q + 2) / 2 <= u) q++;
-        while (q * (q + 1) / 2 > u) q--;
-        I = k + 2 + q;
-        J = k + 2 + (u - q * (q + 1) / 2);
-      }
-      if (!pf_wait(a, a.sdone + k * a.TS + (I - k), 1)) return;
-      if (J != I && !pf_wait(a, a.sdone + k * a.TS + (J - k), 1)) return;
-      if (I <= prev && !pf_wait(a, a.tver + J * a.TS + (I - J), (int)k)) return;
-      pf_load<true>(a, I, k, P);  // P[t][r] = L(32I + r, 32k + t)
-      pf_load<true>(a, J, k, Q);
-      __syncthreads();
+      pf_store(a, cur.I, cur.k, P);
+      pf_release(a.sdone + cur.k * a.TS + (cur.I - cur.k), 1);
+    } else {
       const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-      const long gr = 32 * I + tx;
+      const long gr = 32 * cur.I + tx;
+      double old[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {  // the tile's current values, loaded before the products
+        const long gc = 32 * cur.J + ty + 8 * q;
+        old[q] = (gr < a.n && gc <= gr && gr - gc <= a.bw) ? __ldcg(a.B + gc * a.bw + gr) : 0.0;
+      }
 #pragma unroll
       for (int q = 0; q < 4; q++) {
         const int cy = ty + 8 * q;
-        const long gc = 32 * J + cy;
+        const long gc = 32 * cur.J + cy;
         double s = 0.0;
 #pragma unroll
         for (int t = 0; t < NB; t++) s += P[t][tx] * Q[t][cy];
-        if (gr < a.n && gc <= gr && gr - gc <= a.bw) {
-          double* p = a.B + gc * a.bw + gr;
-          *p = __ldcg(p) - s;
-        }
+        if (gr < a.n && gc <= gr && gr - gc <= a.bw) a.B[gc * a.bw + gr] = old[q] - s;
       }
-      pf_release(a.tver + J * a.TS + (I - J), (int)k + 1);
+      pf_release(a.tver + cur.J * a.TS + (cur.I - cur.J), (int)cur.k + 1);
     }
+    cur = nxt;
   }
 }
 

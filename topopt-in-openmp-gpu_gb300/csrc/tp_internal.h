@@ -133,8 +133,9 @@ struct tp_ctx {
   double *d_x = nullptr, *d_xphys = nullptr, *d_xnew = nullptr, *d_dc = nullptr,
          *d_dv = nullptr, *d_hs = nullptr;
   double* d_E = nullptr;  // E(xPhys) per fine element
-  double* d_fw = nullptr; // filter weights per offset, (2*ceil(rmin))^3
-  double* d_ocb = nullptr;  // OC scratch: x sqrt(-dc/dv) per element
+  double* d_fw = nullptr; // nonzero filter weights, then their packed offsets (x, z, y loop order)
+  int fw_n = 0;           // their count
+  double* d_ocb = nullptr;  // OC scratch, 3 x ocb_n: x sqrt(-dc/dv), max(0, x-0.2), min(1, x+0.2) per element
   long ocb_n = 0;
   float* d_Ef = nullptr;
 
@@ -225,6 +226,17 @@ void fine_inv_diag(tp_ctx* c, double* invD);
 // element-centric form (tp_kernels_fine_ec.cu): returns the number of CTAs
 // launched, or -1 when the plan or the pointers rule it out
 bool set_fine_kz(const double* ke0, double* kz_out);
+// The 45 non-zeros (index, row, column) of KZ = T KE T^T / 64 (T the per-axis
+// sum/difference transform of an element's 8 nodes, b = bx*4 + by*2 + bz,
+// row = 3b + c), listed once for every kernel that unrolls over them.
+#define TP_KZ_PATTERN(X)                                                                                     \
+  X(0, 3, 3) X(1, 3, 14) X(2, 4, 4) X(3, 4, 8) X(4, 5, 5) X(5, 5, 7) X(6, 5, 12) X(7, 6, 6) X(8, 6, 13)     \
+  X(9, 9, 9) X(10, 9, 16) X(11, 9, 20) X(12, 7, 5) X(13, 7, 7) X(14, 7, 12) X(15, 10, 10) X(16, 10, 15)   \
+  X(17, 8, 4) X(18, 8, 8) X(19, 11, 11) X(20, 11, 18) X(21, 12, 5) X(22, 12, 7) X(23, 12, 12)             \
+  X(24, 15, 10) X(25, 15, 15) X(26, 13, 6) X(27, 13, 13) X(28, 16, 9) X(29, 16, 16) X(30, 16, 20)          \
+  X(31, 14, 3) X(32, 14, 14) X(33, 17, 17) X(34, 17, 19) X(35, 18, 11) X(36, 18, 18) X(37, 21, 21)         \
+  X(38, 19, 17) X(39, 19, 19) X(40, 22, 22) X(41, 20, 9) X(42, 20, 16) X(43, 20, 20) X(44, 23, 23)
+void set_design_kz(const double* kz45);  // the KZ values for the element energies (tp_kernels_design.cu)
 bool ec_plan(tp_ctx* c, int nzg, int ncx, EcPlan* p);
 void ec_default_plans(tp_ctx* c);
 template <typename T> int fine_ec(tp_ctx* c, int mode, const T* E, const T* in, T* out, const T* b, const T* invD, T omega, int nr = 1);

@@ -12,8 +12,17 @@
 namespace tp {
 
 __constant__ double c_ke0_design[576];
+__constant__ double c_kz_design[45];
+static bool g_kz_design = false;
 
-void set_design_ke(const double* ke0) { cudaMemcpyToSymbol(c_ke0_design, ke0, sizeof(double) * 576); }
+void set_design_ke(const double* ke0) {
+  cudaMemcpyToSymbol(c_ke0_design, ke0, sizeof(double) * 576);
+  g_kz_design = false;
+}
+void set_design_kz(const double* kz45) {
+  cudaMemcpyToSymbol(c_kz_design, kz45, sizeof(double) * 45);
+  g_kz_design = true;
+}
 
 __host__ __device__ constexpr int dloc_dx(int q) { return (q == 1 || q == 2 || q == 5 || q == 6) ? 1 : 0; }
 __host__ __device__ constexpr int dloc_dy(int q) { return (q == 0 || q == 1 || q == 4 || q == 5) ? 1 : 0; }
@@ -52,11 +61,48 @@ static DGeom dgeom(const tp_ctx* c) {
 
 constexpr int kMaxBlocks = 4096;
 
+// The per-axis sum/difference transform of an element's 8 nodal 3-vectors
+// (v in the reference's local node order, z[(bx*4 + by*2 + bz)*3 + c]): three
+// butterfly stages, x, y, z. The rigid-translation entries (b = 0) are not
+// formed: KZ's row and column 0..2 vanish.
+__device__ __forceinline__ void t8_transform(const double* v, double* z) {
+  // local node of corner (dx, dy, dz): dz*4 + (dy ? (dx ? 1 : 0) : (dx ? 2 : 3))
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    double a[2][2][2];  // [dy][dz][bx]
+#pragma unroll
+    for (int dy = 0; dy < 2; dy++)
+#pragma unroll
+      for (int dz = 0; dz < 2; dz++) {
+        const double v0 = v[3 * (dz * 4 + (dy ? 0 : 3)) + c], v1 = v[3 * (dz * 4 + (dy ? 1 : 2)) + c];
+        a[dy][dz][0] = v0 + v1;
+        a[dy][dz][1] = v1 - v0;
+      }
+    double b[2][2][2];  // [bx][dz][by]
+#pragma unroll
+    for (int bx = 0; bx < 2; bx++)
+#pragma unroll
+      for (int dz = 0; dz < 2; dz++) {
+        b[bx][dz][0] = a[0][dz][bx] + a[1][dz][bx];
+        b[bx][dz][1] = a[1][dz][bx] - a[0][dz][bx];
+      }
+#pragma unroll
+    for (int bx = 0; bx < 2; bx++)
+#pragma unroll
+      for (int by = 0; by < 2; by++) {
+        if (bx || by) z[(bx * 4 + by * 2) * 3 + c] = b[bx][0][by] + b[bx][1][by];
+        z[(bx * 4 + by * 2 + 1) * 3 + c] = b[bx][1][by] - b[bx][0][by];
+      }
+  }
+}
+
 // out_e = -3 (E0-Emin) x_e^2 w_e^T KE u_e (penalty 3, stencil_methods.c:855-858);
 // with w = u, also the compliance partials sum_e E_e u_e^T KE u_e. With nr
 // load cases (columns vs apart) the compliance and its sensitivity are the
-// sums over the cases.
-template <bool COMPLIANCE>
+// sums over the cases. SF: the energy as (T u)^T KZ (T w) -- the butterfly
+// and the 45 non-zeros -- instead of the dense 24 x 24 product (a quarter
+// of the FP64 instructions; equal to rounding).
+template <bool COMPLIANCE, bool SF>
 __global__ void sens_kernel(DGeom g, const double* __restrict__ x, const double* __restrict__ u,
                             const double* __restrict__ w, double* __restrict__ out,
                             double* __restrict__ partials, int nr, long vs) {
@@ -80,18 +126,35 @@ __global__ void sens_kernel(DGeom g, const double* __restrict__ x, const double*
           we[3 * q + c] = COMPLIANCE ? ue[3 * q + c] : w[3 * n + c];
         }
       }
+      if (SF) {
+        double zu[24], zw[24];
+        t8_transform(ue, zu);
+        if (COMPLIANCE) {
 #pragma unroll
-      for (int ii = 0; ii < 8; ii++) {
-        double cl = 0.0;
-#pragma unroll
-        for (int a = 0; a < 3; a++) {
-          double t = 0.0;
-#pragma unroll
-          for (int b = 0; b < 24; b++) t += c_ke0_design[(ii * 3 + a) * 24 + b] * ue[b];
-          cl += we[3 * ii + a] * t;
+          for (int q = 3; q < 24; q++) zw[q] = zu[q];
+        } else {
+          t8_transform(we, zw);
         }
-        if (COMPLIANCE) csum += cl * (1e-6 + xe * xe * xe * Ed);
-        d += cl * (-3.0 * Ed * xe * xe);
+        double en = 0.0;
+#define TP_KZ_TERM(i, rr, ss) en += c_kz_design[i] * zu[rr] * zw[ss];
+        TP_KZ_PATTERN(TP_KZ_TERM)
+#undef TP_KZ_TERM
+        if (COMPLIANCE) csum += en * (1e-6 + xe * xe * xe * Ed);
+        d += en * (-3.0 * Ed * xe * xe);
+      } else {
+#pragma unroll
+        for (int ii = 0; ii < 8; ii++) {
+          double cl = 0.0;
+#pragma unroll
+          for (int a = 0; a < 3; a++) {
+            double t = 0.0;
+#pragma unroll
+            for (int b = 0; b < 24; b++) t += c_ke0_design[(ii * 3 + a) * 24 + b] * ue[b];
+            cl += we[3 * ii + a] * t;
+          }
+          if (COMPLIANCE) csum += cl * (1e-6 + xe * xe * xe * Ed);
+          d += cl * (-3.0 * Ed * xe * xe);
+        }
       }
     }
     out[e] = d;
@@ -114,7 +177,10 @@ void compliance(tp_ctx* c, const double* u, double* dc, int* nblocks, int nr) {
   const DGeom g = dgeom(c);
   const long ne = (long)g.ex * g.ey * g.ez;
   const int nb = blocks_for(ne);
-  sens_kernel<true><<<nb, 256, 0, c->s>>>(g, c->d_xphys, u, nullptr, dc, c->d_red, nr, c->L[0].ndof);
+  if (c->ec_ok && g_kz_design)
+    sens_kernel<true, true><<<nb, 256, 0, c->s>>>(g, c->d_xphys, u, nullptr, dc, c->d_red, nr, c->L[0].ndof);
+  else
+    sens_kernel<true, false><<<nb, 256, 0, c->s>>>(g, c->d_xphys, u, nullptr, dc, c->d_red, nr, c->L[0].ndof);
   TP_CHECK_LAUNCH(c, "compliance");
   *nblocks = nb;
 }
@@ -123,52 +189,53 @@ void element_sens(tp_ctx* c, const double* u, const double* w, double* out) {
   ProfScope ps(c, P_DESIGN);
   const DGeom g = dgeom(c);
   const long ne = (long)g.ex * g.ey * g.ez;
-  sens_kernel<false><<<blocks_for(ne), 256, 0, c->s>>>(g, c->d_xphys, u, w, out, nullptr, 1, 0);
+  if (c->ec_ok && g_kz_design)
+    sens_kernel<false, true><<<blocks_for(ne), 256, 0, c->s>>>(g, c->d_xphys, u, w, out, nullptr, 1, 0);
+  else
+    sens_kernel<false, false><<<blocks_for(ne), 256, 0, c->s>>>(g, c->d_xphys, u, w, out, nullptr, 1, 0);
   TP_CHECK_LAUNCH(c, "element_sens");
 }
 
 // ----------------------------------------------------------------------------
 // Filter neighbourhood: [i-(ceil(rmin)-1), i+ceil(rmin)] clipped to the grid
 // (stencil_optimization.c:254-269), weights max(0, rmin - |d|), loops in the
-// reference's x, z, y order. The weight depends only on the offset, so it is
-// tabulated once per radius on the host (IEEE sqrt, the same bits as the
-// reference's expression) and zero weights are skipped, which leaves every
-// sum unchanged.
+// reference's x, z, y order. The weight depends only on the offset, so the
+// nonzero weights are tabulated once per radius on the host (IEEE sqrt, the
+// same bits as the reference's expression) with their offsets, in that loop
+// order; skipping the zero weights (and the test for them, an FP64 compare
+// per offset) leaves every sum and its order unchanged.
 struct FBox {
-  int cr;               // ceil(rmin)
-  int side;             // 2*cr: offsets -(cr-1) .. cr
-  const double* w;      // side^3 weights, [(di+cr-1)*side + (dk+cr-1)]*side + (dj+cr-1)
+  int nw;               // nonzero weights
+  const double* w;      // nw weights, then nw packed offsets (di, dk, dj) as doubles
 };
-
-__device__ __forceinline__ void box(int i, int n, int cr, int& lo, int& hi) {
-  lo = max(i - (cr - 1), 0);
-  hi = min(i + cr + 1, n);
-}
+constexpr int kFilterSmem = 512;  // weights staged in shared memory (rmin <= 4 always fits)
 
 template <int MODE>  // 0: Hs, 1: forward H x / Hs, 2: adjoint H (v) with v already / Hs
 __global__ void filter_kernel(DGeom g, FBox fb, const double* __restrict__ in, const double* __restrict__ hs,
                               double* __restrict__ out, double* __restrict__ partials) {
+  __shared__ double sw[kFilterSmem];
+  __shared__ int soff[kFilterSmem];  // (di + 64) << 16 | (dk + 64) << 8 | (dj + 64)
+  const bool staged = fb.nw <= kFilterSmem;  // else read from global memory
+  for (int q = threadIdx.x; staged && q < fb.nw; q += blockDim.x) {
+    sw[q] = fb.w[q];
+    soff[q] = (int)fb.w[fb.nw + q];
+  }
+  __syncthreads();
   const long ne = (long)g.ex * g.ey * g.ez;
   double vsum = 0.0;
   for (long e = blockIdx.x * 256L + threadIdx.x; e < ne; e += (long)gridDim.x * 256) {
     const int j = e % g.ey;
     const int k = (e / g.ey) % g.ez;
     const int i = e / ((long)g.ey * g.ez);
-    int i0, i1, k0, k1, j0, j1;
-    box(i, g.ex, fb.cr, i0, i1);
-    box(k, g.ez, fb.cr, k0, k1);
-    box(j, g.ey, fb.cr, j0, j1);
     double o = 0.0, h = 0.0;
-    for (int i2 = i0; i2 < i1; i2++)
-      for (int k2 = k0; k2 < k1; k2++) {
-        const double* wr = fb.w + ((i2 - i + fb.cr - 1) * fb.side + (k2 - k + fb.cr - 1)) * fb.side + (fb.cr - 1 - j);
-        const double* xr = in + ((long)i2 * g.ez + k2) * g.ey;
-        for (int j2 = j0; j2 < j1; j2++) {
-          const double wgt = __ldg(wr + j2);
-          if (MODE == 0) h += wgt;
-          if (MODE != 0 && wgt != 0.0) o += wgt * xr[j2];
-        }
-      }
+    for (int q = 0; q < fb.nw; q++) {
+      const int of = staged ? soff[q] : (int)__ldg(fb.w + fb.nw + q);
+      const int i2 = i + (of >> 16) - 64, k2 = k + ((of >> 8) & 255) - 64, j2 = j + (of & 255) - 64;
+      if (i2 < 0 || i2 >= g.ex || k2 < 0 || k2 >= g.ez || j2 < 0 || j2 >= g.ey) continue;
+      const double wq = staged ? sw[q] : __ldg(fb.w + q);
+      if (MODE == 0) h += wq;
+      if (MODE != 0) o += wq * in[((long)i2 * g.ez + k2) * g.ey + j2];
+    }
     if (MODE == 0) out[e] = h;
     if (MODE == 1) {
       const double v = o / hs[e];
@@ -188,23 +255,26 @@ __global__ void div_kernel(long n, const double* __restrict__ v, const double* _
   if (e < n) t[e] = v[e] / hs[e];
 }
 
-static FBox fbox(const tp_ctx* c) {
-  const int cr = (int)std::ceil(c->p.rmin);
-  return FBox{cr, 2 * cr, c->d_fw};
-}
+static FBox fbox(const tp_ctx* c) { return FBox{c->fw_n, c->d_fw}; }
 
 // (re)tabulates the weights of the context's radius and the row sums Hs
 void filter_hs(tp_ctx* c, double* hs) {
   ProfScope ps(c, P_DESIGN);
-  const int cr = (int)std::ceil(c->p.rmin), side = 2 * cr;
-  std::vector<double> w((size_t)side * side * side);
+  const int cr = (int)std::ceil(c->p.rmin);
+  std::vector<double> wt, of;
   for (int di = -(cr - 1); di <= cr; di++)
     for (int dk = -(cr - 1); dk <= cr; dk++)
       for (int dj = -(cr - 1); dj <= cr; dj++) {
         const unsigned d2 = (unsigned)(di * di + dj * dj + dk * dk);
         const double v = c->p.rmin - std::sqrt((double)d2);
-        w[((size_t)(di + cr - 1) * side + (dk + cr - 1)) * side + (dj + cr - 1)] = v > 0.0 ? v : 0.0;
+        if (v > 0.0) {
+          wt.push_back(v);
+          of.push_back((double)(((di + 64) << 16) | ((dk + 64) << 8) | (dj + 64)));
+        }
       }
+  c->fw_n = (int)wt.size();
+  std::vector<double> w(wt);
+  w.insert(w.end(), of.begin(), of.end());
   if (c->d_fw) cudaFree(c->d_fw);
   c->d_fw = nullptr;
   if (cudaMalloc(&c->d_fw, sizeof(double) * w.size()) != cudaSuccess) {
@@ -272,25 +342,27 @@ __device__ __forceinline__ double oc_xnew(double x, double dc, double dv, double
 // B = x sqrt(-dc/dv) formed once per update, which takes the division and the
 // square root of every element out of the ~50 steps (they agree with the
 // reference's expression to a few ulp; the final pass below evaluates the
-// reference's expression itself at the chosen lmid).
+// reference's expression itself at the chosen lmid). The reference's nested
+// MAX/MIN equal max(lo, min(hi, xs)) with lo = max(0, x - move) and
+// hi = min(1, x + move) -- min and max do not round -- and lo, hi are formed
+// once too: FP64 instructions are what a step costs on this part, and this
+// leaves five per element (multiply, min, max, subtract, multiply-add).
 __global__ void oc_prep_kernel(long n, const double* __restrict__ x, const double* __restrict__ dc,
-                               const double* __restrict__ dv, double* __restrict__ B) {
+                               const double* __restrict__ dv, double* __restrict__ B, double* __restrict__ lo,
+                               double* __restrict__ hi) {
   const long e = blockIdx.x * 256L + threadIdx.x;
-  if (e < n) B[e] = x[e] * sqrt(-dc[e] / dv[e]);
-}
-
-__device__ __forceinline__ double oc_clamp(double x, double xs) {
-  const double move = 0.2;
-  const double a = (x + move > xs) ? xs : x + move;
-  const double b = (1.0 > a) ? a : 1.0;
-  const double cc = (x - move > b) ? x - move : b;
-  return (0.0 > cc) ? 0.0 : cc;
+  if (e >= n) return;
+  const double move = 0.2, xe = x[e];
+  B[e] = xe * sqrt(-dc[e] / dv[e]);
+  lo[e] = fmax(0.0, xe - move);
+  hi[e] = fmin(1.0, xe + move);
 }
 
 // one bisection step: partial sums of dv*(xnew - x) at lmid = (l1 + l2)/2;
 // B = nullptr evaluates the reference's expression per element instead
 __global__ void oc_step_kernel(long n, const double* __restrict__ x, const double* __restrict__ dc,
                                const double* __restrict__ dv, const double* __restrict__ B,
+                               const double* __restrict__ lo, const double* __restrict__ hi,
                                double* __restrict__ scal, double* __restrict__ partials) {
   if (scal[S_OCDONE] != 0.0) return;
   const double lmid = 0.5 * (scal[S_L2] + scal[S_L1]);
@@ -298,7 +370,7 @@ __global__ void oc_step_kernel(long n, const double* __restrict__ x, const doubl
   double s = 0.0;
   for (long e = blockIdx.x * 256L + threadIdx.x; e < n; e += (long)gridDim.x * 256) {
     const double xe = x[e];
-    const double xn = B ? oc_clamp(xe, B[e] * rl) : oc_xnew(xe, dc[e], dv[e], lmid);
+    const double xn = B ? fmax(lo[e], fmin(hi[e], B[e] * rl)) : oc_xnew(xe, dc[e], dv[e], lmid);
     s += dv[e] * (xn - xe);
   }
   s = bsum256(s);
@@ -368,16 +440,19 @@ int oc_bisect(tp_ctx* c, long ne, double* x, double* xnew, const double* dc, con
   ProfScope ps(c, P_DESIGN);
   const int nb = blocks_for(ne);
   oc_init_kernel<<<1, 1, 0, c->s>>>(c->d_scal);
-  const double* B = nullptr;
+  const double *B = nullptr, *lo = nullptr, *hi = nullptr;
   if (c->d_ocb && ne <= c->ocb_n) {
-    oc_prep_kernel<<<grid_for(ne, 256), 256, 0, c->s>>>(ne, x, dc, dv, c->d_ocb);
-    B = c->d_ocb;
+    double* b = c->d_ocb;
+    oc_prep_kernel<<<grid_for(ne, 256), 256, 0, c->s>>>(ne, x, dc, dv, b, b + ne, b + 2 * ne);
+    B = b;
+    lo = b + ne;
+    hi = b + 2 * ne;
   }
   const int kBatch = 24, kMaxSteps = 240;
   int taken = 0;
   for (;;) {
     for (int q = 0; q < kBatch; q++) {
-      oc_step_kernel<<<nb, 256, 0, c->s>>>(ne, x, dc, dv, B, c->d_scal, c->d_red);
+      oc_step_kernel<<<nb, 256, 0, c->s>>>(ne, x, dc, dv, B, lo, hi, c->d_scal, c->d_red);
       oc_finish_kernel<<<1, 256, 0, c->s>>>(c->d_red, nb, c->d_scal, g);
     }
     taken += kBatch;

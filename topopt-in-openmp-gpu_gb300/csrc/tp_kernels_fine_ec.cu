@@ -45,12 +45,9 @@ __device__ __forceinline__ float kz<float>(int i) { return c_kzf[i]; }
 
 // (row, column) of the 45 non-zeros of KZ, row = 3*b + c, in the order the
 // kernel consumes them
-static const unsigned char kKzPattern[45][2] = {
-    {3, 3},   {3, 14},  {4, 4},   {4, 8},   {5, 5},   {5, 7},   {5, 12},  {6, 6},   {6, 13},
-    {9, 9},   {9, 16},  {9, 20},  {7, 5},   {7, 7},   {7, 12},  {10, 10}, {10, 15}, {8, 4},
-    {8, 8},   {11, 11}, {11, 18}, {12, 5},  {12, 7},  {12, 12}, {15, 10}, {15, 15}, {13, 6},
-    {13, 13}, {16, 9},  {16, 16}, {16, 20}, {14, 3},  {14, 14}, {17, 17}, {17, 19}, {18, 11},
-    {18, 18}, {21, 21}, {19, 17}, {19, 19}, {22, 22}, {20, 9},  {20, 16}, {20, 20}, {23, 23}};
+#define TP_KZ_PAIR(i, r, s) {r, s},
+static const unsigned char kKzPattern[45][2] = {TP_KZ_PATTERN(TP_KZ_PAIR)};
+#undef TP_KZ_PAIR
 
 static int loc_node(int dx, int dy, int dz) { return dz * 4 + (dy ? (dx ? 1 : 0) : (dx ? 2 : 3)); }
 

@@ -330,7 +330,7 @@ static void destroy_buffers(tp_ctx* c) {
     if (p) cudaFree(p);
   };
   for (int l = 0; l < TP_MAXL; l++) {
-    F(c->d_ke[l]); F(c->d_kef[l]);
+    F(c->d_ke[l]); F(c->d_kef[l]); F(c->d_mgc[l]); F(c->d_mgi[l]);
     F(c->mg_r[l]); F(c->mg_z[l]); F(c->mg_d[l]); F(c->mg_t[l]);
     F(c->mgf_r[l]); F(c->mgf_z[l]); F(c->mgf_d[l]); F(c->mgf_t[l]);
     F(c->invD[l]); F(c->invDf[l]); F(c->st[l]); F(c->stf[l]); F(c->st_sub[l]);
@@ -338,7 +338,7 @@ static void destroy_buffers(tp_ctx* c) {
   F(c->d_x); F(c->d_xphys); F(c->d_xnew); F(c->d_dc); F(c->d_dv); F(c->d_hs); F(c->d_ocb);
   F(c->d_E); F(c->d_Ef); F(c->d_F); F(c->d_U);
   F(c->d_r); F(c->d_z); F(c->d_p); F(c->d_q);
-  F(c->d_red); F(c->d_scal); F(c->d_flag); F(c->scratch_invD); F(c->d_fw);
+  F(c->d_red); F(c->d_scal); F(c->d_flag); F(c->scratch_invD); F(c->d_fw); F(c->d_mom);
   if (c->h_scal) cudaFreeHost(c->h_scal);
   graph_free(c);
   coarse_free(c);
@@ -369,6 +369,8 @@ tp_status tp_create(const tp_params* p, tp_ctx** out) {
 
   bool ok = true;
   // element stiffness tables
+  std::vector<double> ke0;
+  long mom_n = 0;
   for (int l = 0; l < c->nl && ok; l++) {
     const long nk = 576L << (3 * l);
     std::vector<double> ke(nk);
@@ -379,7 +381,24 @@ tp_status tp_create(const tp_params* p, tp_ctx** out) {
       cudaMemcpy(c->d_ke[l], ke.data(), sizeof(double) * nk, cudaMemcpyHostToDevice);
       cudaMemcpy(c->d_kef[l], kf.data(), sizeof(float) * nk, cudaMemcpyHostToDevice);
     }
+    if (l >= 2 && ok) {  // element matrices from moments where they reproduce the tables
+      std::vector<int> off, pidx;
+      std::vector<double> coef;
+      if (moment_tables(ke0.data(), ke.data(), l, off, pidx, coef)) {
+        const int nnz = (int)coef.size();
+        std::vector<int> ints(pidx);
+        ints.insert(ints.end(), off.begin(), off.end());
+        ok = (c->d_mgc[l] = dalloc<double>(c, nnz)) && (c->d_mgi[l] = dalloc<int>(c, (long)ints.size()));
+        if (ok) {
+          cudaMemcpy(c->d_mgc[l], coef.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice);
+          cudaMemcpy(c->d_mgi[l], ints.data(), sizeof(int) * ints.size(), cudaMemcpyHostToDevice);
+          c->mg_nnz[l] = nnz;
+          mom_n = std::max(mom_n, 27L * c->L[l].ex * c->L[l].ey * c->L[l].ez);
+        }
+      }
+    }
     if (l == 0) {
+      ke0 = ke;
       set_fine_ke(ke.data());
       set_design_ke(ke.data());
       double kz45[45];
@@ -397,6 +416,7 @@ tp_status tp_create(const tp_params* p, tp_ctx** out) {
        (c->d_F = dalloc<double>(c, nv)) && (c->d_U = dalloc<double>(c, nv)) &&
        (c->d_r = dalloc<double>(c, nv)) && (c->d_z = dalloc<double>(c, nv)) &&
        (c->d_p = dalloc<double>(c, nv)) && (c->d_q = dalloc<double>(c, nv));
+  if (ok && mom_n > 0) ok = (c->d_mom = dalloc<double>(c, mom_n)) != nullptr;
   // every solver vector holds one column per load case
   for (int l = 0; l < c->nl && ok; l++) {
     const long nd = c->L[l].ndof, ndr = nd * p->nrhs;

@@ -34,6 +34,8 @@ Level make_level(int nelx, int nely, int nelz, int l);
 // Host set-up (tp_setup.cpp)
 void element_matrix_tables(double nu, int l, double* KE);   // 576 * ncell^3
 void cantilever_load(const Level& L0, double* F);            // 3*nnodes
+bool moment_tables(const double* ke0, const double* ke_l, int l, std::vector<int>& off, std::vector<int>& pidx,
+                   std::vector<double>& coef);               // level-l element matrices from 27 moments
 
 // Reduction scratch: partial sums of one pass, one slot per block.
 constexpr int kRedSlots = 4096;
@@ -127,6 +129,12 @@ struct tp_ctx {
 
   // element stiffness tables per level (576 * ncell^3), FP64 and FP32 copies
   double* d_ke[TP_MAXL] = {};
+  // levels >= 2: element matrices from moments (tp_setup.cpp moment_tables):
+  // coefficients [nnz], then moment indices [nnz] and block offsets [577] as ints
+  double* d_mgc[TP_MAXL] = {};
+  int* d_mgi[TP_MAXL] = {};
+  int mg_nnz[TP_MAXL] = {};   // 0: that level assembles from the sub-cell tables
+  double* d_mom = nullptr;    // 27 moments per coarse element (the largest such level)
   float* d_kef[TP_MAXL] = {};
 
   // design fields (fine elements), FP64

@@ -104,12 +104,131 @@ __global__ void assemble_kernel(CGeom g, const T* __restrict__ E, const T* __res
   }
 }
 
+// Levels >= 2 (tables from moment_tables, tp_setup.cpp): first the 27
+// moments M[px*9 + py*3 + pz] = sum_s E_s mx^px my^py mz^pz of each coarse
+// element's sub-cell densities (one thread per element, factorised along
+// y, z, x), then per node the same 27 x 8 blocks as assemble_kernel, each
+// entry a short sparse combination of one element's moments (about 11
+// coefficients, staged in shared memory) instead of a sum over ncell^3
+// sub-cells. FP64 throughout; the stencil is stored in T.
+__global__ void moments_kernel(CGeom g, const double* __restrict__ E, double* __restrict__ M, long ncoarse) {
+  const long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (e >= ncoarse) return;
+  const int cj = e % g.ey, ck = (e / g.ey) % g.ez, ci = e / ((long)g.ey * g.ez);
+  const int nc = g.ncell;
+  const double h = 1.0 / nc;
+  double mom[27];
+#pragma unroll
+  for (int p = 0; p < 27; p++) mom[p] = 0.0;
+  for (int ii = 0; ii < nc; ii++) {
+    const double mx = (ii + 0.5) * h - 0.5;
+    double yz[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) yz[q] = 0.0;
+    for (int kk = 0; kk < nc; kk++) {
+      const double mz = (kk + 0.5) * h - 0.5;
+      const double* row = E + ((long)(ci * nc + ii) * g.fez + (ck * nc + kk)) * g.fey + (long)cj * nc;
+      double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+      for (int jj = 0; jj < nc; jj++) {
+        const double my = (jj + 0.5) * h - 0.5, ev = row[jj], t = my * ev;
+        s0 += ev;
+        s1 += t;
+        s2 += my * t;
+      }
+      const double s[3] = {s0, s1, s2}, pz[3] = {1.0, mz, mz * mz};
+#pragma unroll
+      for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) yz[a * 3 + b] += s[a] * pz[b];
+    }
+    const double px[3] = {1.0, mx, mx * mx};
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int q = 0; q < 9; q++) mom[a * 9 + q] += yz[q] * px[a];
+  }
+#pragma unroll
+  for (int p = 0; p < 27; p++) M[(long)p * ncoarse + e] = mom[p];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256, 1) moment_stencil_kernel(CGeom g, const double* __restrict__ M, long ncoarse,
+                                                             const double* __restrict__ gcoef,
+                                                             const int* __restrict__ gint, int nnz,
+                                                             T* __restrict__ st, double* __restrict__ invD, int masked) {
+  extern __shared__ double smg[];
+  double* sc = smg;                                   // coefficients
+  int* sp = reinterpret_cast<int*>(smg + nnz);        // moment indices
+  int* so = sp + nnz;                                 // offsets, 64 blocks x 9 entries + 1
+  for (int q = threadIdx.x; q < nnz; q += blockDim.x) {
+    sc[q] = gcoef[q];
+    sp[q] = gint[q];
+  }
+  for (int q = threadIdx.x; q <= 576; q += blockDim.x) so[q] = gint[nnz + q];
+  __syncthreads();
+  const long n = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (n >= g.nnodes) return;
+  const int j = n % g.ny;
+  const int k = (n / g.ny) % g.nz;
+  const int i = n / ((long)g.ny * g.nz);
+  const bool nfix = is_fixed(g, i, j);
+  for (int m = 0; m < 27; m++) {
+    const int mx = m / 9 - 1, mz = (m / 3) % 3 - 1, my = m % 3 - 1;
+    double acc[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) acc[q] = 0.0;
+    const int mi = i + mx, mk = k + mz, mj = j + my;
+    const bool minside = mi >= 0 && mi < g.nx && mk >= 0 && mk < g.nz && mj >= 0 && mj < g.ny;
+    if (minside) {
+#pragma unroll
+      for (int e = 0; e < 8; e++) {
+        const int ex = -(e & 1), ez = -((e >> 1) & 1), ey = -((e >> 2) & 1);
+        const int rx = mx - ex, ry = my - ey, rz = mz - ez;
+        if (rx < 0 || rx > 1 || ry < 0 || ry > 1 || rz < 0 || rz > 1) continue;
+        const int ci = i + ex, ck = k + ez, cj = j + ey;
+        if (ci < 0 || ci >= g.ex || ck < 0 || ck >= g.ez || cj < 0 || cj >= g.ey) continue;
+        const int blk = (cloc(-ex, -ey, -ez) * 8 + cloc(rx, ry, rz)) * 9;
+        const double* Me = M + ((long)ci * g.ez + ck) * g.ey + cj;
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+          double a = 0.0;
+          for (int t = so[blk + q]; t < so[blk + q + 1]; t++) a += sc[t] * Me[(long)sp[t] * ncoarse];
+          acc[q] += a;
+        }
+      }
+    }
+    if (m == 13) {  // the node itself: Jacobi diagonal before BCs
+      for (int c = 0; c < 3; c++) invD[3 * n + c] = nfix ? 1.0 : 1.0 / acc[4 * c];
+    }
+    bool zero = !minside;
+    if (nfix) zero = true;
+    if (masked && minside && is_fixed(g, mi, mj)) zero = true;
+#pragma unroll
+    for (int q = 0; q < 9; q++) {
+      T v = zero ? T(0) : (T)acc[q];
+      if (nfix && m == 13 && (q % 4 == 0)) v = T(1);
+      st[(long)(m * 9 + q) * g.nnodes + n] = v;
+    }
+  }
+}
+
 template <typename T>
 void assemble_stencil(tp_ctx* c, int l, const T* E, const T* ke, T* st, double* invD, int masked) {
   ProfScope ps(c, P_ASSEMBLE);
   const CGeom g = cgeom(c, l);
   const int nsub = g.ncell * g.ncell * g.ncell;
   const int threads = 256;
+  if (l >= 2 && c->mg_nnz[l] > 0 && c->d_mom) {
+    const long nce = (long)c->L[l].ex * c->L[l].ey * c->L[l].ez;
+    const int nnz = c->mg_nnz[l];
+    const size_t smem = sizeof(double) * nnz + sizeof(int) * (nnz + 577);
+    moments_kernel<<<grid_for(nce, 128), 128, 0, c->s>>>(g, c->d_E, c->d_mom, nce);
+    cudaFuncSetAttribute(moment_stencil_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    moment_stencil_kernel<T><<<grid_for(g.nnodes, threads), threads, smem, c->s>>>(
+        g, c->d_mom, nce, c->d_mgc[l], c->d_mgi[l], nnz, st, invD, masked);
+    TP_CHECK_LAUNCH(c, "assemble_stencil");
+    return;
+  }
   if (nsub >= 32) {
     assemble_kernel<T, 32><<<grid_for(g.nnodes * 32, threads), threads, 0, c->s>>>(g, E, ke, st, invD, masked);
   } else if (nsub >= 8) {

@@ -179,11 +179,12 @@ tp_status tp_set_fine_variant(tp_ctx* c, int variant);
  * redone at the next solve. Each variant sums in a fixed order, so repeated
  * runs agree bit for bit; the two variants agree to rounding. */
 tp_status tp_set_coarse_solve_variant(tp_ctx* c, int variant);
-/* Failure detection of the single-launch coarse solve (host-side fault
- * injection, for tests): each grid-barrier wait gives up after spin polls
- * (0 = the default, about a second) and, with missing = 1, waits for one
- * arrival that never comes, so every wait runs out. The solve then reports
- * TP_ERR_TIMEOUT and the context stays usable; (0, 0) restores the defaults. */
+/* Failure detection of the single-launch coarse factor and solve (host-side
+ * fault injection, for tests): each of their waits in global memory gives up
+ * after spin polls (0 = the default, about a second) and, with missing = 1,
+ * each grid barrier of the solve waits for one arrival that never comes, so
+ * every such wait runs out. The factor or solve then reports TP_ERR_TIMEOUT
+ * and the context stays usable; (0, 0) restores the defaults. */
 tp_status tp_fault_coarse_barrier(tp_ctx* c, long spin, int missing);
 /* Times the element-centric kernel's launch shapes (z groups per CTA, x
  * chunks) for each precision and fused mode on the context's grid and keeps

@@ -89,3 +89,24 @@ def test_barrier_wait_gives_up(case):
     assert e.value.status == 7 and "barrier" in str(e.value)
     ctx.fault_coarse_barrier(0, 0)
     assert np.array_equal(ctx.coarse_solve(b).cpu().numpy(), good)  # the context is usable
+
+
+def test_factor_wait_gives_up(case):
+    """The single-launch factorisation's waits are bounded: with a budget of one
+    poll the first wait for the chain CTA's diagonal tile runs out, every CTA
+    leaves, and the assembly reports TP_ERR_TIMEOUT; with the default budget the
+    next assembly gives the same factor as before, bit for bit."""
+    ctx, x, torch = case
+    if ctx.shape != (64, 32, 32):
+        pytest.skip("one grid suffices")
+    lc = ctx.nl - 1
+    b = _dev(torch, np.random.default_rng(8).uniform(-1, 1, ctx.ndof(lc)))
+    ctx.set_coarse_solve_variant(0)
+    good = ctx.coarse_solve(b).cpu().numpy()
+    ctx.fault_coarse_barrier(1, 0)
+    with pytest.raises(tp.TopOptError) as e:
+        ctx.assemble()
+    assert e.value.status == 7 and "wait" in str(e.value)
+    ctx.fault_coarse_barrier(0, 0)
+    ctx.assemble()
+    assert np.array_equal(ctx.coarse_solve(b).cpu().numpy(), good)

@@ -177,10 +177,10 @@ static tp_status assemble(tp_ctx* c) {
   for (int l = 1; l < c->nl; l++) {
     const bool coarsest = (l == c->nl - 1);
     if (!mixed(c) || coarsest) {
-      assemble_stencil<double>(c, l, c->d_E, c->d_ke[l], c->st[l], c->invD[l], l >= 2);
+      assemble_stencil<double>(c, l, c->d_E, c->d_ke[l], c->st[l], c->invD[l]);
     }
     if (mixed(c) && !coarsest) {
-      assemble_stencil<float>(c, l, c->d_Ef, c->d_kef[l], c->stf[l], c->invD[l], l >= 2);
+      assemble_stencil<float>(c, l, c->d_Ef, c->d_kef[l], c->stf[l], c->invD[l]);
       cast_d2f(c, c->L[l].ndof, c->invD[l], c->invDf[l]);
     }
     if (mixed(c) && coarsest) cast_d2f(c, c->L[l].ndof, c->invD[l], c->invDf[l]);
@@ -429,8 +429,10 @@ tp_status tp_create(const tp_params* p, tp_ctx** out) {
       ok = (c->mgf_r[l] = dalloc<float>(c, ndr)) && (c->mgf_z[l] = dalloc<float>(c, ndr)) &&
            (c->mgf_d[l] = dalloc<float>(c, ndr)) && (c->mgf_t[l] = dalloc<float>(c, ndr)) &&
            (c->invDf[l] = dalloc<float>(c, nd));
-    if (ok && l >= 1 && (!mx || coarsest)) ok = (c->st[l] = dalloc<double>(c, 243 * c->L[l].nnodes)) != nullptr;
-    if (ok && l >= 1 && mx && !coarsest) ok = (c->stf[l] = dalloc<float>(c, 243 * c->L[l].nnodes)) != nullptr;
+    if (ok && l >= 1 && (!mx || coarsest))
+      ok = (c->st[l] = dalloc<double>(c, kStencilCoef * c->L[l].nnodes)) != nullptr;
+    if (ok && l >= 1 && mx && !coarsest)
+      ok = (c->stf[l] = dalloc<float>(c, kStencilCoef * c->L[l].nnodes)) != nullptr;
   }
   const long red = std::max<long>(1 << 16, (long)fine_blocks(c) * p->nrhs);
   const long nscal = (long)S_COUNT * p->nrhs;

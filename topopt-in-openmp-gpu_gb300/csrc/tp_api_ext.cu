@@ -22,18 +22,21 @@ tp_status sync_status(tp_ctx* c) {
   return c->err.empty() ? TP_OK : TP_ERR_CUDA;
 }
 
-// level l >= 1 stencil with the matrix-free semantics of the reference's
-// subspace operator (stencil_methods.c:436-519): fixed columns NOT zeroed
-const double* subspace_stencil(tp_ctx* c, int l) {
-  if (l == 1 && c->assembled && c->st[1]) return c->st[1];
+// FP64 stencil of level l >= 1 (half stored, no boundary conditions: the
+// caller picks the semantics when it applies it -- the reference's subspace
+// operator, stencil_methods.c:436-519, keeps the fixed columns; its CSR
+// levels, stencil_assembly.c:226-259, drop them): the context's own where it
+// is FP64, else an FP64 copy assembled on demand
+const double* api_stencil(tp_ctx* c, int l) {
+  if (c->assembled && c->st[l]) return c->st[l];
   if (!c->st_sub[l]) {
-    if (cudaMalloc(&c->st_sub[l], sizeof(double) * 243 * c->L[l].nnodes) != cudaSuccess) return nullptr;
-    c->mem_bytes += 8L * 243 * c->L[l].nnodes;
+    if (cudaMalloc(&c->st_sub[l], sizeof(double) * kStencilCoef * c->L[l].nnodes) != cudaSuccess) return nullptr;
+    c->mem_bytes += 8L * kStencilCoef * c->L[l].nnodes;
   }
   if (!c->st_sub_valid[l]) {
     if (!c->scratch_invD) cudaMalloc(&c->scratch_invD, sizeof(double) * c->L[0].ndof);
     compute_E(c);
-    assemble_stencil<double>(c, l, c->d_E, c->d_ke[l], c->st_sub[l], c->scratch_invD, 0);
+    assemble_stencil<double>(c, l, c->d_E, c->d_ke[l], c->st_sub[l], c->scratch_invD);
     c->st_sub_valid[l] = true;
   }
   return c->st_sub[l];
@@ -91,9 +94,13 @@ tp_status tp_fault_coarse_barrier(tp_ctx* c, long spin, int missing) {
   Coarse& C = c->coarse;
   C.ps_spin = spin;
   C.ps_missing = missing;
-  if (C.graph_exec) {  // the captured solve holds the old values
+  if (C.graph_exec) {  // the captured solve and factorisation hold the old values
     cudaGraphExecDestroy(C.graph_exec);
     C.graph_exec = nullptr;
+  }
+  if (C.factor_exec) {
+    cudaGraphExecDestroy(C.factor_exec);
+    C.factor_exec = nullptr;
   }
   graph_free(c);
   return TP_OK;
@@ -102,13 +109,9 @@ tp_status tp_fault_coarse_barrier(tp_ctx* c, long spin, int missing) {
 tp_status tp_apply_subspace(tp_ctx* c, int level, const double* in, double* out) {
   if (!c || level < 0 || level >= c->nl || !in || !out) return TP_ERR_ARG;
   if (level == 0) return tp_apply(c, 0, in, out);
-  if (level == 1 && c->st[1] && c->assembled) {
-    stencil_apply<double>(c, 1, c->st[1], in, out);
-    return sync_status(c);
-  }
-  const double* st = subspace_stencil(c, level);
+  const double* st = api_stencil(c, level);
   if (!st) return TP_ERR_ALLOC;
-  stencil_apply<double>(c, level, st, in, out);
+  stencil_apply<double>(c, level, st, in, out, 1, 0);  // fixed columns kept
   return sync_status(c);
 }
 
@@ -121,9 +124,10 @@ tp_status tp_smooth_ex(tp_ctx* c, int level, int subspace, int nswp, double omeg
   }
   const double* A = nullptr;
   if (level >= 1) {
-    A = (subspace && level >= 2) ? subspace_stencil(c, level) : c->st[level];
+    A = api_stencil(c, level);
     if (!A) return TP_ERR_STATE;
   }
+  const int masked = (level >= 2 && !subspace) ? 1 : 0;
   const double* D = invD ? invD : c->invD[level];
   const long nd = c->L[level].ndof;
   double* cur = u;
@@ -132,7 +136,7 @@ tp_status tp_smooth_ex(tp_ctx* c, int level, int subspace, int nswp, double omeg
     if (level == 0)
       fine_jacobi<double>(c, c->d_E, D, b, cur, nxt, omega);
     else
-      stencil_jacobi<double>(c, level, A, D, b, cur, nxt, omega);
+      stencil_jacobi<double>(c, level, A, D, b, cur, nxt, omega, 1, masked);
     std::swap(cur, nxt);
   }
   if (cur != u) cudaMemcpyAsync(u, cur, sizeof(double) * nd, cudaMemcpyDeviceToDevice, c->s);
@@ -145,10 +149,16 @@ tp_status tp_download_stencil(tp_ctx* c, int level, int subspace, double* host) 
     tp_status st = tp_assemble(c);
     if (st != TP_OK) return st;
   }
-  const double* A = (subspace && level >= 2) ? subspace_stencil(c, level) : c->st[level];
+  const double* A = api_stencil(c, level);
   if (!A) return TP_ERR_STATE;
-  cudaMemcpyAsync(host, A, sizeof(double) * 243 * c->L[level].nnodes, cudaMemcpyDeviceToHost, c->s);
-  return sync_status(c);
+  const long nc = 243L * c->L[level].nnodes;
+  double* full = nullptr;
+  if (cudaMalloc(&full, sizeof(double) * nc) != cudaSuccess) return TP_ERR_ALLOC;
+  stencil_expand(c, level, A, full, (level >= 2 && !subspace) ? 1 : 0);
+  cudaMemcpyAsync(host, full, sizeof(double) * nc, cudaMemcpyDeviceToHost, c->s);
+  tp_status st = sync_status(c);
+  cudaFree(full);
+  return st;
 }
 
 // Factor the coarsest operator given as CSR on the host (row-major, the

@@ -57,13 +57,16 @@ __device__ __forceinline__ void cp_wait() {
 }
 
 // ----------------------------------------------------------------------------
-// band assembly from the coarsest FP64 stencil (BCs already applied there)
-__global__ void band_scatter_kernel(int nx, int ny, int nz, long nnodes, long bw,
+// band assembly from the coarsest FP64 stencil (half stored, no boundary
+// conditions) with the conditions of that level: fixed rows identity, and
+// with masked the columns of fixed DOFs zeroed. Only neighbours m <= 13 (of
+// smaller or equal node index) reach the lower band.
+__global__ void band_scatter_kernel(int nx, int ny, int nz, int lim, long nnodes, long bw, int masked,
                                     const double* __restrict__ st, double* __restrict__ B) {
   const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (t >= nnodes * 27) return;
+  if (t >= nnodes * 14) return;
   const long n = t % nnodes;
-  const int m = (int)(t / nnodes);
+  const int m = (int)(t / nnodes);  // 0..13
   const int j = n % ny;
   const int k = (n / ny) % nz;
   const int i = n / ((long)ny * nz);
@@ -71,10 +74,20 @@ __global__ void band_scatter_kernel(int nx, int ny, int nz, long nnodes, long bw
   const int mi = i + mx, mk = k + mz, mj = j + my;
   if (mi < 0 || mi >= nx || mk < 0 || mk >= nz || mj < 0 || mj >= ny) return;
   const long nm = ((long)mi * nz + mk) * ny + mj;
+  const bool nfix = i == 0 && (j < lim || j >= ny - lim);
+  const bool mfix = mi == 0 && (mj < lim || mj >= ny - lim);
   for (int c = 0; c < 3; c++)
     for (int d = 0; d < 3; d++) {
       const long r = 3 * n + c, col = 3 * nm + d;
-      if (col <= r && r - col <= bw) B[col * bw + r] = st[(long)(m * 9 + 3 * c + d) * nnodes + n];
+      if (col > r || r - col > bw) continue;
+      double v;
+      if (nfix)
+        v = (r == col) ? 1.0 : 0.0;
+      else if (masked && m != 13 && mfix)
+        v = 0.0;
+      else
+        v = (m == 13) ? st[(long)(3 * c + d) * nnodes + n] : st[((long)(13 - m) * 9 + 3 * d + c) * nnodes + nm];
+      B[col * bw + r] = v;
     }
 }
 
@@ -146,8 +159,9 @@ void coarse_assemble(tp_ctx* c) {
   const int l = c->nl - 1;
   const Level& L = c->L[l];
   cudaMemsetAsync(C.band, 0, C.band_elems * sizeof(double), c->s);
-  const long work = L.nnodes * 27;
-  band_scatter_kernel<<<grid_for(work, 256), 256, 0, c->s>>>(L.nx, L.ny, L.nz, L.nnodes, C.bw, c->st[l], C.band);
+  const long work = L.nnodes * 14;
+  band_scatter_kernel<<<grid_for(work, 256), 256, 0, c->s>>>(L.nx, L.ny, L.nz, L.lim, L.nnodes, C.bw, l >= 2 ? 1 : 0,
+                                                             c->st[l], C.band);
   TP_CHECK_LAUNCH(c, "band_scatter");
 }
 

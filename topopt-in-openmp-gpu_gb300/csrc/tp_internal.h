@@ -160,12 +160,13 @@ struct tp_ctx {
   double* invD[TP_MAXL] = {};
   float* invDf[TP_MAXL] = {};
 
-  // assembled 27-point block stencils of levels 1 .. nl-1 (243 coefficients
-  // per node, coefficient-major: A[(nb*9 + c*3 + d)*nnodes + n])
+  // assembled block stencils of levels 1 .. nl-1, half stored (kStencilCoef
+  // coefficients per node, coefficient-major: A[((m-13)*9 + c*3 + d)*nnodes + n]
+  // for the neighbours m = 13..26), without boundary conditions
   double* st[TP_MAXL] = {};
   float* stf[TP_MAXL] = {};
-  // on demand: levels >= 2 with the subspace-operator semantics (fixed
-  // columns kept), for the reference-signature entry points
+  // on demand: an FP64 copy of a level that only has an FP32 stencil (the
+  // mixed form), for the reference-signature entry points
   double* st_sub[TP_MAXL] = {};
   bool st_sub_valid[TP_MAXL] = {};
   double* scratch_invD = nullptr;
@@ -250,10 +251,16 @@ void ec_default_plans(tp_ctx* c);
 template <typename T> int fine_ec(tp_ctx* c, int mode, const T* E, const T* in, T* out, const T* b, const T* invD, T omega, int nr = 1);
 
 // levels >= 1 (assembled block stencils)
-template <typename T> void assemble_stencil(tp_ctx* c, int l, const T* E, const T* ke, T* st, double* invD, int masked);
-template <typename T> void stencil_apply(tp_ctx* c, int l, const T* st, const T* in, T* out, int nr = 1);
-template <typename T> void stencil_jacobi(tp_ctx* c, int l, const T* st, const T* invD, const T* b, const T* u, T* unew, T omega, int nr = 1);
-template <typename T> void stencil_resid(tp_ctx* c, int l, const T* st, const T* b, const T* u, T* d, int nr = 1);
+// Level >= 1 stencils: the symmetric operator without boundary conditions,
+// half stored (kStencilCoef coefficients per node); masked < 0 applies the
+// level's own conditions (fixed rows identity; columns of fixed DOFs dropped
+// from level 2 on), 0 or 1 forces the column masking off or on.
+constexpr int kStencilCoef = 14 * 9;
+template <typename T> void assemble_stencil(tp_ctx* c, int l, const T* E, const T* ke, T* st, double* invD);
+template <typename T> void stencil_apply(tp_ctx* c, int l, const T* st, const T* in, T* out, int nr = 1, int masked = -1);
+template <typename T> void stencil_jacobi(tp_ctx* c, int l, const T* st, const T* invD, const T* b, const T* u, T* unew, T omega, int nr = 1, int masked = -1);
+template <typename T> void stencil_resid(tp_ctx* c, int l, const T* st, const T* b, const T* u, T* d, int nr = 1, int masked = -1);
+void stencil_expand(tp_ctx* c, int l, const double* st, double* out, int masked);  // full 243-coefficient form with BCs
 
 // grid transfer
 template <typename T> void restrict_fw(tp_ctx* c, int l, const T* fine, T* coarse, int nr = 1);

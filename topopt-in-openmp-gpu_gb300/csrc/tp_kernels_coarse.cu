@@ -4,9 +4,11 @@
 // element the E(rho)-weighted stiffness of its ncell^3 fine sub-cells
 // (stencil_methods.c:436-519), and assembles levels >= 2 into CSR on the
 // host (stencil_assembly.c:126-260). Here every level >= 1 is assembled once
-// per design iteration on the GPU into a block stencil: for each node, the
-// 3x3 coupling blocks to its 27 neighbours. The operator semantics of the
-// reference are kept exactly:
+// per design iteration on the GPU into a block stencil of the symmetric
+// operator without boundary conditions, stored in half: for each node the
+// 3x3 blocks to itself and to its 13 neighbours of larger index (the other
+// 13 are the transposes of blocks the neighbours store). The operator
+// semantics of the reference are applied when the stencil is applied:
 //   level 1      : free rows couple to every neighbour, fixed rows = identity
 //                  (the matrix-free subspace operator);
 //   level >= 2   : additionally the columns of fixed DOFs are zeroed (the CSR
@@ -42,7 +44,7 @@ __device__ __forceinline__ bool is_fixed(const CGeom& g, int i, int j) {
 // ncell^3 sub-cells, then the lanes reduce by shuffles.
 template <typename T, int G>
 __global__ void assemble_kernel(CGeom g, const T* __restrict__ E, const T* __restrict__ ke,
-                                T* __restrict__ st, double* __restrict__ invD, int masked) {
+                                T* __restrict__ st, double* __restrict__ invD) {
   const long tid = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const long n = tid / G;
   const int lane = threadIdx.x % G;
@@ -54,7 +56,7 @@ __global__ void assemble_kernel(CGeom g, const T* __restrict__ E, const T* __res
   const bool nfix = is_fixed(g, i, j);
   const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) / G * G));
 
-  for (int m = 0; m < 27; m++) {
+  for (int m = 13; m < 27; m++) {  // the stored half: the node and its 13 higher neighbours
     const int mx = m / 9 - 1, mz = (m / 3) % 3 - 1, my = m % 3 - 1;
     T acc[9];
 #pragma unroll
@@ -91,15 +93,8 @@ __global__ void assemble_kernel(CGeom g, const T* __restrict__ E, const T* __res
       if (m == 13) {  // the node itself: Jacobi diagonal before BCs
         for (int c = 0; c < 3; c++) invD[3 * n + c] = nfix ? 1.0 : 1.0 / (double)acc[4 * c];
       }
-      bool zero = !minside;
-      if (nfix) zero = true;
-      if (masked && minside && is_fixed(g, mi, mj)) zero = true;
 #pragma unroll
-      for (int q = 0; q < 9; q++) {
-        T v = zero ? T(0) : acc[q];
-        if (nfix && m == 13 && (q % 4 == 0)) v = T(1);
-        st[(long)(m * 9 + q) * g.nnodes + n] = v;
-      }
+      for (int q = 0; q < 9; q++) st[(long)((m - 13) * 9 + q) * g.nnodes + n] = acc[q];
     }
   }
 }
@@ -155,7 +150,7 @@ template <typename T>
 __global__ void __launch_bounds__(256, 1) moment_stencil_kernel(CGeom g, const double* __restrict__ M, long ncoarse,
                                                              const double* __restrict__ gcoef,
                                                              const int* __restrict__ gint, int nnz,
-                                                             T* __restrict__ st, double* __restrict__ invD, int masked) {
+                                                             T* __restrict__ st, double* __restrict__ invD) {
   extern __shared__ double smg[];
   double* sc = smg;                                   // coefficients
   int* sp = reinterpret_cast<int*>(smg + nnz);        // moment indices
@@ -172,7 +167,7 @@ __global__ void __launch_bounds__(256, 1) moment_stencil_kernel(CGeom g, const d
   const int k = (n / g.ny) % g.nz;
   const int i = n / ((long)g.ny * g.nz);
   const bool nfix = is_fixed(g, i, j);
-  for (int m = 0; m < 27; m++) {
+  for (int m = 13; m < 27; m++) {  // the stored half: the node and its 13 higher neighbours
     const int mx = m / 9 - 1, mz = (m / 3) % 3 - 1, my = m % 3 - 1;
     double acc[9];
 #pragma unroll
@@ -200,20 +195,13 @@ __global__ void __launch_bounds__(256, 1) moment_stencil_kernel(CGeom g, const d
     if (m == 13) {  // the node itself: Jacobi diagonal before BCs
       for (int c = 0; c < 3; c++) invD[3 * n + c] = nfix ? 1.0 : 1.0 / acc[4 * c];
     }
-    bool zero = !minside;
-    if (nfix) zero = true;
-    if (masked && minside && is_fixed(g, mi, mj)) zero = true;
 #pragma unroll
-    for (int q = 0; q < 9; q++) {
-      T v = zero ? T(0) : (T)acc[q];
-      if (nfix && m == 13 && (q % 4 == 0)) v = T(1);
-      st[(long)(m * 9 + q) * g.nnodes + n] = v;
-    }
+    for (int q = 0; q < 9; q++) st[(long)((m - 13) * 9 + q) * g.nnodes + n] = (T)acc[q];
   }
 }
 
 template <typename T>
-void assemble_stencil(tp_ctx* c, int l, const T* E, const T* ke, T* st, double* invD, int masked) {
+void assemble_stencil(tp_ctx* c, int l, const T* E, const T* ke, T* st, double* invD) {
   ProfScope ps(c, P_ASSEMBLE);
   const CGeom g = cgeom(c, l);
   const int nsub = g.ncell * g.ncell * g.ncell;
@@ -225,29 +213,36 @@ void assemble_stencil(tp_ctx* c, int l, const T* E, const T* ke, T* st, double* 
     moments_kernel<<<grid_for(nce, 128), 128, 0, c->s>>>(g, c->d_E, c->d_mom, nce);
     cudaFuncSetAttribute(moment_stencil_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     moment_stencil_kernel<T><<<grid_for(g.nnodes, threads), threads, smem, c->s>>>(
-        g, c->d_mom, nce, c->d_mgc[l], c->d_mgi[l], nnz, st, invD, masked);
+        g, c->d_mom, nce, c->d_mgc[l], c->d_mgi[l], nnz, st, invD);
     TP_CHECK_LAUNCH(c, "assemble_stencil");
     return;
   }
   if (nsub >= 32) {
-    assemble_kernel<T, 32><<<grid_for(g.nnodes * 32, threads), threads, 0, c->s>>>(g, E, ke, st, invD, masked);
+    assemble_kernel<T, 32><<<grid_for(g.nnodes * 32, threads), threads, 0, c->s>>>(g, E, ke, st, invD);
   } else if (nsub >= 8) {
-    assemble_kernel<T, 8><<<grid_for(g.nnodes * 8, threads), threads, 0, c->s>>>(g, E, ke, st, invD, masked);
+    assemble_kernel<T, 8><<<grid_for(g.nnodes * 8, threads), threads, 0, c->s>>>(g, E, ke, st, invD);
   } else {
-    assemble_kernel<T, 1><<<grid_for(g.nnodes, threads), threads, 0, c->s>>>(g, E, ke, st, invD, masked);
+    assemble_kernel<T, 1><<<grid_for(g.nnodes, threads), threads, 0, c->s>>>(g, E, ke, st, invD);
   }
   TP_CHECK_LAUNCH(c, "assemble_stencil");
 }
-template void assemble_stencil<double>(tp_ctx*, int, const double*, const double*, double*, double*, int);
-template void assemble_stencil<float>(tp_ctx*, int, const float*, const float*, float*, double*, int);
+template void assemble_stencil<double>(tp_ctx*, int, const double*, const double*, double*, double*);
+template void assemble_stencil<float>(tp_ctx*, int, const float*, const float*, float*, double*);
 
 enum { S_APPLY = 0, S_JACOBI = 1, S_RESID = 2 };
 
-// NR right-hand sides (columns 3*nnodes apart) share each coefficient load.
+// The stencil holds the symmetric operator without boundary conditions in
+// half: for each node n its own block and the blocks to the 13 neighbours
+// with a larger node index (m = 13..26, stored as m - 13); the block to a
+// neighbour with a smaller index is the transpose of the block that
+// neighbour stores (index 13 - m). The conditions are applied here: a
+// fixed node's rows are the identity; with masked (levels >= 2) a free row
+// drops the columns of fixed neighbours. NR right-hand sides (columns
+// 3*nnodes apart) share each coefficient load.
 template <typename T, int MODE, int NR>
 __global__ void stencil_kernel(CGeom g, const T* __restrict__ st, const T* __restrict__ in,
                                T* __restrict__ out, const T* __restrict__ b,
-                               const T* __restrict__ invD, T omega) {
+                               const T* __restrict__ invD, T omega, int masked) {
   const long n = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (n >= g.nnodes) return;
   const long vs = 3 * g.nnodes;
@@ -255,23 +250,39 @@ __global__ void stencil_kernel(CGeom g, const T* __restrict__ st, const T* __res
   const int k = (n / g.ny) % g.nz;
   const int i = n / ((long)g.ny * g.nz);
   T y[NR][3];
+  if (is_fixed(g, i, j)) {
 #pragma unroll
-  for (int r = 0; r < NR; r++) y[r][0] = y[r][1] = y[r][2] = T(0);
+    for (int r = 0; r < NR; r++)
 #pragma unroll
-  for (int m = 0; m < 27; m++) {
-    const int mx = m / 9 - 1, mz = (m / 3) % 3 - 1, my = m % 3 - 1;
-    const int mi = i + mx, mk = k + mz, mj = j + my;
-    if (mi < 0 || mi >= g.nx || mk < 0 || mk >= g.nz || mj < 0 || mj >= g.ny) continue;
-    const long nm = ((long)mi * g.nz + mk) * g.ny + mj;
-    const T* A = st + (long)m * 9 * g.nnodes + n;
-    T a[9];
+      for (int c = 0; c < 3; c++) y[r][c] = in[r * vs + 3 * n + c];
+  } else {
 #pragma unroll
-    for (int q = 0; q < 9; q++) a[q] = A[q * g.nnodes];
+    for (int r = 0; r < NR; r++) y[r][0] = y[r][1] = y[r][2] = T(0);
 #pragma unroll
-    for (int r = 0; r < NR; r++) {
-      const T u0 = in[r * vs + 3 * nm], u1 = in[r * vs + 3 * nm + 1], u2 = in[r * vs + 3 * nm + 2];
+    for (int m = 0; m < 27; m++) {
+      const int mx = m / 9 - 1, mz = (m / 3) % 3 - 1, my = m % 3 - 1;
+      const int mi = i + mx, mk = k + mz, mj = j + my;
+      if (mi < 0 || mi >= g.nx || mk < 0 || mk >= g.nz || mj < 0 || mj >= g.ny) continue;
+      if (masked && m != 13 && is_fixed(g, mi, mj)) continue;
+      const long nm = ((long)mi * g.nz + mk) * g.ny + mj;
+      T a[9];
+      if (m >= 13) {
+        const T* A = st + (long)(m - 13) * 9 * g.nnodes + n;
 #pragma unroll
-      for (int c = 0; c < 3; c++) y[r][c] += a[3 * c] * u0 + a[3 * c + 1] * u1 + a[3 * c + 2] * u2;
+        for (int q = 0; q < 9; q++) a[q] = A[q * g.nnodes];
+      } else {
+        const T* A = st + (long)(13 - m) * 9 * g.nnodes + nm;
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+#pragma unroll
+          for (int d = 0; d < 3; d++) a[3 * c + d] = A[(3 * d + c) * g.nnodes];
+      }
+#pragma unroll
+      for (int r = 0; r < NR; r++) {
+        const T u0 = in[r * vs + 3 * nm], u1 = in[r * vs + 3 * nm + 1], u2 = in[r * vs + 3 * nm + 2];
+#pragma unroll
+        for (int c = 0; c < 3; c++) y[r][c] += a[3 * c] * u0 + a[3 * c + 1] * u1 + a[3 * c + 2] * u2;
+      }
     }
   }
 #pragma unroll
@@ -288,56 +299,91 @@ __global__ void stencil_kernel(CGeom g, const T* __restrict__ st, const T* __res
 // nr columns in chunks of 8, 4, 2, 1 (each chunk reads the stencil once)
 template <typename T, int MODE>
 static void stencil_launch(tp_ctx* c, int l, const T* st, const T* in, T* out, const T* b, const T* invD, T omega,
-                           int nr) {
+                           int nr, int masked) {
   const CGeom g = cgeom(c, l);
   const long vs = 3 * g.nnodes;
   const unsigned grid = grid_for(g.nnodes, 128);
+  if (masked < 0) masked = l >= 2;
   for (int r0 = 0; r0 < nr;) {
     const int left = nr - r0;
     const long o = r0 * vs;
     const T* bb = b ? b + o : nullptr;
     if (left >= 8) {
-      stencil_kernel<T, MODE, 8><<<grid, 128, 0, c->s>>>(g, st, in + o, out + o, bb, invD, omega);
+      stencil_kernel<T, MODE, 8><<<grid, 128, 0, c->s>>>(g, st, in + o, out + o, bb, invD, omega, masked);
       r0 += 8;
     } else if (left >= 4) {
-      stencil_kernel<T, MODE, 4><<<grid, 128, 0, c->s>>>(g, st, in + o, out + o, bb, invD, omega);
+      stencil_kernel<T, MODE, 4><<<grid, 128, 0, c->s>>>(g, st, in + o, out + o, bb, invD, omega, masked);
       r0 += 4;
     } else if (left >= 2) {
-      stencil_kernel<T, MODE, 2><<<grid, 128, 0, c->s>>>(g, st, in + o, out + o, bb, invD, omega);
+      stencil_kernel<T, MODE, 2><<<grid, 128, 0, c->s>>>(g, st, in + o, out + o, bb, invD, omega, masked);
       r0 += 2;
     } else {
-      stencil_kernel<T, MODE, 1><<<grid, 128, 0, c->s>>>(g, st, in + o, out + o, bb, invD, omega);
+      stencil_kernel<T, MODE, 1><<<grid, 128, 0, c->s>>>(g, st, in + o, out + o, bb, invD, omega, masked);
       r0 += 1;
     }
   }
 }
 
 template <typename T>
-void stencil_apply(tp_ctx* c, int l, const T* st, const T* in, T* out, int nr) {
+void stencil_apply(tp_ctx* c, int l, const T* st, const T* in, T* out, int nr, int masked) {
   ProfScope ps(c, P_STENCIL);
-  stencil_launch<T, S_APPLY>(c, l, st, in, out, nullptr, nullptr, T(0), nr);
+  stencil_launch<T, S_APPLY>(c, l, st, in, out, nullptr, nullptr, T(0), nr, masked);
   TP_CHECK_LAUNCH(c, "stencil_apply");
 }
 template <typename T>
-void stencil_jacobi(tp_ctx* c, int l, const T* st, const T* invD, const T* b, const T* u, T* unew, T omega, int nr) {
+void stencil_jacobi(tp_ctx* c, int l, const T* st, const T* invD, const T* b, const T* u, T* unew, T omega, int nr,
+                    int masked) {
   ProfScope ps(c, P_STENCIL);
-  stencil_launch<T, S_JACOBI>(c, l, st, u, unew, b, invD, omega, nr);
+  stencil_launch<T, S_JACOBI>(c, l, st, u, unew, b, invD, omega, nr, masked);
   TP_CHECK_LAUNCH(c, "stencil_jacobi");
 }
 template <typename T>
-void stencil_resid(tp_ctx* c, int l, const T* st, const T* b, const T* u, T* d, int nr) {
+void stencil_resid(tp_ctx* c, int l, const T* st, const T* b, const T* u, T* d, int nr, int masked) {
   ProfScope ps(c, P_STENCIL);
-  stencil_launch<T, S_RESID>(c, l, st, u, d, b, nullptr, T(0), nr);
+  stencil_launch<T, S_RESID>(c, l, st, u, d, b, nullptr, T(0), nr, masked);
   TP_CHECK_LAUNCH(c, "stencil_resid");
 }
-template void stencil_apply<double>(tp_ctx*, int, const double*, const double*, double*, int);
-template void stencil_apply<float>(tp_ctx*, int, const float*, const float*, float*, int);
+template void stencil_apply<double>(tp_ctx*, int, const double*, const double*, double*, int, int);
+template void stencil_apply<float>(tp_ctx*, int, const float*, const float*, float*, int, int);
 template void stencil_jacobi<double>(tp_ctx*, int, const double*, const double*, const double*, const double*, double*,
-                                     double, int);
+                                     double, int, int);
 template void stencil_jacobi<float>(tp_ctx*, int, const float*, const float*, const float*, const float*, float*, float,
-                                    int);
-template void stencil_resid<double>(tp_ctx*, int, const double*, const double*, const double*, double*, int);
-template void stencil_resid<float>(tp_ctx*, int, const float*, const float*, const float*, float*, int);
+                                    int, int);
+template void stencil_resid<double>(tp_ctx*, int, const double*, const double*, const double*, double*, int, int);
+template void stencil_resid<float>(tp_ctx*, int, const float*, const float*, const float*, float*, int, int);
+
+// The stencil of level l in the full 27-block form with the boundary
+// conditions applied (masked: also the columns of fixed neighbours), as the
+// reference-layout entry points hand it out: out[(m*9 + 3c + d)*nnodes + n].
+__global__ void stencil_expand_kernel(CGeom g, const double* __restrict__ st, double* __restrict__ out, int masked) {
+  const long n = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (n >= g.nnodes) return;
+  const int j = n % g.ny;
+  const int k = (n / g.ny) % g.nz;
+  const int i = n / ((long)g.ny * g.nz);
+  const bool nfix = is_fixed(g, i, j);
+  for (int m = 0; m < 27; m++) {
+    const int mx = m / 9 - 1, mz = (m / 3) % 3 - 1, my = m % 3 - 1;
+    const int mi = i + mx, mk = k + mz, mj = j + my;
+    const bool minside = mi >= 0 && mi < g.nx && mk >= 0 && mk < g.nz && mj >= 0 && mj < g.ny;
+    const bool zero = !minside || nfix || (masked && m != 13 && is_fixed(g, mi, mj));
+    const long nm = minside ? ((long)mi * g.nz + mk) * g.ny + mj : n;
+    for (int c = 0; c < 3; c++)
+      for (int d = 0; d < 3; d++) {
+        double v = 0.0;
+        if (!zero) v = m >= 13 ? st[((long)(m - 13) * 9 + 3 * c + d) * g.nnodes + n]
+                               : st[((long)(13 - m) * 9 + 3 * d + c) * g.nnodes + nm];
+        if (nfix && m == 13 && c == d) v = 1.0;
+        out[((long)m * 9 + 3 * c + d) * g.nnodes + n] = v;
+      }
+  }
+}
+
+void stencil_expand(tp_ctx* c, int l, const double* st, double* out, int masked) {
+  const CGeom g = cgeom(c, l);
+  stencil_expand_kernel<<<grid_for(g.nnodes, 128), 128, 0, c->s>>>(g, st, out, masked);
+  TP_CHECK_LAUNCH(c, "stencil_expand");
+}
 
 // ---------------------------------------------------------------------------
 // Full-weighting restriction, level l+1 <- level l (stencil_methods.c:595-688):

@@ -258,30 +258,47 @@ __global__ void stencil_kernel(CGeom g, const T* __restrict__ st, const T* __res
   } else {
 #pragma unroll
     for (int r = 0; r < NR; r++) y[r][0] = y[r][1] = y[r][2] = T(0);
+    // BATCH neighbours at a time (a whole x plane for one column): all their
+    // coefficient and vector loads are issued before the first multiply-add
+    // (a neighbour outside the grid, or a masked fixed one, reads the node's
+    // own entries and contributes zero), so that many loads are in flight
+    constexpr int BATCH = NR == 1 ? 9 : 3;
 #pragma unroll
-    for (int m = 0; m < 27; m++) {
-      const int mx = m / 9 - 1, mz = (m / 3) % 3 - 1, my = m % 3 - 1;
-      const int mi = i + mx, mk = k + mz, mj = j + my;
-      if (mi < 0 || mi >= g.nx || mk < 0 || mk >= g.nz || mj < 0 || mj >= g.ny) continue;
-      if (masked && m != 13 && is_fixed(g, mi, mj)) continue;
-      const long nm = ((long)mi * g.nz + mk) * g.ny + mj;
-      T a[9];
-      if (m >= 13) {
-        const T* A = st + (long)(m - 13) * 9 * g.nnodes + n;
+    for (int m0 = 0; m0 < 27; m0 += BATCH) {
+      T a[BATCH][9], u[BATCH][NR][3];
+      bool ok[BATCH];
 #pragma unroll
-        for (int q = 0; q < 9; q++) a[q] = A[q * g.nnodes];
-      } else {
-        const T* A = st + (long)(13 - m) * 9 * g.nnodes + nm;
+      for (int t = 0; t < BATCH; t++) {
+        const int m = m0 + t;
+        const int mx = m / 9 - 1, mz = (m / 3) % 3 - 1, my = m % 3 - 1;
+        const int mi = i + mx, mk = k + mz, mj = j + my;
+        ok[t] = mi >= 0 && mi < g.nx && mk >= 0 && mk < g.nz && mj >= 0 && mj < g.ny &&
+                !(masked && m != 13 && is_fixed(g, mi, mj));
+        const long nm = ok[t] ? ((long)mi * g.nz + mk) * g.ny + mj : n;
+        if (m >= 13) {
+          const T* A = st + (long)(m - 13) * 9 * g.nnodes + n;
 #pragma unroll
-        for (int c = 0; c < 3; c++)
+          for (int q = 0; q < 9; q++) a[t][q] = A[q * g.nnodes];
+        } else {
+          const T* A = st + (long)(13 - m) * 9 * g.nnodes + nm;
 #pragma unroll
-          for (int d = 0; d < 3; d++) a[3 * c + d] = A[(3 * d + c) * g.nnodes];
+          for (int c = 0; c < 3; c++)
+#pragma unroll
+            for (int d = 0; d < 3; d++) a[t][3 * c + d] = A[(3 * d + c) * g.nnodes];
+        }
+#pragma unroll
+        for (int r = 0; r < NR; r++)
+#pragma unroll
+          for (int d = 0; d < 3; d++) u[t][r][d] = in[r * vs + 3 * nm + d];
       }
 #pragma unroll
-      for (int r = 0; r < NR; r++) {
-        const T u0 = in[r * vs + 3 * nm], u1 = in[r * vs + 3 * nm + 1], u2 = in[r * vs + 3 * nm + 2];
+      for (int t = 0; t < BATCH; t++) {
+        if (!ok[t]) continue;
 #pragma unroll
-        for (int c = 0; c < 3; c++) y[r][c] += a[3 * c] * u0 + a[3 * c + 1] * u1 + a[3 * c + 2] * u2;
+        for (int r = 0; r < NR; r++)
+#pragma unroll
+          for (int c = 0; c < 3; c++)
+            y[r][c] += a[t][3 * c] * u[t][r][0] + a[t][3 * c + 1] * u[t][r][1] + a[t][3 * c + 2] * u[t][r][2];
       }
     }
   }

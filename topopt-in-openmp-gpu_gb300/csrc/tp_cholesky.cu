@@ -572,12 +572,12 @@ __device__ bool pf_wait(const PfArgs& a, const int* flag, int target) {
   return __syncthreads_and(ok) != 0;
 }
 
+// the CTA's stores happen before the barrier, the barrier before thread 0's
+// release store at GPU scope, which is cumulative: a CTA that acquires the
+// flag sees them all (no separate fence needed)
 __device__ __forceinline__ void pf_release(int* flag, int v) {
   __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    asm volatile("st.release.gpu.global.s32 [%0], %1;\n" ::"l"(flag), "r"(v) : "memory");
-  }
+  if (threadIdx.x == 0) asm volatile("st.release.gpu.global.s32 [%0], %1;\n" ::"l"(flag), "r"(v) : "memory");
 }
 
 // tile (I, J) into A[r][c] (TR: A[c][r]); zero outside the matrix, above the
@@ -1313,8 +1313,9 @@ __device__ __forceinline__ bool ps_barrier(unsigned* bar, int* err, unsigned tar
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    __threadfence();
-    atomicAdd(bar, 1u);
+    // arrive with a release (cumulative over the CTA's stores, which the
+    // barrier above ordered before it)
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;\n" ::"l"(bar) : "memory");
     for (long it = 0;; it++) {
       unsigned v;
       asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(bar) : "memory");

@@ -1206,9 +1206,11 @@ __global__ void bwd_diag_kernel(const double* __restrict__ DT, long n, int nbs, 
 // The same block triangular solves as ONE cooperative launch: every half step
 // of the forward and the backward sweep (Lrow product, D_k product, L^T
 // product, D_k^T product) is a phase, and the CTAs meet at a grid barrier
-// between phases instead of at a kernel boundary. CTA b owns rows
-// b*R .. b*R+R-1 of every block; each row is split into P = 8/R fixed parts,
-// one warp each, so every sum is formed in the same order on every call.
+// between phases instead of at a kernel boundary. CTA b owns R rows of every
+// block, from mirrored positions (ps_row_of), because a block row's length
+// grows or shrinks linearly with its position in every phase: each CTA then
+// has the same work. Each row is split into P = 8/R fixed parts, one warp
+// each, so every sum is formed in the same order on every call.
 // While a CTA works on phase h (and waits at the barrier after it), the
 // matrix rows of phase h+1 -- constant during the solve -- arrive in shared
 // memory by cp.async; the vectors written by other CTAs are read through L2
@@ -1216,6 +1218,28 @@ __global__ void bwd_diag_kernel(const double* __restrict__ DT, long n, int nbs, 
 // status word and every CTA leaves at its next barrier; the host reads (and
 // clears) the word after the solve and reports TP_ERR_TIMEOUT.
 constexpr int kPsWarps = 8;
+
+// Row rl (0 .. R-1) of CTA b among G: rl*G + b for even rl, rl*G + G-1-b for
+// odd rl, so the R rows of a CTA pair short with long; a bijection onto
+// 0 .. R*G-1.
+__device__ __forceinline__ int ps_row_of(int b, int rl, int G) { return rl * G + ((rl & 1) ? G - 1 - b : b); }
+
+// Warp w's row rl and part p. Warps w and w+4 share a sub-partition's FP64
+// unit; with R = 4 (P = 2) they take rows 0 and 3 (or 1 and 2), whose
+// lengths add up to the same total, so the four units carry equal work.
+__device__ __forceinline__ void ps_warp_row(int w, int R, int P, int& rl, int& p) {
+  if (R == 4) {
+    p = w & 1;
+    rl = (w < 4) ? (w >> 1) : 3 - ((w - 4) >> 1);
+  } else {
+    rl = w / P;
+    p = w % P;
+  }
+}
+__device__ __forceinline__ int ps_part_warp(int rl, int q, int R, int P) {
+  if (R == 4) return (rl < 2) ? rl * 2 + q : 4 + (3 - rl) * 2 + q;
+  return rl * P + q;
+}
 
 struct PsArgs {
   const double* lrow;
@@ -1340,8 +1364,9 @@ template <int NR>
 __global__ void __launch_bounds__(kPsWarps * 32) ps_solve_kernel(PsArgs a) {
   extern __shared__ double sm[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int rl = w / a.P, p = w % a.P;
-  const int i = blockIdx.x * a.R + rl;
+  int rl, p;
+  ps_warp_row(w, a.R, a.P, rl, p);
+  const int i = ps_row_of(blockIdx.x, rl, gridDim.x);
   auto buf = [&](int b) { return sm + (long)(b * kPsWarps + w) * a.seg; };  // stage b of this warp
   double* part = sm + 2L * kPsWarps * a.seg;  // [warp][NR]
   const int nph = 4 * a.nblk - 2;
@@ -1392,10 +1417,10 @@ __global__ void __launch_bounds__(kPsWarps * 32) ps_solve_kernel(PsArgs a) {
     if (threadIdx.x < a.R * NR) {
       const int rr = threadIdx.x / NR, v = threadIdx.x % NR;
       const long b0 = (long)k * a.nbs;
-      const long row = blockIdx.x * a.R + rr;
+      const long row = ps_row_of(blockIdx.x, rr, gridDim.x);
       if (row < lmin((long)a.nbs, a.n - b0)) {
         double sum = 0.0;
-        for (int q = 0; q < a.P; q++) sum += part[(rr * a.P + q) * NR + v];
+        for (int q = 0; q < a.P; q++) sum += part[ps_part_warp(rr, q, a.R, a.P) * NR + v];
         const long o = v * a.n + b0 + row;
         if (kind == PH_FA)
           a.t[o] = a.rhs[o] - sum;

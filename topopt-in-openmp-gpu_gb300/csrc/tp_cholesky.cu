@@ -860,7 +860,7 @@ __global__ void __launch_bounds__(kDinvThreads)
   extern __shared__ double smem[];
   double* X = smem;                    // nbs x 33
   double* Lt = X + (long)nbs * 33;     // 32 x 33
-  double* Acc = Lt + 32 * 33;          // 32 x 33
+  double* Acc = Lt + 32 * 33;          // the chunk's 32 reciprocal pivots
   const int blk = blockIdx.y, cc = blockIdx.x, tid = threadIdx.x;
   const long b0 = (long)blk * nbs;
   const int s = (int)lmin((long)nbs, n - b0);
@@ -889,21 +889,33 @@ __global__ void __launch_bounds__(kDinvThreads)
       }
       __syncthreads();
     }
-#pragma unroll
-    for (int q = 0; q < 4; q++) Acc[a * 33 + q0 + q] = acc[q];
     for (int idx = tid; idx < 1024; idx += kDinvThreads) {
       const int ra = idx & 31, cs = idx >> 5;
       const long r = b0 + R * 32 + ra, col = b0 + R * 32 + cs;
       Lt[ra * 33 + cs] = (R * 32 + ra < s && R * 32 + cs < s && ra >= cs) ? bget(B, bw, r, col) : 0.0;
     }
     __syncthreads();
-    if (tid < 32) {
-      const int col = tid;
-      for (int ra = 0; ra < 32; ra++) {
-        double v = Acc[ra * 33 + col];
-        for (int t = 0; t < ra; t++) v -= Lt[ra * 33 + t] * X[(long)(R * 32 + t) * 33 + col];
-        const double d = Lt[ra * 33 + ra];
-        X[(long)(R * 32 + ra) * 33 + col] = (R * 32 + ra < s && d != 0.0) ? v / d : 0.0;
+    if (tid < 32) {  // reciprocal pivots of the chunk (rows past s give zero rows of X)
+      const double d = Lt[tid * 33 + tid];
+      Acc[tid] = (R * 32 + tid < s && d != 0.0) ? 1.0 / d : 0.0;
+    }
+    __syncthreads();
+    // X_R = L_RR^{-1} acc, right-looking over all warps: row t is finished
+    // by its 8 threads, then every row below subtracts L(a,t) X(t,:)
+    for (int t = 0; t < 32; t++) {
+      if (a == t) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          acc[q] *= Acc[t];
+          X[(long)(R * 32 + t) * 33 + q0 + q] = acc[q];
+        }
+      }
+      __syncthreads();
+      if (a > t) {
+        const double l = Lt[a * 33 + t];
+        const double* xr = X + (long)(R * 32 + t) * 33 + q0;
+#pragma unroll
+        for (int q = 0; q < 4; q++) acc[q] -= l * xr[q];
       }
     }
     __syncthreads();

@@ -240,7 +240,8 @@ enum { S_APPLY = 0, S_JACOBI = 1, S_RESID = 2 };
 // drops the columns of fixed neighbours. NR right-hand sides (columns
 // 3*nnodes apart) share each coefficient load.
 template <typename T, int MODE, int NR>
-__global__ void stencil_kernel(CGeom g, const T* __restrict__ st, const T* __restrict__ in,
+__global__ void __launch_bounds__(128, (NR == 1 && sizeof(T) == 4) ? 4 : 1)
+    stencil_kernel(CGeom g, const T* __restrict__ st, const T* __restrict__ in,
                                T* __restrict__ out, const T* __restrict__ b,
                                const T* __restrict__ invD, T omega, int masked) {
   const long n = blockIdx.x * (long)blockDim.x + threadIdx.x;

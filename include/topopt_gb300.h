@@ -168,6 +168,13 @@ tp_status tp_set_cg(tp_ctx* c, double cgtol, int cgmax, int nswp, double omega);
  * applies (nely <= 256, 16-byte aligned vectors), else the node-centric
  * stencil; variant 1 = the node-centric stencil everywhere. */
 tp_status tp_set_fine_variant(tp_ctx* c, int variant);
+/* Arithmetic of the element-centric level-0 kernel on double vectors (no
+ * counterpart in the reference): 0 = FP64; 1 = double-single, pairs of FP32
+ * numbers with about 48 significant bits, each addition's error bounded by
+ * ~2^-46 (|a| + |b|) instead of 2^-53 (|a| + |b|). The vectors stay FP64 in
+ * memory. The default is 1 for TP_MIXED (its CG matvec and residual) and 0
+ * for TP_FP64. */
+tp_status tp_set_fine_arith(tp_ctx* c, int arith);
 /* Coarsest-level direct solver selection (no counterpart in the reference,
  * whose coarse factor and solve are CHOLMOD's, stencil_assembly.c:435-484):
  * variant 0 = the band Cholesky as one cooperative launch (a chain CTA
@@ -190,7 +197,8 @@ tp_status tp_fault_coarse_barrier(tp_ctx* c, long spin, int missing);
  * chunks) for each precision and fused mode on the context's grid and keeps
  * the fastest. It overwrites the solver work vectors (not F, U, x, xPhys):
  * call it before a solve, not inside one. ms_out (optional, 8 entries)
- * receives the best time per (precision, mode). */
+ * receives the best time per (precision, mode): FP32 modes 0-3, then the
+ * double-vector modes 4-7 in the arithmetic tp_set_fine_arith selected. */
 tp_status tp_autotune(tp_ctx* c, double* ms_out);
 /* Multi-load problem generator (no counterpart in the reference, whose one
  * load is built at stencil_optimization.c:41-95): fills F_host (ncase columns

@@ -72,6 +72,13 @@ tp_status tp_set_fine_variant(tp_ctx* c, int variant) {
   return TP_OK;
 }
 
+tp_status tp_set_fine_arith(tp_ctx* c, int arith) {
+  if (!c || arith < 0 || arith > 1) return TP_ERR_ARG;
+  c->fine_ds = arith;
+  graph_free(c);
+  return TP_OK;
+}
+
 tp_status tp_set_coarse_solve_variant(tp_ctx* c, int variant) {
   if (!c || variant < 0 || variant > 1) return TP_ERR_ARG;
   Coarse& C = c->coarse;

@@ -182,8 +182,11 @@ struct tp_ctx {
   // level-0 kernel selection: 0 element-centric where it applies, 1 the
   // node-centric stencil everywhere; plans per precision and fused mode
   int fine_variant = 0;
+  // element-centric operator on double vectors evaluated in double-single
+  // (pairs of floats) instead of FP64; plans of its own
+  int fine_ds = 0;
   bool ec_ok = false;        // KZ built and its sparsity pattern verified
-  tp::EcPlan ec_f32[4], ec_f64[4];
+  tp::EcPlan ec_f32[4], ec_f64[4], ec_ds[4];
 
   bool assembled = false;    // operators built for the current xPhys
   long mem_bytes = 0;

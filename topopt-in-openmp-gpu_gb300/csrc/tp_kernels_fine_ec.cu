@@ -28,6 +28,7 @@
 // are computed twice.
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 
 #include "tp_internal.h"
 
@@ -35,6 +36,89 @@ namespace tp {
 
 __constant__ double c_kz[45];
 __constant__ float c_kzf[45];
+__constant__ float c_kzd[45][2];  // c_kz as double-single pairs
+
+// ---------------------------------------------------------------------------
+// Double-single arithmetic: a value is h + l, two FP32 numbers with
+// |l| <= ulp(h), about 48 significant bits (Dekker, "A floating-point
+// technique for extending the available precision", 1971; the sum's error
+// term is Knuth's two-sum). The FP64 pipe of this part issues one warp
+// instruction per ~67 cycles per SM sub-partition, the FP32 pipe one per
+// cycle, so an FP64 operand in memory can be worked on as a pair of floats
+// for a fraction of the FP64 time. The additions are the "sloppy" form: the
+// error of a + b is at most ~2^-46 (|a| + |b|), a bound relative to the
+// operands rather than to the result, which is the bound a sum of element
+// contributions needs (an FP64 evaluation of it has the same form with 2^-53).
+// The _rn intrinsics keep the compiler from contracting the error terms.
+struct Dsf {
+  float h, l;
+  Dsf() = default;
+  __device__ __forceinline__ Dsf(float v) : h(v), l(0.f) {}
+  __device__ __forceinline__ Dsf(float a, float b) : h(a), l(b) {}
+};
+// s + e renormalised, exact when |s| >= |e|
+__device__ __forceinline__ Dsf ds_quick(float s, float e) {
+  const float r = __fadd_rn(s, e);
+  return Dsf(r, __fsub_rn(e, __fsub_rn(r, s)));
+}
+__device__ __forceinline__ Dsf operator+(Dsf a, Dsf b) {
+  const float s = __fadd_rn(a.h, b.h);
+  const float bb = __fsub_rn(s, a.h);
+  const float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));  // a.h + b.h - s, exactly
+  return ds_quick(s, __fadd_rn(e, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ Dsf operator-(Dsf a) { return Dsf(-a.h, -a.l); }
+__device__ __forceinline__ Dsf operator-(Dsf a, Dsf b) { return a + (-b); }
+__device__ __forceinline__ Dsf operator*(Dsf a, Dsf b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);  // the rounding error of p, exactly
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return ds_quick(p, e);
+}
+__device__ __forceinline__ Dsf& operator+=(Dsf& a, Dsf b) { return a = a + b; }
+__device__ __forceinline__ Dsf& operator-=(Dsf& a, Dsf b) { return a = a - b; }
+
+// double -> double-single with integer operations only (the FP64 pipe stays
+// free): h keeps the sign, the exponent and the leading 23 stored mantissa
+// bits (truncated), l the remaining 29 bits rounded to 24. Magnitudes below
+// FP32's normal range become 0, magnitudes above it infinity, NaN stays NaN.
+__device__ __forceinline__ Dsf ds_from(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
+  const unsigned sg = hw & 0x80000000u;
+  const int e = (int)((hw >> 20) & 0x7ffu);  // biased by 1023
+  if (e < 897) return Dsf(0.f);              // |v| < 2^-126
+  if (e > 1150) {                            // |v| >= 2^128, inf, NaN
+    const bool nan = e == 2047 && ((hw & 0xfffffu) | lw) != 0u;
+    return Dsf(__uint_as_float(nan ? 0x7fc00000u : (sg | 0x7f800000u)));
+  }
+  const float h = __uint_as_float(sg | ((unsigned)(e - 896) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
+  // the low 29 mantissa bits carry weight 2^(e - 1023 - 52)
+  const float sc = e >= 949 ? __uint_as_float((unsigned)(e - 948) << 23) : 0.f;
+  const float l = __fmul_rn(__int2float_rn((int)(lw & 0x1fffffffu)), sc);
+  return Dsf(h, sg ? -l : l);
+}
+__device__ __forceinline__ double ds_to(Dsf a) { return (double)a.h + (double)a.l; }
+
+// storage type T <-> arithmetic type A of the element-centric kernel
+template <typename A, typename T>
+struct EcCvt {
+  static __device__ __forceinline__ A in(T v) { return v; }
+  static __device__ __forceinline__ T out(A v) { return v; }
+};
+template <>
+struct EcCvt<Dsf, double> {
+  static __device__ __forceinline__ Dsf in(double v) { return ds_from(v); }
+  static __device__ __forceinline__ double out(Dsf v) { return ds_to(v); }
+};
+template <typename A>
+__device__ __forceinline__ A ec_shfl_down(A v, int d) {
+  return __shfl_down_sync(0xffffffffu, v, d);
+}
+__device__ __forceinline__ Dsf ec_shfl_down(Dsf v, int d) {
+  return Dsf(__shfl_down_sync(0xffffffffu, v.h, d), __shfl_down_sync(0xffffffffu, v.l, d));
+}
 
 template <typename T>
 __device__ __forceinline__ T kz(int i);
@@ -42,6 +126,8 @@ template <>
 __device__ __forceinline__ double kz<double>(int i) { return c_kz[i]; }
 template <>
 __device__ __forceinline__ float kz<float>(int i) { return c_kzf[i]; }
+template <>
+__device__ __forceinline__ Dsf kz<Dsf>(int i) { return Dsf(c_kzd[i][0], c_kzd[i][1]); }
 
 // (row, column) of the 45 non-zeros of KZ, row = 3*b + c, in the order the
 // kernel consumes them
@@ -77,11 +163,13 @@ bool set_fine_kz(const double* ke0, double* kz_out) {
         }
   bool in_pat[24][24] = {};
   double v[45];
-  float vf[45];
+  float vf[45], vd[45][2];
   for (int i = 0; i < 45; i++) {
     in_pat[kKzPattern[i][0]][kKzPattern[i][1]] = true;
     v[i] = KZ[kKzPattern[i][0]][kKzPattern[i][1]];
     vf[i] = (float)v[i];
+    vd[i][0] = vf[i];
+    vd[i][1] = (float)(v[i] - (double)vf[i]);
   }
   bool ok = mx > 0.0;
   for (int r = 0; r < 24; r++)
@@ -92,6 +180,7 @@ bool set_fine_kz(const double* ke0, double* kz_out) {
   if (ok) {
     cudaMemcpyToSymbol(c_kz, v, sizeof(v));
     cudaMemcpyToSymbol(c_kzf, vf, sizeof(vf));
+    cudaMemcpyToSymbol(c_kzd, vd, sizeof(vd));
   }
   return ok;
 }
@@ -137,7 +226,9 @@ __device__ __forceinline__ void ec_rows(const EcGeom& g, int gi, int& k0, int& k
 
 constexpr int EC_APPLY = FM_APPLY, EC_APPLY_DOT = FM_APPLY_DOT, EC_JACOBI = FM_JACOBI, EC_RESID = FM_RESID;
 
-template <typename T, int MODE, int RMAX>
+// T: the type of the vectors in memory; A: the type the operator is evaluated
+// in (T itself, or Dsf for double vectors)
+template <typename T, typename A, int MODE, int RMAX>
 __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restrict__ E, const T* __restrict__ in,
                                                       T* __restrict__ out, const T* __restrict__ bv,
                                                       const T* __restrict__ invD, T omega,
@@ -146,6 +237,8 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
   // the items of the columns shared by warps, (ey/32 + 1) * rows * 3, fit one
   // per thread of a group when 3 * RMAX <= 16
   static_assert(3 * RMAX <= 16, "one shared-column item per thread");
+  static_assert(sizeof(A) == sizeof(T), "shared-memory exchange arrays are sized for T");
+  using Cv = EcCvt<A, T>;
   constexpr bool HASB = (MODE == EC_JACOBI || MODE == EC_RESID);
   constexpr bool HASD = (MODE == EC_JACOBI);
   extern __shared__ __align__(16) unsigned char smem[];
@@ -182,9 +275,9 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
   unsigned char* sl = smem;
   unsigned char* sb = sl + NST * g.slab_bytes;
   unsigned char* sd = sb + 2 * g.own_bytes;
-  T* bnd_nb = reinterpret_cast<T*>(sd + 2 * g.own_bytes);  // [nzg][nwy][RMAX][6]
-  T* bnd_own = bnd_nb + nzg * nwy * RMAX * 6;              // [nzg][nwy][RMAX][6]
-  T* carry_b = bnd_own + nzg * nwy * RMAX * 6;             // [nzg][nwy + 1][RMAX][3]
+  A* bnd_nb = reinterpret_cast<A*>(sd + 2 * g.own_bytes);  // [nzg][nwy][RMAX][6]
+  A* bnd_own = bnd_nb + nzg * nwy * RMAX * 6;              // [nzg][nwy][RMAX][6]
+  A* carry_b = bnd_own + nzg * nwy * RMAX * 6;             // [nzg][nwy + 1][RMAX][3]
 
   auto slab_src = [&](int p) { return in + ((long)p * nz + kmin) * row3; };
   auto own_src = [&](const T* v, int p) { return v + ((long)p * nz + K0) * row3; };
@@ -196,11 +289,11 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
   // views: value of node row kr, column j, component c at [(kr - base row) * row3 + 3 j + c]
   auto slab_at = [&](int p) { return ec_view<T>(sl + (p % NST) * g.slab_bytes, slab_src(p)); };
 
-  for (int q = tid; q < nzg * (nwy + 1) * RMAX * 3; q += nthr) carry_b[q] = T(0);
+  for (int q = tid; q < nzg * (nwy + 1) * RMAX * 3; q += nthr) carry_b[q] = A(0);
 
   double dot = 0.0;
   // output components [c0, c1) of plane P, node row kr, column j
-  auto epi = [&](const T* uP, const T* bP, const T* dP, int P, int kr, int j, int c0, int c1, const T* y) {
+  auto epi = [&](const T* uP, const T* bP, const T* dP, int P, int kr, int j, int c0, int c1, const A* y) {
     if (P < i0) return;
     const long li = (long)(kr - kmin) * row3 + 3 * j;
     const long n3 = ((long)P * nz + kr) * row3 + 3 * j;
@@ -210,7 +303,7 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
     for (int c = 0; c < 3; c++) {
       if (c < c0 || c >= c1) continue;
       const T u = uP[li + c];
-      const T yc = fixed ? u : y[c];
+      const T yc = fixed ? u : Cv::out(y[c]);
       if (MODE == EC_APPLY || MODE == EC_APPLY_DOT) out[n3 + c] = yc;
       if (MODE == EC_APPLY_DOT) dot += (double)u * (double)yc;
       if (HASB) {
@@ -238,18 +331,18 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
   issue_own(Ls);
   cp_async_commit();
 
-  T carry[RMAX][3];
+  A carry[RMAX][3];
 #pragma unroll
-  for (int r = 0; r < RMAX; r++) carry[r][0] = carry[r][1] = carry[r][2] = T(0);
+  for (int r = 0; r < RMAX; r++) carry[r][0] = carry[r][1] = carry[r][2] = A(0);
   const bool lact = gact && t < ey;
 
   for (int L = Ls; L < Le; ++L) {
-    T Ev[RMAX + 1];
+    A Ev[RMAX + 1];
     const T* EL = E + ((long)L * ez + (k0 - 1)) * ey + t;
 #pragma unroll
     for (int q = 0; q <= RMAX; q++) {
       const int ek = k0 - 1 + q;
-      Ev[q] = (lact && q <= nrow && ek >= 0 && ek < ez) ? EL[(long)q * ey] : T(0);
+      Ev[q] = (lact && q <= nrow && ek >= 0 && ek < ez) ? Cv::in(EL[(long)q * ey]) : A(0);
     }
     if (L + 2 <= Le) issue_slab(L + 2);
     if (L + 1 <= Le) issue_own(L + 1);
@@ -263,13 +356,14 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
 
     if (gact) {
       // y and x butterflies of node row kr: X[(bx*2 + by)*3 + c]
-      auto xrow = [&](int kr, T* X) {
+      auto xrow = [&](int kr, A* X) {
         if (lact && kr >= 0 && kr < nz) {
           const long o = (long)(kr - kmin) * row3 + 3 * t;
 #pragma unroll
           for (int c = 0; c < 3; c++) {
-            const T a0 = u0[o + c], a1 = u0[o + 3 + c], b0 = u1[o + c], b1 = u1[o + 3 + c];
-            const T s0 = a0 + a1, d0 = a1 - a0, s1 = b0 + b1, d1 = b1 - b0;
+            const A a0 = Cv::in(u0[o + c]), a1 = Cv::in(u0[o + 3 + c]);
+            const A b0 = Cv::in(u1[o + c]), b1 = Cv::in(u1[o + 3 + c]);
+            const A s0 = a0 + a1, d0 = a1 - a0, s1 = b0 + b1, d1 = b1 - b0;
             X[c] = s0 + s1;
             X[3 + c] = d0 + d1;
             X[6 + c] = s1 - s0;
@@ -277,21 +371,21 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
           }
         } else {
 #pragma unroll
-          for (int a = 0; a < 12; a++) X[a] = T(0);
+          for (int a = 0; a < 12; a++) X[a] = A(0);
         }
       };
-      T Xp[12], Xn[12], accp[12], accn[12];
+      A Xp[12], Xn[12], accp[12], accn[12];
       xrow(k0 - 1, Xp);
 #pragma unroll
-      for (int a = 0; a < 12; a++) accp[a] = T(0);
+      for (int a = 0; a < 12; a++) accp[a] = A(0);
 #pragma unroll
       for (int q = 0; q <= RMAX; q++) {
         if (q > nrow) break;
         const int ek = k0 - 1 + q;
         xrow(ek + 1, Xn);
         if (ek >= 0 && ek < ez) {
-          const T Ee = Ev[q];
-          T Z[24];
+          const A Ee = Ev[q];
+          A Z[24];
 #pragma unroll
           for (int a = 0; a < 4; a++)
 #pragma unroll
@@ -303,96 +397,96 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
           // w = KZ Z, pairs (bz = 0, 1) of each (bx, by, c); node row ek takes
           // E (w0 - w1), node row ek + 1 takes E (w0 + w1)
           {
-            const T w1 = kz<T>(0) * Z[3] + kz<T>(1) * Z[14];
+            const A w1 = kz<A>(0) * Z[3] + kz<A>(1) * Z[14];
             accp[0] -= Ee * w1;
             accn[0] = Ee * w1;
           }
           {
-            const T w1 = kz<T>(2) * Z[4] + kz<T>(3) * Z[8];
+            const A w1 = kz<A>(2) * Z[4] + kz<A>(3) * Z[8];
             accp[1] -= Ee * w1;
             accn[1] = Ee * w1;
           }
           {
-            const T w1 = kz<T>(4) * Z[5] + kz<T>(5) * Z[7] + kz<T>(6) * Z[12];
+            const A w1 = kz<A>(4) * Z[5] + kz<A>(5) * Z[7] + kz<A>(6) * Z[12];
             accp[2] -= Ee * w1;
             accn[2] = Ee * w1;
           }
           {
-            const T w0 = kz<T>(7) * Z[6] + kz<T>(8) * Z[13];
-            const T w1 = kz<T>(9) * Z[9] + kz<T>(10) * Z[16] + kz<T>(11) * Z[20];
+            const A w0 = kz<A>(7) * Z[6] + kz<A>(8) * Z[13];
+            const A w1 = kz<A>(9) * Z[9] + kz<A>(10) * Z[16] + kz<A>(11) * Z[20];
             accp[3] += Ee * (w0 - w1);
             accn[3] = Ee * (w0 + w1);
           }
           {
-            const T w0 = kz<T>(12) * Z[5] + kz<T>(13) * Z[7] + kz<T>(14) * Z[12];
-            const T w1 = kz<T>(15) * Z[10] + kz<T>(16) * Z[15];
+            const A w0 = kz<A>(12) * Z[5] + kz<A>(13) * Z[7] + kz<A>(14) * Z[12];
+            const A w1 = kz<A>(15) * Z[10] + kz<A>(16) * Z[15];
             accp[4] += Ee * (w0 - w1);
             accn[4] = Ee * (w0 + w1);
           }
           {
-            const T w0 = kz<T>(17) * Z[4] + kz<T>(18) * Z[8];
-            const T w1 = kz<T>(19) * Z[11] + kz<T>(20) * Z[18];
+            const A w0 = kz<A>(17) * Z[4] + kz<A>(18) * Z[8];
+            const A w1 = kz<A>(19) * Z[11] + kz<A>(20) * Z[18];
             accp[5] += Ee * (w0 - w1);
             accn[5] = Ee * (w0 + w1);
           }
           {
-            const T w0 = kz<T>(21) * Z[5] + kz<T>(22) * Z[7] + kz<T>(23) * Z[12];
-            const T w1 = kz<T>(24) * Z[10] + kz<T>(25) * Z[15];
+            const A w0 = kz<A>(21) * Z[5] + kz<A>(22) * Z[7] + kz<A>(23) * Z[12];
+            const A w1 = kz<A>(24) * Z[10] + kz<A>(25) * Z[15];
             accp[6] += Ee * (w0 - w1);
             accn[6] = Ee * (w0 + w1);
           }
           {
-            const T w0 = kz<T>(26) * Z[6] + kz<T>(27) * Z[13];
-            const T w1 = kz<T>(28) * Z[9] + kz<T>(29) * Z[16] + kz<T>(30) * Z[20];
+            const A w0 = kz<A>(26) * Z[6] + kz<A>(27) * Z[13];
+            const A w1 = kz<A>(28) * Z[9] + kz<A>(29) * Z[16] + kz<A>(30) * Z[20];
             accp[7] += Ee * (w0 - w1);
             accn[7] = Ee * (w0 + w1);
           }
           {
-            const T w0 = kz<T>(31) * Z[3] + kz<T>(32) * Z[14];
-            const T w1 = kz<T>(33) * Z[17] + kz<T>(34) * Z[19];
+            const A w0 = kz<A>(31) * Z[3] + kz<A>(32) * Z[14];
+            const A w1 = kz<A>(33) * Z[17] + kz<A>(34) * Z[19];
             accp[8] += Ee * (w0 - w1);
             accn[8] = Ee * (w0 + w1);
           }
           {
-            const T w0 = kz<T>(35) * Z[11] + kz<T>(36) * Z[18];
-            const T w1 = kz<T>(37) * Z[21];
+            const A w0 = kz<A>(35) * Z[11] + kz<A>(36) * Z[18];
+            const A w1 = kz<A>(37) * Z[21];
             accp[9] += Ee * (w0 - w1);
             accn[9] = Ee * (w0 + w1);
           }
           {
-            const T w0 = kz<T>(38) * Z[17] + kz<T>(39) * Z[19];
-            const T w1 = kz<T>(40) * Z[22];
+            const A w0 = kz<A>(38) * Z[17] + kz<A>(39) * Z[19];
+            const A w1 = kz<A>(40) * Z[22];
             accp[10] += Ee * (w0 - w1);
             accn[10] = Ee * (w0 + w1);
           }
           {
-            const T w0 = kz<T>(41) * Z[9] + kz<T>(42) * Z[16] + kz<T>(43) * Z[20];
-            const T w1 = kz<T>(44) * Z[23];
+            const A w0 = kz<A>(41) * Z[9] + kz<A>(42) * Z[16] + kz<A>(43) * Z[20];
+            const A w1 = kz<A>(44) * Z[23];
             accp[11] += Ee * (w0 - w1);
             accn[11] = Ee * (w0 + w1);
           }
         } else {
 #pragma unroll
-          for (int a = 0; a < 12; a++) accn[a] = T(0);
+          for (int a = 0; a < 12; a++) accn[a] = A(0);
         }
         if (q >= 1) {
           // node row ek = k0 + r is complete: x and y butterflies back
           const int r = q - 1;
-          T own0[3], own1[3], nb0[3], nb1[3];
+          A own0[3], own1[3], nb0[3], nb1[3];
 #pragma unroll
           for (int c = 0; c < 3; c++) {
-            const T p0s = accp[c] - accp[6 + c], p0d = accp[3 + c] - accp[9 + c];
-            const T p1s = accp[c] + accp[6 + c], p1d = accp[3 + c] + accp[9 + c];
+            const A p0s = accp[c] - accp[6 + c], p0d = accp[3 + c] - accp[9 + c];
+            const A p1s = accp[c] + accp[6 + c], p1d = accp[3 + c] + accp[9 + c];
             own0[c] = p0s + p0d;  // plane L,   column t + 1
             own1[c] = p1s + p1d;  // plane L+1, column t + 1
             nb0[c] = p0s - p0d;   // plane L,   column t
             nb1[c] = p1s - p1d;   // plane L+1, column t
           }
-          T rv0[3], rv1[3];
+          A rv0[3], rv1[3];
 #pragma unroll
           for (int c = 0; c < 3; c++) {
-            rv0[c] = __shfl_down_sync(0xffffffffu, nb0[c], 1);
-            rv1[c] = __shfl_down_sync(0xffffffffu, nb1[c], 1);
+            rv0[c] = ec_shfl_down(nb0[c], 1);
+            rv1[c] = ec_shfl_down(nb1[c], 1);
           }
           const int bo = ((tz * nwy + wy) * RMAX + r) * 6;
           if (lane == 0) {
@@ -409,7 +503,7 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
               bnd_own[bo + 3 + c] = own1[c];
             }
           } else if (lact) {
-            T y[3];
+            A y[3];
 #pragma unroll
             for (int c = 0; c < 3; c++) {
               y[c] = carry[r][c] + own0[c] + rv0[c];
@@ -430,7 +524,7 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
     // left plus the share of lane 0 of the warp on the right
     if (tail) {
       const int j = 32 * tcb;
-      T o0 = T(0), o1 = T(0), n0 = T(0), n1 = T(0);
+      A o0 = A(0), o1 = A(0), n0 = A(0), n1 = A(0);
       if (tcb >= 1) {
         const int bo = ((tz * nwy + tcb - 1) * RMAX + tr) * 6;
         o0 = bnd_own[bo + tc];
@@ -441,10 +535,10 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
         n0 = bnd_nb[bo + tc];
         n1 = bnd_nb[bo + 3 + tc];
       }
-      T& cr = carry_b[((tz * (nwy + 1) + tcb) * RMAX + tr) * 3 + tc];
-      const T v = cr + o0 + n0;
+      A& cr = carry_b[((tz * (nwy + 1) + tcb) * RMAX + tr) * 3 + tc];
+      const A v = cr + o0 + n0;
       cr = o1 + n1;
-      const T y[3] = {v, v, v};  // only component tc is stored
+      const A y[3] = {v, v, v};  // only component tc is stored
       epi(u0, bL, dL, L, k0 + tr, j, tc, tc + 1, y);
     }
     __syncthreads();
@@ -463,8 +557,8 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
         if (r < nrow) epi(uP, bP, dP, P, k0 + r, t + 1, 0, 3, carry[r]);
     }
     if (tail) {
-      const T v = carry_b[((tz * (nwy + 1) + tcb) * RMAX + tr) * 3 + tc];
-      const T y[3] = {v, v, v};
+      const A v = carry_b[((tz * (nwy + 1) + tcb) * RMAX + tr) * 3 + tc];
+      const A y[3] = {v, v, v};
       epi(uP, bP, dP, P, k0 + tr, 32 * tcb, tc, tc + 1, y);
     }
   }
@@ -528,6 +622,7 @@ void ec_default_plans(tp_ctx* c) {
     ec_plan(c, nzg, (want + zctas - 1) / zctas, &p);
     for (int m = 0; m < 4; m++) (prec == 0 ? c->ec_f32 : c->ec_f64)[m] = p;
   }
+  for (int m = 0; m < 4; m++) c->ec_ds[m] = c->ec_f64[m];
 }
 
 static EcGeom ec_geom(const tp_ctx* c, const EcPlan& p, size_t tsize, bool own, long vstride) {
@@ -558,13 +653,13 @@ static size_t ec_smem(const EcGeom& g, const EcPlan& p, size_t tsize) {
          tsize * (size_t)(2 * p.nzg * nwy * kEcRmax * 6 + p.nzg * (nwy + 1) * kEcRmax * 3);
 }
 
-template <typename T, int MODE>
-static int ec_launch(tp_ctx* c, const EcPlan& p, const T* E, const T* in, T* out, const T* b, const T* invD,
-                     T omega, int nrhs, long vstride) {
+template <typename T, typename A, int MODE>
+static int ec_launch_as(tp_ctx* c, const EcPlan& p, const T* E, const T* in, T* out, const T* b, const T* invD,
+                        T omega, int nrhs, long vstride) {
   const bool own = (MODE == EC_JACOBI || MODE == EC_RESID) && p.own;
   const EcGeom g = ec_geom(c, p, sizeof(T), own, vstride);
   const size_t smem = ec_smem(g, p, sizeof(T));
-  auto kern = fine_ec_kernel<T, MODE, kEcRmax>;
+  auto kern = fine_ec_kernel<T, A, MODE, kEcRmax>;
   static size_t set_for = 0;  // largest size the attribute was raised to
   if (smem > 48 * 1024 && smem > set_for) {
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
@@ -580,9 +675,18 @@ static int ec_launch(tp_ctx* c, const EcPlan& p, const T* E, const T* in, T* out
   return (int)(grid.x * grid.y);  // partials per right-hand side
 }
 
+// double vectors are worked on in double-single when the context asks for it
+template <typename T, int MODE>
+static int ec_launch(tp_ctx* c, const EcPlan& p, const T* E, const T* in, T* out, const T* b, const T* invD,
+                     T omega, int nrhs, long vstride) {
+  if constexpr (std::is_same<T, double>::value)
+    if (c->fine_ds) return ec_launch_as<T, Dsf, MODE>(c, p, E, in, out, b, invD, omega, nrhs, vstride);
+  return ec_launch_as<T, T, MODE>(c, p, E, in, out, b, invD, omega, nrhs, vstride);
+}
+
 template <typename T>
 const EcPlan& ec_plan_for(const tp_ctx* c, int mode) {
-  return sizeof(T) == 8 ? c->ec_f64[mode] : c->ec_f32[mode];
+  return sizeof(T) == 8 ? (c->fine_ds ? c->ec_ds[mode] : c->ec_f64[mode]) : c->ec_f32[mode];
 }
 
 static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
@@ -689,7 +793,9 @@ extern "C" tp_status tp_autotune(tp_ctx* c, double* ms_out) {
   graph_free(c);  // a captured CG loop keeps the launch shapes it was recorded with
   int sms = 148;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-  ec_tune<double>(c, c->ec_f64, c->d_E, c->d_p, c->d_q, c->d_r, c->invD[0], sms, ms_out ? ms_out + 4 : nullptr);
+  // the double-vector plans of the arithmetic in use (FP64 or double-single)
+  ec_tune<double>(c, c->fine_ds ? c->ec_ds : c->ec_f64, c->d_E, c->d_p, c->d_q, c->d_r, c->invD[0], sms,
+                  ms_out ? ms_out + 4 : nullptr);
   if (c->mgf_r[0] && c->invDf[0])
     ec_tune<float>(c, c->ec_f32, c->d_Ef, c->mgf_z[0], c->mgf_t[0], c->mgf_r[0], c->invDf[0], sms, ms_out);
   cudaError_t e = cudaStreamSynchronize(c->s);

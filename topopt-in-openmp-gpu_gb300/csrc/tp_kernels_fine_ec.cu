@@ -39,16 +39,21 @@ __constant__ float c_kzf[45];
 __constant__ float c_kzd[45][2];  // c_kz as double-single pairs
 
 // ---------------------------------------------------------------------------
-// Double-single arithmetic: a value is h + l, two FP32 numbers with
-// |l| <= ulp(h), about 48 significant bits (Dekker, "A floating-point
-// technique for extending the available precision", 1971; the sum's error
-// term is Knuth's two-sum). The FP64 pipe of this part issues one warp
-// instruction per ~67 cycles per SM sub-partition, the FP32 pipe one per
-// cycle, so an FP64 operand in memory can be worked on as a pair of floats
-// for a fraction of the FP64 time. The additions are the "sloppy" form: the
-// error of a + b is at most ~2^-46 (|a| + |b|), a bound relative to the
-// operands rather than to the result, which is the bound a sum of element
-// contributions needs (an FP64 evaluation of it has the same form with 2^-53).
+// Double-single arithmetic: a value is the unevaluated sum h + l of two FP32
+// numbers (Dekker, "A floating-point technique for extending the available
+// precision", 1971; the sum's error term is Knuth's two-sum). The FP64 pipe of
+// this part issues one warp instruction per ~67 cycles per SM sub-partition,
+// the FP32 pipe one per cycle, so an FP64 operand in memory can be worked on
+// as a pair of floats for a fraction of the FP64 time.
+// The sum of element contributions needs each operation's error bounded
+// relative to its operands, as an FP64 evaluation bounds it by 2^-53
+// (|a| + |b|), not relative to its result. Here: a + b takes the exact
+// two-sum of the high parts and adds the low parts and the two-sum's error
+// in FP32; a * b takes the exact product of the high parts (an FMA gives its
+// error) plus the cross terms. Both are left unnormalised (l is not folded
+// back into h), which keeps the bounds at ~2^-46 (|a| + |b|) and ~2^-46 |a| |b|
+// -- l only ever holds rounding-sized terms -- for 8 and 4 instructions
+// instead of 11 and 7; the sum h + l is formed in FP64 once, on output.
 // The _rn intrinsics keep the compiler from contracting the error terms.
 struct Dsf {
   float h, l;
@@ -56,16 +61,11 @@ struct Dsf {
   __device__ __forceinline__ Dsf(float v) : h(v), l(0.f) {}
   __device__ __forceinline__ Dsf(float a, float b) : h(a), l(b) {}
 };
-// s + e renormalised, exact when |s| >= |e|
-__device__ __forceinline__ Dsf ds_quick(float s, float e) {
-  const float r = __fadd_rn(s, e);
-  return Dsf(r, __fsub_rn(e, __fsub_rn(r, s)));
-}
 __device__ __forceinline__ Dsf operator+(Dsf a, Dsf b) {
   const float s = __fadd_rn(a.h, b.h);
   const float bb = __fsub_rn(s, a.h);
   const float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));  // a.h + b.h - s, exactly
-  return ds_quick(s, __fadd_rn(e, __fadd_rn(a.l, b.l)));
+  return Dsf(s, __fadd_rn(e, __fadd_rn(a.l, b.l)));
 }
 __device__ __forceinline__ Dsf operator-(Dsf a) { return Dsf(-a.h, -a.l); }
 __device__ __forceinline__ Dsf operator-(Dsf a, Dsf b) { return a + (-b); }
@@ -74,7 +74,7 @@ __device__ __forceinline__ Dsf operator*(Dsf a, Dsf b) {
   float e = __fmaf_rn(a.h, b.h, -p);  // the rounding error of p, exactly
   e = __fmaf_rn(a.h, b.l, e);
   e = __fmaf_rn(a.l, b.h, e);
-  return ds_quick(p, e);
+  return Dsf(p, e);
 }
 __device__ __forceinline__ Dsf& operator+=(Dsf& a, Dsf b) { return a = a + b; }
 __device__ __forceinline__ Dsf& operator-=(Dsf& a, Dsf b) { return a = a - b; }
@@ -378,9 +378,10 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
       xrow(k0 - 1, Xp);
 #pragma unroll
       for (int a = 0; a < 12; a++) accp[a] = A(0);
-#pragma unroll
-      for (int q = 0; q <= RMAX; q++) {
-        if (q > nrow) break;
+      // Unrolled, the double-single body (each operation 7 to 11 FP32
+      // instructions) outgrows the instruction cache: it stays a loop, and
+      // the carries and moduli it indexes by row live in local memory.
+      auto row_step = [&](int q) {
         const int ek = k0 - 1 + q;
         xrow(ek + 1, Xn);
         if (ek >= 0 && ek < ez) {
@@ -516,6 +517,19 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
         for (int a = 0; a < 12; a++) {
           Xp[a] = Xn[a];
           accp[a] = accn[a];
+        }
+      };
+      if constexpr (std::is_same<A, Dsf>::value) {
+#pragma unroll 1
+        for (int q = 0; q <= RMAX; q++) {
+          if (q > nrow) break;
+          row_step(q);
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q <= RMAX; q++) {
+          if (q > nrow) break;
+          row_step(q);
         }
       }
     }

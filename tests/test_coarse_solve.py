@@ -74,6 +74,28 @@ def test_single_launch_against_oracle(case):
     assert relerr(sol, ref) < 1e-9
 
 
+def test_double_single_factor(case):
+    """The factor and the block inverses in double-single arithmetic (the
+    mixed form's default; about 48 bits against FP64's 53): the solution
+    stays within 1e-8 of the FP64 factor's and solves the system to 1e-8."""
+    ctx, x, torch = case
+    lc = ctx.nl - 1
+    rhs = np.random.default_rng(7).uniform(-1, 1, ctx.ndof(lc))
+    b = _dev(torch, rhs)
+    ctx.set_coarse_solve_variant(0)
+    s64 = ctx.coarse_solve(b).cpu().numpy()
+    try:
+        ctx.set_coarse_arith(1)
+        ctx.assemble()
+        sds = ctx.coarse_solve(b).cpu().numpy()
+    finally:
+        ctx.set_coarse_arith(0)
+        ctx.assemble()
+    assert 0 < relerr(sds, s64) < 1e-8
+    back = ctx.apply(lc, _dev(torch, sds)).cpu().numpy()
+    assert relerr(back, rhs) < 1e-8
+
+
 def test_barrier_wait_gives_up(case):
     ctx, x, torch = case
     if ctx.shape != (64, 32, 32):

@@ -464,7 +464,7 @@ tp_status tp_create(const tp_params* p, tp_ctx** out) {
   }
   filter_hs(c, c->d_hs);
   ec_default_plans(c);
-  c->fine_ds = mixed(c) ? 1 : 0;
+  c->fine_ds = c->coarse.ds = mixed(c) ? 1 : 0;
   tp_status st = sync_check(c);
   *out = c;
   if (st != TP_OK) return st;

@@ -79,20 +79,32 @@ tp_status tp_set_fine_arith(tp_ctx* c, int arith) {
   return TP_OK;
 }
 
-tp_status tp_set_coarse_solve_variant(tp_ctx* c, int variant) {
-  if (!c || variant < 0 || variant > 1) return TP_ERR_ARG;
+// the factorisation is redone with the chosen launches or arithmetic at the next solve
+static void coarse_reset(tp_ctx* c) {
   Coarse& C = c->coarse;
-  C.solve_variant = variant;
   if (C.graph_exec) {
     cudaGraphExecDestroy(C.graph_exec);
     C.graph_exec = nullptr;
   }
-  if (C.factor_exec) {  // the factorisation is redone with the chosen launches at the next solve
+  if (C.factor_exec) {
     cudaGraphExecDestroy(C.factor_exec);
     C.factor_exec = nullptr;
   }
   c->assembled = false;
   graph_free(c);
+}
+
+tp_status tp_set_coarse_solve_variant(tp_ctx* c, int variant) {
+  if (!c || variant < 0 || variant > 1) return TP_ERR_ARG;
+  c->coarse.solve_variant = variant;
+  coarse_reset(c);
+  return TP_OK;
+}
+
+tp_status tp_set_coarse_arith(tp_ctx* c, int arith) {
+  if (!c || arith < 0 || arith > 1) return TP_ERR_ARG;
+  c->coarse.ds = arith;
+  coarse_reset(c);
   return TP_OK;
 }
 

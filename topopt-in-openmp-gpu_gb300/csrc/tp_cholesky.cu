@@ -19,8 +19,14 @@
 //            cooperative launch with grid barriers between the half steps
 //            (or, where that launch plan does not apply, as two launches per
 //            block step).
+// The mixed form runs the single-launch factor and the block inverses in
+// double-single arithmetic (tp_dsf.cuh) on the same FP64 storage: its V-cycle
+// is FP32, and FP64 instructions are what the chain of 32-column steps waits
+// on. The sweeps stay FP64: their phases wait on grid barriers and L2 reads,
+// not on their few multiply-adds.
 #include <algorithm>
 
+#include "tp_dsf.cuh"
 #include "tp_internal.h"
 
 namespace tp {
@@ -39,6 +45,16 @@ __device__ __forceinline__ double bget(const double* B, long bw, long r, long c)
 
 static void ps_plan(tp_ctx* c);
 static void pf_plan(tp_ctx* c);
+
+// the operations the factor and solve kernels need on either value type
+__device__ __forceinline__ double vshfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ Dsf vshfl(Dsf v, int src) { return ds_shfl(v, src); }
+__device__ __forceinline__ double vrsqrt(double d) { return rsqrt(d); }
+__device__ __forceinline__ Dsf vrsqrt(Dsf d) { return ds_rsqrt(d); }
+__device__ __forceinline__ bool vpos(double d) { return d > 0.0; }
+__device__ __forceinline__ bool vpos(Dsf d) { return ds_val(d) > 0.0f; }
+__device__ __forceinline__ double vrcp(double d) { return d != 0.0 ? 1.0 / d : 0.0; }
+__device__ __forceinline__ Dsf vrcp(Dsf d) { return ds_val(d) != 0.0f ? ds_rcp(d) : Dsf(0.0f); }
 
 // 8-byte asynchronous copies global -> shared (cp.async); the z form writes
 // zero instead when the source is outside the band
@@ -201,26 +217,26 @@ __device__ __forceinline__ void flag_wait(volatile int* flag, int* info) {
 // so after unrolling every column test is resolved at compile time and no
 // FP64 instruction is issued with all its lanes switched off (such an
 // instruction still holds the FP64 unit).
-template <int W, bool FULL>
-__device__ __forceinline__ void diag_columns(double (*S)[NB + 1], double* rp, volatile int* ready, int nb, long k,
-                                             int* info, int t) {
-  double v[8];  // v[q] = A(t, W + 4q), lower part
+template <typename V, int W, bool FULL>
+__device__ __forceinline__ void diag_columns(V (*S)[NB + 1], V* rp, volatile int* ready, int nb, long k, int* info,
+                                             int t) {
+  V v[8];  // v[q] = A(t, W + 4q), lower part
 #pragma unroll
   for (int q = 0; q < 8; q++) {
     const int c = W + 4 * q;
-    v[q] = ((FULL || c < nb) && t >= c && (FULL || t < nb)) ? S[t][c] : 0.0;
+    v[q] = ((FULL || c < nb) && t >= c && (FULL || t < nb)) ? S[t][c] : V(0.0);
   }
 #pragma unroll
   for (int j = 0; j < NB; j++) {
     if (!FULL && j >= nb) break;
     if ((j & 3) == W) {  // pivot j: column j (v[j >> 2]) has all its updates
-      double d = __shfl_sync(0xffffffffu, v[j >> 2], j);
-      if (!(d > 0.0)) {
+      V d = vshfl(v[j >> 2], j);
+      if (!vpos(d)) {
         if (t == 0) atomicCAS(info, 0, (int)(k + j + 1));
-        d = 1.0;
+        d = V(1.0);
       }
-      const double r = rsqrt(d);
-      const double l = (t >= j) ? v[j >> 2] * r : 0.0;  // L(j,j) = d r
+      const V r = vrsqrt(d);
+      const V l = (t >= j) ? v[j >> 2] * r : V(0.0);  // L(j,j) = d r
       v[j >> 2] = l;
       S[t][j] = l;
       if (t == 0) rp[j] = r;
@@ -228,7 +244,7 @@ __device__ __forceinline__ void diag_columns(double (*S)[NB + 1], double* rp, vo
       __syncwarp();
       if (t == 0) ready[j] = 1;
       if (j >= 1) {  // the updates from pivot j-1 deferred in the last step
-        const double lt = S[t][j - 1];
+        const V lt = S[t][j - 1];
 #pragma unroll
         for (int q = 0; q < 8; q++) {
           const int c = W + 4 * q;
@@ -238,7 +254,7 @@ __device__ __forceinline__ void diag_columns(double (*S)[NB + 1], double* rp, vo
     } else {
       flag_wait(&ready[j], info);
     }
-    const double lt = S[t][j];
+    const V lt = S[t][j];
     if (((j + 1) & 3) == W) {  // the next pivot's column first, the rest after it
       if (j + 1 < NB && (FULL || j + 1 < nb)) v[((j + 1) >> 2) & 7] -= lt * S[(j + 1) & (NB - 1)][j];
     } else {
@@ -251,14 +267,14 @@ __device__ __forceinline__ void diag_columns(double (*S)[NB + 1], double* rp, vo
   }
 }
 
-template <bool FULL>
-__device__ __forceinline__ void diag_columns_of(int w, double (*S)[NB + 1], double* rp, volatile int* ready, int nb,
-                                                long k, int* info, int t) {
+template <typename V, bool FULL>
+__device__ __forceinline__ void diag_columns_of(int w, V (*S)[NB + 1], V* rp, volatile int* ready, int nb, long k,
+                                                int* info, int t) {
   switch (w) {
-    case 0: diag_columns<0, FULL>(S, rp, ready, nb, k, info, t); break;
-    case 1: diag_columns<1, FULL>(S, rp, ready, nb, k, info, t); break;
-    case 2: diag_columns<2, FULL>(S, rp, ready, nb, k, info, t); break;
-    default: diag_columns<3, FULL>(S, rp, ready, nb, k, info, t); break;
+    case 0: diag_columns<V, 0, FULL>(S, rp, ready, nb, k, info, t); break;
+    case 1: diag_columns<V, 1, FULL>(S, rp, ready, nb, k, info, t); break;
+    case 2: diag_columns<V, 2, FULL>(S, rp, ready, nb, k, info, t); break;
+    default: diag_columns<V, 3, FULL>(S, rp, ready, nb, k, info, t); break;
   }
 }
 
@@ -271,9 +287,9 @@ __device__ void factor_diag_block(double* __restrict__ B, long bw, long k, int n
   __syncthreads();
   if (w < 4) {
     if (nb == NB)
-      diag_columns_of<true>(w, S, rp, ready, nb, k, info, t);
+      diag_columns_of<double, true>(w, S, rp, ready, nb, k, info, t);
     else
-      diag_columns_of<false>(w, S, rp, ready, nb, k, info, t);
+      diag_columns_of<double, false>(w, S, rp, ready, nb, k, info, t);
   }
   __syncthreads();
   for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
@@ -308,28 +324,28 @@ constexpr int kTrsmThreads = 128;
 // The tile A (row t, column c; 32 x 32 in shared memory) is solved in place;
 // a finished column is published in A itself (its other entries live in the
 // owner's registers until the end).
-template <int W, bool FULL>
-__device__ __forceinline__ void trsm_columns(double (*A)[NB + 1], int nb, const double (*Lb)[NB + 1],
-                                             const double* rp, volatile int* ready, int* info, int t) {
-  double (*X)[NB + 1] = A;
-  double v[8];
+template <typename V, int W, bool FULL>
+__device__ __forceinline__ void trsm_columns(V (*A)[NB + 1], int nb, const V (*Lb)[NB + 1], const V* rp,
+                                             volatile int* ready, int* info, int t) {
+  V (*X)[NB + 1] = A;
+  V v[8];
 #pragma unroll
   for (int q = 0; q < 8; q++) {
     const int c = W + 4 * q;
-    v[q] = (FULL || c < nb) ? A[t][c] : 0.0;
+    v[q] = (FULL || c < nb) ? A[t][c] : V(0.0);
   }
 #pragma unroll
   for (int p = 0; p < NB; p++) {
     if (!FULL && p >= nb) break;
     if ((p & 3) == W) {
-      const double x = v[p >> 2] * rp[p];
+      const V x = v[p >> 2] * rp[p];
       v[p >> 2] = x;
       X[t][p] = x;
       __threadfence_block();
       __syncwarp();
       if (t == 0) ready[p] = 1;
       if (p >= 1) {  // the updates from column p-1 deferred in the last step
-        const double xt = X[t][p - 1];
+        const V xt = X[t][p - 1];
 #pragma unroll
         for (int q = 0; q < 8; q++) {
           const int c = W + 4 * q;
@@ -339,7 +355,7 @@ __device__ __forceinline__ void trsm_columns(double (*A)[NB + 1], int nb, const 
     } else {
       flag_wait(&ready[p], info);
     }
-    const double xt = X[t][p];
+    const V xt = X[t][p];
     if (((p + 1) & 3) == W) {
       if (p + 1 < NB && (FULL || p + 1 < nb)) v[((p + 1) >> 2) & 7] -= xt * Lb[(p + 1) & (NB - 1)][p];
     } else {
@@ -358,23 +374,24 @@ __device__ __forceinline__ void trsm_columns(double (*A)[NB + 1], int nb, const 
 }
 
 // solve the tile A in place with warps 0-3 (the caller syncs before and after)
-__device__ __forceinline__ void trsm_tile(double (*A)[NB + 1], int nb, const double (*Lb)[NB + 1], const double* rp,
+template <typename V>
+__device__ __forceinline__ void trsm_tile(V (*A)[NB + 1], int nb, const V (*Lb)[NB + 1], const V* rp,
                                           volatile int* ready, int* info) {
   const int w = threadIdx.x >> 5, t = threadIdx.x & 31;
   if (w >= 4) return;
   if (nb == NB) {
     switch (w) {
-      case 0: trsm_columns<0, true>(A, nb, Lb, rp, ready, info, t); break;
-      case 1: trsm_columns<1, true>(A, nb, Lb, rp, ready, info, t); break;
-      case 2: trsm_columns<2, true>(A, nb, Lb, rp, ready, info, t); break;
-      default: trsm_columns<3, true>(A, nb, Lb, rp, ready, info, t); break;
+      case 0: trsm_columns<V, 0, true>(A, nb, Lb, rp, ready, info, t); break;
+      case 1: trsm_columns<V, 1, true>(A, nb, Lb, rp, ready, info, t); break;
+      case 2: trsm_columns<V, 2, true>(A, nb, Lb, rp, ready, info, t); break;
+      default: trsm_columns<V, 3, true>(A, nb, Lb, rp, ready, info, t); break;
     }
   } else {
     switch (w) {
-      case 0: trsm_columns<0, false>(A, nb, Lb, rp, ready, info, t); break;
-      case 1: trsm_columns<1, false>(A, nb, Lb, rp, ready, info, t); break;
-      case 2: trsm_columns<2, false>(A, nb, Lb, rp, ready, info, t); break;
-      default: trsm_columns<3, false>(A, nb, Lb, rp, ready, info, t); break;
+      case 0: trsm_columns<V, 0, false>(A, nb, Lb, rp, ready, info, t); break;
+      case 1: trsm_columns<V, 1, false>(A, nb, Lb, rp, ready, info, t); break;
+      case 2: trsm_columns<V, 2, false>(A, nb, Lb, rp, ready, info, t); break;
+      default: trsm_columns<V, 3, false>(A, nb, Lb, rp, ready, info, t); break;
     }
   }
 }
@@ -582,13 +599,13 @@ __device__ __forceinline__ void pf_release(int* flag, int v) {
 
 // tile (I, J) into A[r][c] (TR: A[c][r]); zero outside the matrix, above the
 // diagonal and outside the band
-template <bool TR>
-__device__ void pf_load(const PfArgs& a, long I, long J, double (*A)[NB + 1]) {
+template <bool TR, typename V>
+__device__ void pf_load(const PfArgs& a, long I, long J, V (*A)[NB + 1]) {
   for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
     const int r = idx & 31, c = idx >> 5;
     const long gr = 32 * I + r, gc = 32 * J + c;
     const bool in = gr < a.n && gr >= gc && gr - gc <= a.bw;
-    const double v = in ? __ldcg(a.B + gc * a.bw + gr) : 0.0;
+    const V v = ds_in<V>(in ? __ldcg(a.B + gc * a.bw + gr) : 0.0);
     if (TR)
       A[c][r] = v;
     else
@@ -596,18 +613,20 @@ __device__ void pf_load(const PfArgs& a, long I, long J, double (*A)[NB + 1]) {
   }
 }
 
-__device__ void pf_store(const PfArgs& a, long I, long J, const double (*A)[NB + 1]) {
+template <typename V>
+__device__ void pf_store(const PfArgs& a, long I, long J, const V (*A)[NB + 1]) {
   for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
     const int r = idx & 31, c = idx >> 5;
     const long gr = 32 * I + r, gc = 32 * J + c;
-    if (gr < a.n && gr >= gc && gr - gc <= a.bw) a.B[gc * a.bw + gr] = A[r][c];
+    if (gr < a.n && gr >= gc && gr - gc <= a.bw) a.B[gc * a.bw + gr] = ds_out(A[r][c]);
   }
 }
 
+template <typename V>
 __device__ void pf_chain(const PfArgs& a, double* smem) {
-  double(*D)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(smem);  // diagonal tile, then L_kk
-  double(*X)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(smem + NB * (NB + 1));  // panel tile (k+1,k)
-  double* rp = smem + 2 * NB * (NB + 1);
+  V(*D)[NB + 1] = reinterpret_cast<V(*)[NB + 1]>(smem);                // diagonal tile, then L_kk
+  V(*X)[NB + 1] = reinterpret_cast<V(*)[NB + 1]>(smem + NB * (NB + 1));  // panel tile (k+1,k)
+  V* rp = reinterpret_cast<V*>(smem + 2 * NB * (NB + 1));
   volatile int* ready = reinterpret_cast<volatile int*>(rp + NB);
   const int w = threadIdx.x >> 5, t = threadIdx.x & 31;
   pf_load<false>(a, 0, 0, D);
@@ -617,13 +636,13 @@ __device__ void pf_chain(const PfArgs& a, double* smem) {
     __syncthreads();
     if (w < 4) {
       if (nb == NB)
-        diag_columns_of<true>(w, D, rp, ready, nb, 32 * k, a.info, t);
+        diag_columns_of<V, true>(w, D, rp, ready, nb, 32 * k, a.info, t);
       else
-        diag_columns_of<false>(w, D, rp, ready, nb, 32 * k, a.info, t);
+        diag_columns_of<V, false>(w, D, rp, ready, nb, 32 * k, a.info, t);
     }
     __syncthreads();
     pf_store(a, k, k, D);
-    if (threadIdx.x < NB) a.rpk[k * NB + threadIdx.x] = threadIdx.x < nb ? rp[threadIdx.x] : 0.0;
+    if (threadIdx.x < NB) a.rpk[k * NB + threadIdx.x] = threadIdx.x < nb ? ds_out(rp[threadIdx.x]) : 0.0;
     pf_release(a.fdone + k, 1);
     if (pf_imax(a.n, a.bw, k) < k + 1) break;
     const bool prev = k >= 1 && k + 1 <= pf_imax(a.n, a.bw, k - 1);  // tiles (k+1, *) hold a step k-1 update
@@ -645,7 +664,7 @@ __device__ void pf_chain(const PfArgs& a, double* smem) {
       while ((r + 1) * (r + 2) / 2 <= e) r++;
       while (r * (r + 1) / 2 > e) r--;
       const int c = e - r * (r + 1) / 2;
-      double s = 0.0;
+      V s = V(0.0);
 #pragma unroll
       for (int q = 0; q < NB; q++) s += X[r][q] * X[c][q];
       D[r][c] -= s;
@@ -761,21 +780,23 @@ __device__ __forceinline__ void pf_fetch(const PfArgs& a, const PfItem& it, PfRe
 }
 
 // S: P, Q row-major (P solved in place); U: transposed, P[t][r] = L(32I + r, 32k + t)
-__device__ __forceinline__ void pf_put(const PfItem& it, const PfRegs& R, double (*P)[NB + 1],
-                                       double (*Q)[NB + 1], double* rp, volatile int* ready) {
+template <typename V>
+__device__ __forceinline__ void pf_put(const PfItem& it, const PfRegs& R, V (*P)[NB + 1], V (*Q)[NB + 1], V* rp,
+                                       volatile int* ready) {
 #pragma unroll
   for (int m = 0; m < 4; m++) {
     const int idx = threadIdx.x + 256 * m, r = idx & 31, c = idx >> 5;
+    const V p = ds_in<V>(R.p[m]), q = ds_in<V>(R.q[m]);
     if (it.solve) {
-      P[r][c] = R.p[m];
-      Q[r][c] = R.q[m];
+      P[r][c] = p;
+      Q[r][c] = q;
     } else {
-      P[c][r] = R.p[m];
-      Q[c][r] = R.q[m];
+      P[c][r] = p;
+      Q[c][r] = q;
     }
   }
   if (it.solve && threadIdx.x < NB) {
-    rp[threadIdx.x] = R.r;
+    rp[threadIdx.x] = ds_in<V>(R.r);
     ready[threadIdx.x] = 0;
   }
 }
@@ -783,10 +804,11 @@ __device__ __forceinline__ void pf_put(const PfItem& it, const PfRegs& R, double
 // The non-chain CTAs take items g = blockIdx.x - 1 + m (gridDim.x - 1). While
 // one item is computed, the next item's inputs are loaded into registers if
 // its flags are already set (otherwise it waits for them when its turn comes).
+template <typename V>
 __device__ void pf_bulk(const PfArgs& a, double* smem) {
-  double(*P)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(smem);
-  double(*Q)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(smem + NB * (NB + 1));
-  double* rp = smem + 2 * NB * (NB + 1);
+  V(*P)[NB + 1] = reinterpret_cast<V(*)[NB + 1]>(smem);
+  V(*Q)[NB + 1] = reinterpret_cast<V(*)[NB + 1]>(smem + NB * (NB + 1));
+  V* rp = reinterpret_cast<V*>(smem + 2 * NB * (NB + 1));
   volatile int* ready = reinterpret_cast<volatile int*>(rp + NB);
   const long nbulk = gridDim.x - 1, total = a.off[a.NT];
   long g = blockIdx.x - 1, kk = 0;
@@ -828,10 +850,10 @@ __device__ void pf_bulk(const PfArgs& a, double* smem) {
       for (int q = 0; q < 4; q++) {
         const int cy = ty + 8 * q;
         const long gc = 32 * cur.J + cy;
-        double s = 0.0;
+        V s = V(0.0);
 #pragma unroll
         for (int t = 0; t < NB; t++) s += P[t][tx] * Q[t][cy];
-        if (gr < a.n && gc <= gr && gr - gc <= a.bw) a.B[gc * a.bw + gr] = old[q] - s;
+        if (gr < a.n && gc <= gr && gr - gc <= a.bw) a.B[gc * a.bw + gr] = ds_out(ds_in<V>(old[q]) - s);
       }
       pf_release(a.tver + cur.J * a.TS + (cur.I - cur.J), (int)cur.k + 1);
     }
@@ -839,12 +861,13 @@ __device__ void pf_bulk(const PfArgs& a, double* smem) {
   }
 }
 
+template <typename V>
 __global__ void __launch_bounds__(256) pf_kernel(PfArgs a) {
   extern __shared__ double sm[];
   if (blockIdx.x == 0)
-    pf_chain(a, sm);
+    pf_chain<V>(a, sm);
   else
-    pf_bulk(a, sm);
+    pf_bulk<V>(a, sm);
 }
 
 // Inverse of each diagonal NBSxNBS block of L, one CTA per (block, 32-column
@@ -854,13 +877,14 @@ __global__ void __launch_bounds__(256) pf_kernel(PfArgs a) {
 // with X kept in shared memory. Writes D (row-major) and D^T (row-major).
 constexpr int kDinvThreads = 256;
 
+template <typename V>
 __global__ void __launch_bounds__(kDinvThreads)
     dinv_kernel(const double* __restrict__ B, long bw, long n, int nbs, double* __restrict__ D,
                 double* __restrict__ DT) {
-  extern __shared__ double smem[];
-  double* X = smem;                    // nbs x 33
-  double* Lt = X + (long)nbs * 33;     // 32 x 33
-  double* Acc = Lt + 32 * 33;          // the chunk's 32 reciprocal pivots
+  extern __shared__ double smem_d[];
+  V* X = reinterpret_cast<V*>(smem_d);  // nbs x 33
+  V* Lt = X + (long)nbs * 33;           // 32 x 33
+  V* Acc = Lt + 32 * 33;                // the chunk's 32 reciprocal pivots
   const int blk = blockIdx.y, cc = blockIdx.x, tid = threadIdx.x;
   const long b0 = (long)blk * nbs;
   const int s = (int)lmin((long)nbs, n - b0);
@@ -870,20 +894,20 @@ __global__ void __launch_bounds__(kDinvThreads)
   const int a = tid >> 3, q0 = (tid & 7) * 4;
   const int nR = (s + 31) / 32;
   for (int R = cc; R < nR; R++) {
-    double acc[4];
+    V acc[4];
 #pragma unroll
-    for (int q = 0; q < 4; q++) acc[q] = (R == cc && a == q0 + q) ? 1.0 : 0.0;
+    for (int q = 0; q < 4; q++) acc[q] = V((R == cc && a == q0 + q) ? 1.0f : 0.0f);
     for (int S = cc; S < R; S++) {
       for (int idx = tid; idx < 1024; idx += kDinvThreads) {
         const int ra = idx & 31, cs = idx >> 5;
         const long r = b0 + R * 32 + ra, col = b0 + S * 32 + cs;
-        Lt[ra * 33 + cs] = (R * 32 + ra < s) ? bget(B, bw, r, col) : 0.0;
+        Lt[ra * 33 + cs] = ds_in<V>((R * 32 + ra < s) ? bget(B, bw, r, col) : 0.0);
       }
       __syncthreads();
 #pragma unroll 4
       for (int t = 0; t < 32; t++) {
-        const double l = Lt[a * 33 + t];
-        const double* xr = X + (long)(S * 32 + t) * 33 + q0;
+        const V l = Lt[a * 33 + t];
+        const V* xr = X + (long)(S * 32 + t) * 33 + q0;
 #pragma unroll
         for (int q = 0; q < 4; q++) acc[q] -= l * xr[q];
       }
@@ -892,12 +916,11 @@ __global__ void __launch_bounds__(kDinvThreads)
     for (int idx = tid; idx < 1024; idx += kDinvThreads) {
       const int ra = idx & 31, cs = idx >> 5;
       const long r = b0 + R * 32 + ra, col = b0 + R * 32 + cs;
-      Lt[ra * 33 + cs] = (R * 32 + ra < s && R * 32 + cs < s && ra >= cs) ? bget(B, bw, r, col) : 0.0;
+      Lt[ra * 33 + cs] = ds_in<V>((R * 32 + ra < s && R * 32 + cs < s && ra >= cs) ? bget(B, bw, r, col) : 0.0);
     }
     __syncthreads();
     if (tid < 32) {  // reciprocal pivots of the chunk (rows past s give zero rows of X)
-      const double d = Lt[tid * 33 + tid];
-      Acc[tid] = (R * 32 + tid < s && d != 0.0) ? 1.0 / d : 0.0;
+      Acc[tid] = R * 32 + tid < s ? vrcp(Lt[tid * 33 + tid]) : V(0.0f);
     }
     __syncthreads();
     // X_R = L_RR^{-1} acc, right-looking over all warps: row t is finished
@@ -912,8 +935,8 @@ __global__ void __launch_bounds__(kDinvThreads)
       }
       __syncthreads();
       if (a > t) {
-        const double l = Lt[a * 33 + t];
-        const double* xr = X + (long)(R * 32 + t) * 33 + q0;
+        const V l = Lt[a * 33 + t];
+        const V* xr = X + (long)(R * 32 + t) * 33 + q0;
 #pragma unroll
         for (int q = 0; q < 4; q++) acc[q] -= l * xr[q];
       }
@@ -923,12 +946,12 @@ __global__ void __launch_bounds__(kDinvThreads)
   // D[r][j0+col] for r in [0, nbs): zero above the diagonal chunk and past s
   for (int idx = tid; idx < nbs * 32; idx += kDinvThreads) {
     const int r = idx >> 5, col = idx & 31;
-    const double v = (r >= j0 && r < s && j0 + col < s) ? X[(long)r * 33 + col] : 0.0;
+    const double v = (r >= j0 && r < s && j0 + col < s) ? ds_out(X[(long)r * 33 + col]) : 0.0;
     Db[(long)r * nbs + j0 + col] = v;
   }
   for (int idx = tid; idx < nbs * 32; idx += kDinvThreads) {
     const int col = idx / nbs, r = idx % nbs;
-    const double v = (r >= j0 && r < s && j0 + col < s) ? X[(long)r * 33 + col] : 0.0;
+    const double v = (r >= j0 && r < s && j0 + col < s) ? ds_out(X[(long)r * 33 + col]) : 0.0;
     DTb[(long)(j0 + col) * nbs + r] = v;
   }
 }
@@ -1024,14 +1047,13 @@ static void pf_plan(tp_ctx* c) {
     TS = std::max(TS, T + 2);
     off[k + 1] = off[k] + (T >= 1 ? (T - 1) + T * (T + 1) / 2 - 1 : 0);
   }
-  if (cudaFuncSetAttribute(pf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPfSmem) != cudaSuccess) {
-    cudaGetLastError();
-    return;
-  }
-  int per = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pf_kernel, 256, kPfSmem) != cudaSuccess || per < 1) {
-    cudaGetLastError();
-    return;
+  for (auto kern : {pf_kernel<double>, pf_kernel<Dsf>}) {
+    int per = 0;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPfSmem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, 256, kPfSmem) != cudaSuccess || per < 1) {
+      cudaGetLastError();
+      return;
+    }
   }
   C.pf_NT = (int)NT;
   C.pf_TS = (int)TS;
@@ -1064,7 +1086,7 @@ static void pf_launch(tp_ctx* c) {
   cfg.stream = c->s;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, pf_kernel, a);
+  cudaLaunchKernelEx(&cfg, C.ds ? pf_kernel<Dsf> : pf_kernel<double>, a);
 }
 
 static void coarse_factor_launches(tp_ctx* c, size_t dinv_smem) {
@@ -1074,7 +1096,8 @@ static void coarse_factor_launches(tp_ctx* c, size_t dinv_smem) {
     pf_launch(c);
   else
     step_launches(c);
-  dinv_kernel<<<dim3(C.nbs / 32, C.nblk), kDinvThreads, dinv_smem, c->s>>>(C.band, C.bw, C.n, C.nbs, C.dinv, C.dinvT);
+  (C.ds ? dinv_kernel<Dsf> : dinv_kernel<double>)<<<dim3(C.nbs / 32, C.nblk), kDinvThreads, dinv_smem, c->s>>>(
+      C.band, C.bw, C.n, C.nbs, C.dinv, C.dinvT);
   lrow_kernel<<<dim3((unsigned)((C.bw + 31) / 32), C.nbs / 32, C.nblk), dim3(32, 8), 0, c->s>>>(C.band, C.bw, C.n,
                                                                                                C.nbs, C.lrow);
 }
@@ -1086,7 +1109,8 @@ void coarse_factor(tp_ctx* c) {
   Coarse& C = c->coarse;
   const size_t smem = ((size_t)C.nbs * 33 + 2 * 32 * 33) * sizeof(double);
   if (!C.factor_exec) {
-    cudaFuncSetAttribute(dinv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(dinv_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(dinv_kernel<Dsf>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
       coarse_factor_launches(c, smem);

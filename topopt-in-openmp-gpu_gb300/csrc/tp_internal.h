@@ -82,6 +82,7 @@ struct Coarse {
   long ps_spin = 0;             // polls before a barrier wait gives up (0: the default, about a second)
   int ps_missing = 0;           // arrivals each barrier waits for beyond the grid (failure-detection test only)
   int solve_variant = 0;        // 0: single launches (factor and solve) where their plans apply; 1: launches per step
+  int ds = 0;                   // single-launch factor and block inverses in double-single arithmetic
   // single-launch factor (one cooperative kernel for all 32-column steps)
   bool pf_ok = false;
   int pf_NT = 0, pf_TS = 0;     // diagonal tiles; row stride of its flag arrays

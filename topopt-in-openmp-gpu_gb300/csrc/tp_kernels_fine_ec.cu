@@ -30,6 +30,7 @@
 #include <cmath>
 #include <type_traits>
 
+#include "tp_dsf.cuh"
 #include "tp_internal.h"
 
 namespace tp {
@@ -37,69 +38,6 @@ namespace tp {
 __constant__ double c_kz[45];
 __constant__ float c_kzf[45];
 __constant__ float c_kzd[45][2];  // c_kz as double-single pairs
-
-// ---------------------------------------------------------------------------
-// Double-single arithmetic: a value is the unevaluated sum h + l of two FP32
-// numbers (Dekker, "A floating-point technique for extending the available
-// precision", 1971; the sum's error term is Knuth's two-sum). The FP64 pipe of
-// this part issues one warp instruction per ~67 cycles per SM sub-partition,
-// the FP32 pipe one per cycle, so an FP64 operand in memory can be worked on
-// as a pair of floats for a fraction of the FP64 time.
-// The sum of element contributions needs each operation's error bounded
-// relative to its operands, as an FP64 evaluation bounds it by 2^-53
-// (|a| + |b|), not relative to its result. Here: a + b takes the exact
-// two-sum of the high parts and adds the low parts and the two-sum's error
-// in FP32; a * b takes the exact product of the high parts (an FMA gives its
-// error) plus the cross terms. Both are left unnormalised (l is not folded
-// back into h), which keeps the bounds at ~2^-46 (|a| + |b|) and ~2^-46 |a| |b|
-// -- l only ever holds rounding-sized terms -- for 8 and 4 instructions
-// instead of 11 and 7; the sum h + l is formed in FP64 once, on output.
-// The _rn intrinsics keep the compiler from contracting the error terms.
-struct Dsf {
-  float h, l;
-  Dsf() = default;
-  __device__ __forceinline__ Dsf(float v) : h(v), l(0.f) {}
-  __device__ __forceinline__ Dsf(float a, float b) : h(a), l(b) {}
-};
-__device__ __forceinline__ Dsf operator+(Dsf a, Dsf b) {
-  const float s = __fadd_rn(a.h, b.h);
-  const float bb = __fsub_rn(s, a.h);
-  const float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));  // a.h + b.h - s, exactly
-  return Dsf(s, __fadd_rn(e, __fadd_rn(a.l, b.l)));
-}
-__device__ __forceinline__ Dsf operator-(Dsf a) { return Dsf(-a.h, -a.l); }
-__device__ __forceinline__ Dsf operator-(Dsf a, Dsf b) { return a + (-b); }
-__device__ __forceinline__ Dsf operator*(Dsf a, Dsf b) {
-  const float p = __fmul_rn(a.h, b.h);
-  float e = __fmaf_rn(a.h, b.h, -p);  // the rounding error of p, exactly
-  e = __fmaf_rn(a.h, b.l, e);
-  e = __fmaf_rn(a.l, b.h, e);
-  return Dsf(p, e);
-}
-__device__ __forceinline__ Dsf& operator+=(Dsf& a, Dsf b) { return a = a + b; }
-__device__ __forceinline__ Dsf& operator-=(Dsf& a, Dsf b) { return a = a - b; }
-
-// double -> double-single with integer operations only (the FP64 pipe stays
-// free): h keeps the sign, the exponent and the leading 23 stored mantissa
-// bits (truncated), l the remaining 29 bits rounded to 24. Magnitudes below
-// FP32's normal range become 0, magnitudes above it infinity, NaN stays NaN.
-__device__ __forceinline__ Dsf ds_from(double v) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-  const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
-  const unsigned sg = hw & 0x80000000u;
-  const int e = (int)((hw >> 20) & 0x7ffu);  // biased by 1023
-  if (e < 897) return Dsf(0.f);              // |v| < 2^-126
-  if (e > 1150) {                            // |v| >= 2^128, inf, NaN
-    const bool nan = e == 2047 && ((hw & 0xfffffu) | lw) != 0u;
-    return Dsf(__uint_as_float(nan ? 0x7fc00000u : (sg | 0x7f800000u)));
-  }
-  const float h = __uint_as_float(sg | ((unsigned)(e - 896) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
-  // the low 29 mantissa bits carry weight 2^(e - 1023 - 52)
-  const float sc = e >= 949 ? __uint_as_float((unsigned)(e - 948) << 23) : 0.f;
-  const float l = __fmul_rn(__int2float_rn((int)(lw & 0x1fffffffu)), sc);
-  return Dsf(h, sg ? -l : l);
-}
-__device__ __forceinline__ double ds_to(Dsf a) { return (double)a.h + (double)a.l; }
 
 // storage type T <-> arithmetic type A of the element-centric kernel
 template <typename A, typename T>

@@ -98,6 +98,7 @@ def load():
     L.tp_set_cg.argtypes = [V, D, I, I, D]
     L.tp_set_fine_variant.argtypes = [V, I]
     L.tp_set_fine_arith.argtypes = [V, I]
+    L.tp_set_coarse_arith.argtypes = [V, I]
     L.tp_set_coarse_solve_variant.argtypes = [V, I]
     L.tp_fault_coarse_barrier.argtypes = [V, ctypes.c_long, I]
     L.tp_autotune.argtypes = [V, P]
@@ -231,6 +232,10 @@ class TopOpt:
     def set_fine_arith(self, arith):
         """Level-0 kernel on double vectors: 0 FP64; 1 double-single (default in the mixed form)."""
         self._check(self.L.tp_set_fine_arith(self.ctx, arith))
+
+    def set_coarse_arith(self, arith):
+        """Coarsest-level Cholesky: 0 FP64; 1 double-single (default in the mixed form)."""
+        self._check(self.L.tp_set_coarse_arith(self.ctx, arith))
 
     def set_coarse_solve_variant(self, variant):
         """0: coarse triangular sweeps in one cooperative launch; 1: two launches per block step."""

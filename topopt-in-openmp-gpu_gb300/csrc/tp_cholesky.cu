@@ -25,6 +25,7 @@
 // on. The sweeps stay FP64: their phases wait on grid barriers and L2 reads,
 // not on their few multiply-adds.
 #include <algorithm>
+#include <type_traits>
 
 #include "tp_dsf.cuh"
 #include "tp_internal.h"
@@ -267,6 +268,44 @@ __device__ __forceinline__ void diag_columns(V (*S)[NB + 1], V* rp, volatile int
   }
 }
 
+// Double-single form of the panel-tile solve, same column ownership: at FP32
+// speed the per-column hand-off dominates, and a named barrier over the four
+// warps (bar.sync 1, 128; it orders their shared-memory accesses) costs less
+// than the flag, fences and polls (16k against 21k cycles per tile). The
+// owner of the next column updates that column first. (For the diagonal
+// factor the flags stay ahead, 22k against 35k: there the warps that do not
+// own the pivot run ahead into their updates.)
+__device__ __forceinline__ void bar_warps0to3() { asm volatile("bar.sync 1, 128;\n" ::: "memory"); }
+
+template <int W, bool FULL>
+__device__ __forceinline__ void trsm_columns_ds(Dsf (*A)[NB + 1], int nb, const Dsf (*Lb)[NB + 1], const Dsf* rp,
+                                                int t) {
+  Dsf v[8];
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const int c = W + 4 * q;
+    v[q] = (FULL || c < nb) ? A[t][c] : Dsf(0.f);
+  }
+#pragma unroll
+  for (int p = 0; p < NB; p++) {
+    if (!FULL && p >= nb) break;
+    if ((p & 3) == W) {
+      const Dsf x = v[p >> 2] * rp[p];
+      v[p >> 2] = x;
+      A[t][p] = x;
+    }
+    bar_warps0to3();
+    const Dsf xt = A[t][p];
+    if (((p + 1) & 3) == W && p + 1 < NB && (FULL || p + 1 < nb)) v[(p + 1) >> 2] -= xt * Lb[p + 1][p];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const int c = W + 4 * q;
+      if (c > p + 1 && (FULL || c < nb)) v[q] -= xt * Lb[c][p];
+    }
+  }
+  // each column was stored in the step that finished it
+}
+
 template <typename V, bool FULL>
 __device__ __forceinline__ void diag_columns_of(int w, V (*S)[NB + 1], V* rp, volatile int* ready, int nb, long k,
                                                 int* info, int t) {
@@ -379,6 +418,24 @@ __device__ __forceinline__ void trsm_tile(V (*A)[NB + 1], int nb, const V (*Lb)[
                                           volatile int* ready, int* info) {
   const int w = threadIdx.x >> 5, t = threadIdx.x & 31;
   if (w >= 4) return;
+  if constexpr (std::is_same<V, Dsf>::value) {
+    if (nb == NB) {
+      switch (w) {
+        case 0: trsm_columns_ds<0, true>(A, nb, Lb, rp, t); break;
+        case 1: trsm_columns_ds<1, true>(A, nb, Lb, rp, t); break;
+        case 2: trsm_columns_ds<2, true>(A, nb, Lb, rp, t); break;
+        default: trsm_columns_ds<3, true>(A, nb, Lb, rp, t); break;
+      }
+    } else {
+      switch (w) {
+        case 0: trsm_columns_ds<0, false>(A, nb, Lb, rp, t); break;
+        case 1: trsm_columns_ds<1, false>(A, nb, Lb, rp, t); break;
+        case 2: trsm_columns_ds<2, false>(A, nb, Lb, rp, t); break;
+        default: trsm_columns_ds<3, false>(A, nb, Lb, rp, t); break;
+      }
+    }
+    return;
+  }
   if (nb == NB) {
     switch (w) {
       case 0: trsm_columns<V, 0, true>(A, nb, Lb, rp, ready, info, t); break;

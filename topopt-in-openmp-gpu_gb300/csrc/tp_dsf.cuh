@@ -21,7 +21,8 @@ namespace tp {
 // -- l only ever holds rounding-sized terms -- for 8 and 4 instructions
 // instead of 11 and 7; the sum h + l is formed in FP64 once, on output.
 // The _rn intrinsics keep the compiler from contracting the error terms.
-struct Dsf {
+// 8-byte aligned, so a pair moves to and from shared memory as one access.
+struct __align__(8) Dsf {
   float h, l;
   Dsf() = default;
   __device__ __forceinline__ Dsf(float v) : h(v), l(0.f) {}

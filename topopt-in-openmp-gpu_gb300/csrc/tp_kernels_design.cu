@@ -345,8 +345,24 @@ __device__ __forceinline__ double oc_xnew(double x, double dc, double dv, double
 // reference's expression itself at the chosen lmid). The reference's nested
 // MAX/MIN equal max(lo, min(hi, xs)) with lo = max(0, x - move) and
 // hi = min(1, x + move) -- min and max do not round -- and lo, hi are formed
-// once too: FP64 instructions are what a step costs on this part, and this
-// leaves five per element (multiply, min, max, subtract, multiply-add).
+// once too. FP64 instructions are what a step costs on this part: lo, hi and
+// xs are non-negative, so the clamp is an integer comparison of their bit
+// patterns (the same values as fmin/fmax; a NaN xs, from a positive dc,
+// counts as +inf, as fmin treats it), which leaves three per element
+// (multiply, subtract, multiply-add). The sum keeps the reference's form
+// dv (xnew - x) and its fold order: near the root gt is small, and another
+// rounding of it can turn a bisection decision.
+// max(lo, min(hi, v)) for 0 <= lo <= hi finite and any v: a NaN v gives hi
+// (+inf here, as fmin ignores it), a negative v or -0 (B = -0 when the
+// filtered dc is +0) gives lo (+0 here)
+__device__ __forceinline__ double oc_clamp(double lo, double hi, double v) {
+  long long iv = __double_as_longlong(v);
+  if (iv < 0) iv = (iv & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL ? 0x7ff0000000000000LL : 0;
+  else if (iv > 0x7ff0000000000000LL) iv = 0x7ff0000000000000LL;
+  const long long il = __double_as_longlong(lo), ih = __double_as_longlong(hi);
+  iv = iv < ih ? iv : ih;
+  return __longlong_as_double(iv > il ? iv : il);
+}
 __global__ void oc_prep_kernel(long n, const double* __restrict__ x, const double* __restrict__ dc,
                                const double* __restrict__ dv, double* __restrict__ B, double* __restrict__ lo,
                                double* __restrict__ hi) {
@@ -370,7 +386,7 @@ __global__ void oc_step_kernel(long n, const double* __restrict__ x, const doubl
   double s = 0.0;
   for (long e = blockIdx.x * 256L + threadIdx.x; e < n; e += (long)gridDim.x * 256) {
     const double xe = x[e];
-    const double xn = B ? fmax(lo[e], fmin(hi[e], B[e] * rl)) : oc_xnew(xe, dc[e], dv[e], lmid);
+    const double xn = B ? oc_clamp(lo[e], hi[e], B[e] * rl) : oc_xnew(xe, dc[e], dv[e], lmid);
     s += dv[e] * (xn - xe);
   }
   s = bsum256(s);

@@ -1,7 +1,8 @@
 #!/usr/bin/env python
 """Design iterations/s of the SIMP compliance loop with its multigrid-CG state
-solve at 256x128x128 elements (-l 4), mixed precision (FP32 V-cycle, FP64 CG)
-against the plain FP64 form, plus the fine-grid matvec's HBM roofline.
+solve at 256x128x128 elements (-l 4), mixed precision (FP32 V-cycle; FP64 CG
+vectors with a double-single matvec and coarse factor) against the plain FP64
+form, plus the fine-grid matvec's HBM roofline.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -429,8 +430,11 @@ def main():
     # The HBM roofline is reported for the level-0 FP32 Jacobi sweep: the
     # bandwidth-bound matvec kernel of the mixed V-cycle (the most launched
     # fine-grid kernel). The larger shares -- the coarse band Cholesky and the
-    # FP64 CG matvec -- are bound by the FP64 pipe (measured peak on this part:
-    # about 600 GFMA/s); their achieved FP64 rates are in "fp64_bound".
+    # CG matvec on FP64 vectors -- are compute kernels: in the mixed form both
+    # run in double-single arithmetic (FP32 issue and dependent latency bound;
+    # the factor's chain of 32-column steps), in the FP64 form on the FP64 pipe
+    # (about 600 GFMA/s on this part). Their FP64-equivalent operation rates
+    # are in "compute_bound".
     dom = "fine_jacobi_f32" if "fine_jacobi_f32" in kernels else None
     roofline = None
     if dom:
@@ -442,32 +446,33 @@ def main():
                     "frac": round(ach / hbm, 4), "traffic": tr, "algorithmic_bytes": nbytes[dom],
                     "avg_launch_us": round(avg_s * 1e6, 2), "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind
                     if peak_kind == "measured" else "fallback 6.8 TB/s"}
-    fp64_bound = {}
+    compute_bound = {}
     nn = (shape[0] + 1) * (shape[1] + 1) * (shape[2] + 1)
     if "fine_apply_f64" in prof and prof["fine_apply_f64"][0]:
         la, ms = prof["fine_apply_f64"]
-        # executed FP64 operations of the element-centric matvec: about 171
-        # per element (butterflies, the 45-term product, accumulation) and the
-        # recomputed halo rows and layers (x 1.25)
-        fp64_bound["fine_apply_f64"] = {"share": kernels["fine_apply_f64"]["share"],
-                                        "fp64_gops": round(171 * 1.25 * nn / (ms / la / 1000.0) / 1e9, 1)}
+        # operations of the element-centric matvec: about 171 per element
+        # (butterflies, the 45-term product, accumulation) and the recomputed
+        # halo rows and layers (x 1.25), each one double-single operation here
+        compute_bound["fine_apply_f64"] = {"share": kernels["fine_apply_f64"]["share"], "arith": "double-single",
+                                           "fp64_equiv_gops": round(171 * 1.25 * nn / (ms / la / 1000.0) / 1e9, 1)}
     if "coarse_factor" in prof and prof["coarse_factor"][0]:
         q = 2 ** (a.nl - 1)
         nzc, nyc = shape[2] // q + 1, shape[1] // q + 1
         ncoarse = 3 * (shape[0] // q + 1) * nyc * nzc
         bw = 3 * (nzc * nyc + nyc + 1) + 2
         la, ms = prof["coarse_factor"]  # two timed scopes per factorisation: band assembly, factor
-        fp64_bound["coarse_factor"] = {"share": kernels["coarse_factor"]["share"],
-                                       "gfma": round(ncoarse * bw * bw / 2 / 1e9, 2),
-                                       "fp64_gfma_per_s": round(ncoarse * bw * bw / 2 / (2 * ms / la / 1000.0) / 1e9, 1)}
+        compute_bound["coarse_factor"] = {"share": kernels["coarse_factor"]["share"], "arith": "double-single",
+                                          "gfma": round(ncoarse * bw * bw / 2 / 1e9, 2),
+                                          "gfma_per_s": round(ncoarse * bw * bw / 2 / (2 * ms / la / 1000.0) / 1e9, 1)}
     launches = sum(v[0] for k, v in prof.items())
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms_a / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 V-cycle / f64 CG", "data": "synthetic",
-        "config": {"workload": "SIMP cantilever %s -l %d, volfrac 0.2, rmin 1.5, mixed (FP32 V-cycle, FP64 CG "
-                               "and coarse Cholesky)" % (a.shape, a.nl),
+        "dtype": "f32 V-cycle; f64 CG vectors, dots and coarse sweeps; double-single (2 x f32) CG matvec and "
+                 "coarse factor", "data": "synthetic",
+        "config": {"workload": "SIMP cantilever %s -l %d, volfrac 0.2, rmin 1.5, mixed (FP32 V-cycle; FP64 CG "
+                               "vectors; double-single CG matvec and coarse factor)" % (a.shape, a.nl),
                    "elements": shape[0] * shape[1] * shape[2], "dofs": 3 * (shape[0] + 1) * (shape[1] + 1) * (shape[2] + 1),
                    "design_iterations": "%d..%d" % (W + 1, W + K), "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (129 MB): fine vectors are %d MB each" %
@@ -477,7 +482,7 @@ def main():
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * shape[0] * shape[1] * shape[2],
                 "d2h_bytes_per_step": 2 * 8 * shape[0] * shape[1] * shape[2] + 8 * 6},
         "roofline": roofline,
-        "fp64_bound": fp64_bound,
+        "compute_bound": compute_bound,
         "kernels": kernels,
         "gpu_launches": launches,
         "clocks": clk,

@@ -39,7 +39,9 @@ typedef enum {
 
 typedef enum {
   TP_FP64 = 0, /* everything FP64: the drop-in form of the reference's path */
-  TP_MIXED = 1 /* FP32 V-cycle and smoother; FP64 CG, dots, update, coarse Cholesky */
+  TP_MIXED = 1 /* FP32 V-cycle and smoother; FP64 CG vectors, dots, updates and coarse sweeps;
+                  double-single CG matvec and coarse factor (tp_set_fine_arith,
+                  tp_set_coarse_arith switch those to FP64) */
 } tp_precision;
 
 typedef struct tp_ctx tp_ctx;
@@ -110,8 +112,8 @@ tp_status tp_reference_load(int nelx, int nely, int nelz, double* F_host);
 tp_status tp_fixed_dofs(const tp_ctx* c, int level, long* out_host, long* count);
 
 /* Builds every level's operator for the current xPhys: E(xPhys), inverse
- * Jacobi diagonals, assembled stencils of levels >= 1, and the FP64 band
- * Cholesky factor of the coarsest level (stencil_solvers.c:283-302). */
+ * Jacobi diagonals, assembled stencils of levels >= 1, and the band Cholesky
+ * factor of the coarsest level on FP64 storage (stencil_solvers.c:283-302). */
 tp_status tp_assemble(tp_ctx* c);
 
 /* Operators on device vectors of level `level`.

@@ -51,7 +51,8 @@ enum Scalar {
   S_COUNT
 };
 
-// The coarsest-level direct solver: band Cholesky in FP64 (tp_cholesky.cu).
+// The coarsest-level direct solver: band Cholesky on FP64 storage, FP64 or
+// double-single arithmetic (tp_cholesky.cu).
 // Its status word (Coarse::info) holds the first non-positive pivot's column
 // + 1, or'ed with kCoarseWaitGaveUp if a bounded wait inside the factor gave up.
 constexpr int kCoarseWaitGaveUp = 1 << 30;

@@ -63,6 +63,18 @@ def test_create_rejects_bad_arguments(lib, field, value):
     assert not ctx.value
 
 
+@pytest.mark.parametrize("setter", ["tp_set_fine_variant", "tp_set_fine_arith", "tp_set_coarse_solve_variant",
+                                    "tp_set_coarse_arith"])
+def test_selectors_reject_bad_arguments(lib, setter):
+    """The kernel and arithmetic selectors check their arguments before any
+    CUDA call: no context, or a choice other than 0 and 1, is TP_ERR_ARG."""
+    f = getattr(lib, setter)
+    f.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    assert f(None, 0) == 1
+    assert f(None, 1) == 1
+    assert f(None, 2) == 1
+
+
 def test_status_strings(lib):
     assert lib.tp_status_string(0) == b"ok"
     assert lib.tp_status_string(4) == b"coarse matrix not positive definite"

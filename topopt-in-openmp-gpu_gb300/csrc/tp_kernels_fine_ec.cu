@@ -316,9 +316,10 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
       xrow(k0 - 1, Xp);
 #pragma unroll
       for (int a = 0; a < 12; a++) accp[a] = A(0);
-      // Unrolled, the double-single body (each operation 7 to 11 FP32
-      // instructions) outgrows the instruction cache: it stays a loop, and
-      // the carries and moduli it indexes by row live in local memory.
+      // Unrolled, the double-single body (each operation 4 to 8 FP32
+      // instructions, ~2.4k per row) outgrows the instruction cache: it stays
+      // a loop, and the carries and moduli it indexes by row live in local
+      // memory.
       auto row_step = [&](int q) {
         const int ek = k0 - 1 + q;
         xrow(ek + 1, Xn);

@@ -21,9 +21,12 @@
 //            block step).
 // The mixed form runs the single-launch factor and the block inverses in
 // double-single arithmetic (tp_dsf.cuh) on the same FP64 storage: its V-cycle
-// is FP32, and FP64 instructions are what the chain of 32-column steps waits
-// on. The sweeps stay FP64: their phases wait on grid barriers and L2 reads,
-// not on their few multiply-adds.
+// is FP32, so the last bits of FP64 buy its coarse correction nothing, while
+// FP64 instructions hold the FP64 unit ~67 cycles each (at 256x128x128 the
+// factor takes 28 ms instead of 33, the inverses 2.2 ms instead of 5.2; the
+// chain's serial pivot work and hand-offs then bound the factor). The sweeps
+// stay FP64: their phases wait on grid barriers and L2 reads, not on their
+// few multiply-adds.
 #include <algorithm>
 #include <type_traits>
 

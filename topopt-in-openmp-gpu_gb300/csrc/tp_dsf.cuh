@@ -17,7 +17,7 @@ namespace tp {
 // two-sum of the high parts and adds the low parts and the two-sum's error
 // in FP32; a * b takes the exact product of the high parts (an FMA gives its
 // error) plus the cross terms. Both are left unnormalised (l is not folded
-// back into h), which keeps the bounds at ~2^-46 (|a| + |b|) and ~2^-46 |a| |b|
+// back into h), which keeps the bounds at ~2^-45 (|a| + |b|) and ~2^-45 |a| |b|
 // -- l only ever holds rounding-sized terms -- for 8 and 4 instructions
 // instead of 11 and 7; the sum h + l is formed in FP64 once, on output.
 // The _rn intrinsics keep the compiler from contracting the error terms.
@@ -48,8 +48,11 @@ __device__ __forceinline__ Dsf& operator-=(Dsf& a, Dsf b) { return a = a - b; }
 
 // double -> double-single with integer operations only (the FP64 pipe stays
 // free): h keeps the sign, the exponent and the leading 23 stored mantissa
-// bits (truncated), l the remaining 29 bits rounded to 24. Magnitudes below
-// FP32's normal range become 0, magnitudes above it infinity, NaN stays NaN.
+// bits (truncated), l the remaining 29 bits rounded to 24, scaled by
+// 2^-52 * 2^(e-1023) (two normal factors; one factor 2^(e-1075) would
+// underflow below |v| = 2^-74). Within 2^-47 |v| down to |v| ~ 2^-102,
+// where l turns subnormal; magnitudes below FP32's normal range become 0,
+// above it infinity, NaN stays NaN.
 __device__ __forceinline__ Dsf ds_from(double v) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(v);
   const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
@@ -62,8 +65,8 @@ __device__ __forceinline__ Dsf ds_from(double v) {
   }
   const float h = __uint_as_float(sg | ((unsigned)(e - 896) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
   // the low 29 mantissa bits carry weight 2^(e - 1023 - 52)
-  const float sc = e >= 949 ? __uint_as_float((unsigned)(e - 948) << 23) : 0.f;
-  const float l = __fmul_rn(__int2float_rn((int)(lw & 0x1fffffffu)), sc);
+  const float l = __fmul_rn(__fmul_rn(__int2float_rn((int)(lw & 0x1fffffffu)), 0x1p-52f),
+                            __uint_as_float((unsigned)(e - 896) << 23));
   return Dsf(h, sg ? -l : l);
 }
 __device__ __forceinline__ double ds_to(Dsf a) { return (double)a.h + (double)a.l; }
@@ -71,7 +74,8 @@ __device__ __forceinline__ double ds_to(Dsf a) { return (double)a.h + (double)a.
 // 1/sqrt(d): the FP32 estimate h = rsqrtf(d) refined by one Newton step for
 // the reciprocal square root, r = h + h (1 - d h^2) / 2, with 1 - d h^2
 // formed from the exact square of h and d's two parts (1 - p is exact for
-// p near 1). From FP32's ~2^-23 the step leaves ~2^-44 relative error.
+// p near 1). From rsqrtf's few-ulp estimate the step leaves under 2^-42
+// relative error.
 __device__ __forceinline__ Dsf ds_rsqrt(Dsf d) {
   const float x = __fadd_rn(d.h, d.l);
   const float h = rsqrtf(x);

@@ -205,6 +205,15 @@ tp_status tp_set_coarse_arith(tp_ctx* c, int arith);
  * every such wait runs out. The factor or solve then reports TP_ERR_TIMEOUT
  * and the context stays usable; (0, 0) restores the defaults. */
 tp_status tp_fault_coarse_barrier(tp_ctx* c, long spin, int missing);
+/* Failure detection of the set-up (host-side fault injection, for tests; no
+ * counterpart in the reference, which checks no allocation): with k > 0, the
+ * k-th device or pinned-host allocation the library makes from now on fails
+ * as if cudaMalloc had returned cudaErrorMemoryAllocation, without calling it;
+ * k = 0 switches the injection off. tp_create then returns TP_ERR_ALLOC with
+ * the context's message set, and tp_destroy of that context frees what was
+ * allocated. Returns the number of the library's allocations currently live
+ * (every context's), so a test can check that nothing is left behind. */
+long tp_fault_alloc(long k);
 /* Times the element-centric kernel's launch shapes (z groups per CTA, x
  * chunks) for each precision and fused mode on the context's grid and keeps
  * the fastest. It overwrites the solver work vectors (not F, U, x, xPhys):
@@ -227,6 +236,21 @@ tp_status tp_multiload(int nelx, int nely, int nelz, int ncase, int nload, unsig
  * reference for one load; 1 = the graph launch always; 2 = the host-driven
  * loop always (every kernel then shows in the tp_profile_* timings). */
 tp_status tp_set_graph_solve(tp_ctx* c, int on);
+
+/* How tp_design_iteration drives one iteration (no counterpart in the
+ * reference, whose loop waits on the device ~55 times per iteration:
+ * stencil_optimization.c:148-189, gpu_definitions.c:94-157):
+ * on = 1 (default) with a single host wait, at the iteration's end -- the CG
+ * loop is one graph launch (a conditional while node, also for one load), the
+ * volume and the constraint value stay on the device, the OC bisection is one
+ * graph launch (a conditional while node over batches of 8 steps, capped at
+ * 240 steps), and the coarse factor's status word comes back with the
+ * scalars; on = 0 host-driven as the reference (one residual read per CG
+ * iteration for one load, the volume read before the OC update, the
+ * bisection checked every 24 steps). Both give the same bits. With
+ * tp_profile_enable on, iterations run host-driven so that every kernel is
+ * timed. */
+tp_status tp_set_device_loop(tp_ctx* c, int on);
 
 /* Checkpoint/restart of the loop state (no counterpart in the reference):
  * x, xPhys, U and F (all load cases) with the grid, level count, load-case
@@ -271,17 +295,22 @@ tp_status tp_oc_bisect(tp_ctx* c, long n, const double* x_dev, const double* dv_
 
 /* Density-filter adjoint v <- H (v / Hs) without any device allocation and
  * without a context; it has no counterpart in the reference. It is for callers
- * that cannot call cudaMalloc: work recorded while a CUDA stream is being
- * captured into a graph (allocation is not allowed during capture), and
- * applications whose device memory belongs to another allocator or runtime.
- * The caller passes v (device, nelx*nely*nelz doubles, overwritten in place)
- * and a cudaStream_t (NULL = the default stream); the work is queued on that
- * stream and the call returns without waiting. The intermediate v/Hs lives in
- * a fixed 16 MiB device array compiled into the library, so grids above
+ * that cannot call cudaMalloc: applications that reserve the GPU's memory as
+ * their own arena or pool and forbid linked libraries to allocate or free
+ * device memory (an outside allocation can exhaust or fragment the arena, and
+ * cudaFree waits for the whole device), and loops with a fixed time budget
+ * that cannot absorb an allocation's latency. The caller passes v (device,
+ * nelx*nely*nelz doubles, overwritten in place) and a cudaStream_t (NULL = the
+ * default stream); the work is queued on that stream and the call returns
+ * without waiting. The intermediate v/Hs lives in a fixed 16 MiB device array
+ * compiled into the library, so grids above
  * tp_filter_T_noalloc_max_elements() elements (2^21) are rejected with
- * TP_ERR_ARG. The first call on a device looks up that array's device address
- * (cudaGetSymbolAddress) and should come before any stream capture. All calls
- * share the array: calls that overlap on the GPU race. */
+ * TP_ERR_ARG, as are a non-positive or non-finite rmin. The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress) and
+ * should come before any stream capture. All calls share the array, which
+ * keeps the last call's contents: calls that overlap on the GPU race. A launch
+ * failure returns TP_ERR_CUDA; an error left pending by the caller's own
+ * earlier work is neither reported nor cleared. */
 tp_status tp_filter_T_noalloc(int nelx, int nely, int nelz, double rmin, double* v_dev, void* stream);
 long tp_filter_T_noalloc_max_elements(void);
 

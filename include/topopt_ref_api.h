@@ -189,6 +189,14 @@ void getC(MTYPE C[6][6], const MTYPE nu);
 void getB(MTYPE B[6][24], MTYPE *jdet, const MTYPE iso[3], const MTYPE xe[24]);
 void getKEsubspace(MTYPE *KEarray, const MTYPE nu, const int l);
 
+/* No counterpart in the reference: bytes the entry points above have copied
+ * host -> device (*h2d) and device -> host (*d2h) since the library was
+ * loaded or last reset (reset != 0 clears the counts after reading them).
+ * Every GPU-backed entry point copies its host arrays in and out at each
+ * call; TOPOPT_PRECISION=mixed in the environment selects the mixed form
+ * (FP32 V-cycle, FP64 CG) for all of them, the default being FP64. */
+void topopt_ref_transfer_bytes(long *h2d, long *d2h, int reset);
+
 #ifdef __cplusplus
 }
 #endif

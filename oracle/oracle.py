@@ -355,3 +355,58 @@ class Reference:
         hist = {"c": hc[:loops], "vol": hv[:loops], "change": hch[:loops],
                 "relres": hr[:loops], "cgiters": hcg[:loops].astype(np.int64)}
         return loops, hist, xp, u
+
+
+class ReferenceBench:
+    """Timing samples of the reference's own design iteration (oracle/_ref,
+    ref_bench_* in oracle/ref_driver.c): the state of its loop on one grid,
+    and the seconds of the iteration's fixed part (assembly, diagonals,
+    coarse factor, initial residual, one CG iteration), of one more CG
+    iteration and of the design update. A design iteration with n CG
+    iterations costs fixed + (n - 1) * cg + design."""
+
+    def __init__(self, nelx, nely, nelz, nl, volfrac, rmin, flavour=64):
+        path = os.path.join(HERE, "_ref", "libref%d.so" % flavour)
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        L = ctypes.CDLL(path)
+        V = ctypes.c_void_p
+        L.ref_bench_create.restype = V
+        L.ref_bench_create.argtypes = [ctypes.c_int] * 4 + [ctypes.c_float, ctypes.c_float]
+        L.ref_bench_destroy.argtypes = [V]
+        for f in ("ref_bench_fixed", "ref_bench_cg"):
+            getattr(L, f).restype = ctypes.c_double
+            getattr(L, f).argtypes = [V]
+        L.ref_bench_design.restype = ctypes.c_double
+        L.ref_bench_design.argtypes = [V, _D]
+        L.ref_bench_kernels.argtypes = [V, _D]
+        self.L = L
+        self.path = path
+        self.h = L.ref_bench_create(nelx, nely, nelz, nl, volfrac, rmin)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ref_bench_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def fixed(self):
+        return self.L.ref_bench_fixed(self.h)
+
+    def cg(self):
+        return self.L.ref_bench_cg(self.h)
+
+    def design(self):
+        c = np.zeros(1)
+        t = self.L.ref_bench_design(self.h, _p(c))
+        return t, float(c[0])
+
+    KERNELS = ("fine_matvec", "level1_matvec", "restrict_0", "prolong_0", "inv_diag_0", "compliance",
+               "filter", "filter_T")
+
+    def kernels_ms(self):
+        ms = np.zeros(len(self.KERNELS))
+        self.L.ref_bench_kernels(self.h, _p(ms))
+        return dict(zip(self.KERNELS, (float(v) for v in ms)))

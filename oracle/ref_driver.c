@@ -23,6 +23,9 @@
 #include "stencil_solvers.h"
 #include "stencil_utility.h"
 
+#include <omp.h>
+#include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 typedef struct {
@@ -450,6 +453,10 @@ int ref_run(int nelx, int nely, int nelz, float volfrac_f, float rmin_f, int nl,
   unsigned int loop = 0;
   float change = 1;
   DTYPE vol = 0.0;
+  /* REF_VERBOSE=1 prints one progress line per design iteration to stderr,
+   * the fields of the reference's verbose line (stencil_optimization.c:173-181) */
+  const int verbose = getenv("REF_VERBOSE") != NULL;
+  const double t0 = omp_get_wtime();
   while ((change > 1e-2) && (loop < (unsigned)max_iterations)) {
     loop++;
     int cgiter;
@@ -469,6 +476,11 @@ int ref_run(int nelx, int nely, int nelz, float volfrac_f, float rmin_f, int nl,
     hist_change[loop - 1] = change;
     hist_cg[loop - 1] = cgiter;
     hist_relres[loop - 1] = cgres;
+    if (verbose) {
+      fprintf(stderr, "It.:%4u Obj.:%.17g Vol.:%.6f ch.:%.4f relres: %.4e iters: %4d time: %.3f\n",
+              loop, (double)cc, (double)vol, change, cgres, cgiter, omp_get_wtime() - t0);
+      fflush(stderr);
+    }
   }
   if (xphys_out) el_from_padded(c, xPhys, xphys_out);
   if (u_out) {
@@ -486,4 +498,171 @@ int ref_run(int nelx, int nely, int nelz, float volfrac_f, float rmin_f, int nl,
   free(F); free(U); free(dc); free(dv); free(x); free(xPhys); free(xnew);
   ref_destroy(c);
   return (int)loop;
+}
+
+/* ---- timing samples of the reference's own design iteration ----
+ * For the CPU baseline: the state of top3dmgcg (stencil_optimization.c:
+ * 22-137) on one grid, and the parts of one design iteration timed with
+ * omp_get_wtime around the reference's own calls only (no layout
+ * conversion inside a timed span):
+ *   ref_bench_fixed   solveStateMG_halo with its CG loop cut to one
+ *                     iteration (a tolerance every residual meets): the
+ *                     per-iteration assembly, diagonals and coarse factor,
+ *                     the initial residual and one CG iteration
+ *   ref_bench_cg      one more iteration of that CG loop, the body of
+ *                     stencil_solvers.c:340-390 on the reference's functions
+ *   ref_bench_design  the rest of the iteration, stencil_optimization.c:
+ *                     157-178 (volume, compliance and sensitivities, filter
+ *                     adjoint, OC update, change, filter)
+ * A design iteration with n CG iterations costs fixed + (n - 1) cg + design. */
+/* stencil_solvers.c:129-133; the reference's headers do not declare it */
+void VcyclePreconditioner(const struct gpuGrid *gpu_gc, const DTYPE *x, const int nl, const int l,
+                          MTYPE **const invD, struct CoarseSolverData *bottomSolverData,
+                          const struct CSRMatrix *coarseMatrices, CTYPE omega, const int nswp, CTYPE **r,
+                          CTYPE **z, CTYPE **d);
+
+typedef struct {
+  RefCtx *c;
+  struct SolverDataBuffer sd;
+  CTYPE *F;
+  STYPE *U;
+  DTYPE *dc, *dv, *x, *xPhys, *xnew;
+  DTYPE volfrac, rmin;
+  CTYPE rhoold;
+  size_t nelem;
+} RefBench;
+
+void *ref_bench_create(int nelx, int nely, int nelz, int nl, float volfrac_f, float rmin_f) {
+  RefBench *b = calloc(1, sizeof(RefBench));
+  b->c = ref_create(nelx, nely, nelz, nl);
+  struct gridContext *g = &b->c->gc;
+  b->volfrac = volfrac_f;
+  b->rmin = rmin_f;
+  b->nelem = nelem_padded(b->c);
+  allocateZeroPaddedStateField(*g, 0, &b->F);
+  allocateZeroPaddedStateField_STYPE(*g, 0, &b->U);
+  cantilever_load(g, b->F);
+  b->dc = calloc(b->nelem, sizeof(DTYPE));
+  b->dv = malloc(sizeof(DTYPE) * b->nelem);
+  b->x = calloc(b->nelem, sizeof(DTYPE));
+  b->xPhys = calloc(b->nelem, sizeof(DTYPE));
+  b->xnew = calloc(b->nelem, sizeof(DTYPE));
+  for (size_t q = 0; q < b->nelem; q++) b->dv[q] = 1.0;
+  for (int i = 1; i < g->nelx + 1; i++)
+    for (int k = 1; k < g->nelz + 1; k++)
+      for (int j = 1; j < g->nely + 1; j++) {
+        const size_t idx = (size_t)i * (g->wrapy - 1) * (g->wrapz - 1) + (size_t)k * (g->wrapy - 1) + j;
+        b->x[idx] = b->volfrac;
+        b->xPhys[idx] = b->volfrac;
+      }
+  allocateSolverData(*g, nl, &b->sd);
+  initializeCholmod(*g, nl - 1, &b->sd.bottomSolver, b->sd.coarseMatrices[nl - 1]);
+  applyDensityFilterGradient(*g, b->rmin, b->dv);
+  return b;
+}
+
+void ref_bench_destroy(void *p) {
+  RefBench *b = p;
+  const int nl = b->c->nl;
+  finishCholmod(b->c->gc, nl - 1, &b->sd.bottomSolver, b->sd.coarseMatrices[nl - 1], 0);
+  freeSolverData(&b->sd, nl);
+  free(b->F); free(b->U); free(b->dc); free(b->dv); free(b->x); free(b->xPhys); free(b->xnew);
+  ref_destroy(b->c);
+  free(b);
+}
+
+double ref_bench_fixed(void *p) {
+  RefBench *b = p;
+  int it = 0;
+  float rr = 0;
+  const double t0 = omp_get_wtime();
+  solveStateMG_halo(&b->c->gpu, b->xPhys, 4, b->c->nl, (CTYPE)1e30, &b->sd, &it, &rr, b->F, b->U);
+  const double t = omp_get_wtime() - t0;
+  /* rho of the iteration just taken, the next iteration's rhoold */
+  b->rhoold = innerProduct(b->sd.r, b->sd.z, 3 * (size_t)b->c->gc.wrapx * b->c->gc.wrapy * b->c->gc.wrapz);
+  return t;
+}
+
+double ref_bench_cg(void *p) {
+  RefBench *b = p;
+  struct SolverDataBuffer *data = &b->sd;
+  const struct gridContext *gc = &b->c->gc;
+  const uint_fast32_t ndof = 3 * gc->wrapx * gc->wrapy * gc->wrapz;
+  CTYPE *r = data->r, *pp = data->p, *q = data->q, *z = data->z;
+  STYPE *u = b->U;
+  const MTYPE omega = 0.6;
+  const double t0 = omp_get_wtime();
+  VcyclePreconditioner(&b->c->gpu, b->xPhys, b->c->nl, 0, data->invD, &data->bottomSolver,
+                       data->coarseMatrices, omega, 4, data->rmg, data->zmg, data->dmg);
+  const CTYPE rho = innerProduct(r, z, ndof);
+  const CTYPE beta = rho / b->rhoold;
+#pragma omp parallel for schedule(static)
+  for (uint_fast32_t i = 0; i < ndof; i++) pp[i] = beta * pp[i] + z[i];
+  applyStateOperator_stencil(&b->c->gpu.target[0], b->xPhys, pp, q);
+  const CTYPE dpr = innerProduct(pp, q, ndof);
+  const CTYPE alpha = rho / dpr;
+  b->rhoold = rho;
+#pragma omp parallel for schedule(static)
+  for (uint_fast32_t i = 0; i < ndof; i++) u[i] += (STYPE)(alpha * pp[i]);
+#pragma omp parallel for schedule(static)
+  for (uint_fast32_t i = 0; i < ndof; i++) r[i] -= alpha * q[i];
+  volatile CTYPE rn = norm(r, ndof);
+  (void)rn;
+  return omp_get_wtime() - t0;
+}
+
+double ref_bench_design(void *p, double *c_out) {
+  RefBench *b = p;
+  struct gridContext *g = &b->c->gc;
+  DTYPE cc = 0.0;
+  const double t0 = omp_get_wtime();
+  DTYPE vol = compute_volume(*g, b->xPhys);
+  getComplianceAndSensetivity_halo(&b->c->gpu.target[0], b->xPhys, b->U, &cc, b->dc);
+  applyDensityFilterGradient(*g, b->rmin, b->dc);
+  vol /= (DTYPE)(g->nelx * g->nely * g->nelz);
+  const DTYPE gv = vol - b->volfrac;
+  update_solution(b->x, b->xnew, b->dv, b->dc, (int)b->nelem, gv);
+  volatile float change = compute_change(b->x, b->xnew, (int)b->nelem);
+  (void)change;
+  applyDensityFilter(*g, b->rmin, b->x, b->xPhys);
+  const double t = omp_get_wtime() - t0;
+  if (c_out) *c_out = (double)cc;
+  return t;
+}
+
+/* milliseconds of single calls of the reference's kernels on the bench's
+ * state: [0] fine matvec, [1] level-1 matvec, [2] restriction 0->1,
+ * [3] prolongation 1->0, [4] inverse diagonal of level 0, [5] compliance and
+ * sensitivities, [6] density filter, [7] filter adjoint */
+void ref_bench_kernels(void *p, double *ms) {
+  RefBench *b = p;
+  struct gridContext *g = &b->c->gc;
+  const struct gpuNode *node = &b->c->gpu.target[0];
+  struct SolverDataBuffer *d = &b->sd;
+  double t;
+  DTYPE cc = 0;
+  t = omp_get_wtime();
+  applyStateOperator_stencil(node, b->xPhys, d->p, d->q);
+  ms[0] = 1e3 * (omp_get_wtime() - t);
+  t = omp_get_wtime();
+  applyStateOperatorSubspace_halo(node, 1, b->xPhys, d->zmg[1], d->dmg[1]);
+  ms[1] = 1e3 * (omp_get_wtime() - t);
+  t = omp_get_wtime();
+  projectToCoarserGrid_halo(node, 0, d->r, d->rmg[1]);
+  ms[2] = 1e3 * (omp_get_wtime() - t);
+  t = omp_get_wtime();
+  projectToFinerGrid_halo(node, 0, d->zmg[1], d->dmg[0]);
+  ms[3] = 1e3 * (omp_get_wtime() - t);
+  t = omp_get_wtime();
+  assembleInvertedMatrixDiagonalSubspace_halo(node, b->xPhys, 0, d->invD[0]);
+  ms[4] = 1e3 * (omp_get_wtime() - t);
+  t = omp_get_wtime();
+  getComplianceAndSensetivity_halo(node, b->xPhys, b->U, &cc, b->dc);
+  ms[5] = 1e3 * (omp_get_wtime() - t);
+  t = omp_get_wtime();
+  applyDensityFilter(*g, b->rmin, b->x, b->xnew);
+  ms[6] = 1e3 * (omp_get_wtime() - t);
+  t = omp_get_wtime();
+  applyDensityFilterGradient(*g, b->rmin, b->dc);
+  ms[7] = 1e3 * (omp_get_wtime() - t);
 }

@@ -7,7 +7,9 @@ It loads oracle/_ref/libref64.so (the reference's sources, FP64 typedefs,
 CHOLMOD/CBLAS stand-ins) through oracle/ref_driver.c and records inputs and
 outputs in the canonical unpadded layout (see oracle/topopt_oracle.h). The
 fixtures are the pin for the oracle restatement and for the CUDA path.
---big adds the 128x64x64 (-l 4) 20-iteration history (about 20 minutes).
+--big adds the 128x64x64 (-l 4) 20-iteration history (about 20 minutes);
+--config4 writes only the 256x128x128 (-l 4) history (hours), with samples of
+the final design instead of the whole field.
 """
 import os
 import sys
@@ -86,6 +88,18 @@ def history(shape, nl, iters, flavour=64):
     return h
 
 
+def history_compact(shape, nl, iters):
+    """The 20-iteration history of a grid too large to store its fields:
+    compliance, volume, change, relres and CG counts in full, and of the final
+    xPhys its sum, its 2-norm and 256 seeded samples (default_rng(11))."""
+    h = history(shape, nl, iters)
+    xp = h.pop("xphys")
+    idx = np.sort(np.random.default_rng(11).choice(xp.size, 256, replace=False))
+    h.update({"xphys_idx": idx, "xphys_val": xp[idx], "xphys_sum": xp.sum(),
+              "xphys_norm": np.linalg.norm(xp)})
+    return h
+
+
 def adjoint(shape=(64, 32, 32), nl=4):
     """Sensitivities of the reference on i.i.d. U[0.01, 1] design variables
     (numpy default_rng(0)) through the density filter, rmin 1.5 and 2.5: the
@@ -127,6 +141,11 @@ def ke_fixture():
 
 
 def main():
+    if "--config4" in sys.argv:
+        # the headline grid, 256x128x128 -l 4, 20 iterations (hours on 8 cores)
+        np.savez_compressed(os.path.join(HERE, "history_256x128x128_l4.npz"),
+                            **history_compact((256, 128, 128), 4, 20))
+        return
     big = "--big" in sys.argv
     np.savez_compressed(os.path.join(HERE, "ke.npz"), **ke_fixture())
     np.savez_compressed(os.path.join(HERE, "kernels_16x8x8_l3.npz"), **kernels((16, 8, 8), 3, solve_after=0))

@@ -159,6 +159,30 @@ def test_csr_pattern_matches_reference(grid):
     assert np.array_equal(np.ctypeslib.as_array(M.colIndex, shape=(nnz,)), ci)
 
 
+@pytest.mark.skipif(not os.path.exists(REF64), reason="reference not built in this checkout")
+@pytest.mark.parametrize("flavour", [32, 64])
+@pytest.mark.parametrize("shape", [(16, 8, 8), (12, 6, 10)])
+def test_vtk_files_match_reference_bytes(tmp_path, flavour, shape):
+    """The two .vtu writers (stencil_optimization.c:399-598) of the drop-in
+    library and of the reference's own build, given the same padded density
+    array, write the same bytes (host code only: no GPU call)."""
+    tp.load()
+    ours = ctypes.CDLL(os.path.join(tp.PKG, "libtopopt_ref%d.so" % flavour))
+    ref = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libref%d.so" % flavour))
+    dt = np.float64 if flavour == 64 else np.float32
+    dims = padded_dims(*shape, 0)
+    rho = np.random.default_rng(9).uniform(0.0, 1.0, (dims[3] - 1) * (dims[4] - 1) * (dims[5] - 1)).astype(dt)
+    for fn in ("writeDensityVtkFile", "writeDensityVtkFileWithHalo"):
+        files = []
+        for tag, lib in (("ours", ours), ("ref", ref)):
+            f = getattr(lib, fn)
+            f.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_char_p]
+            path = tmp_path / ("%s_%s.vtu" % (fn, tag))
+            f(shape[0], shape[1], shape[2], ptr(rho), os.fsencode(str(path)))
+            files.append(path.read_bytes())
+        assert len(files[0]) > 1000 and files[0] == files[1], fn
+
+
 # ---------------------------------------------------------------- GPU ----
 @pytest.mark.gpu
 def test_operators_through_reference_signatures(grid, cuda):

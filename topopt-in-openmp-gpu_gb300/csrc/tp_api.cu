@@ -2,6 +2,7 @@
 // V-cycle, PCG and the design loop, all stream-ordered on one CUDA stream
 // of one GPU.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -13,6 +14,45 @@ using namespace tp;
 
 namespace tp {
 
+namespace {
+std::atomic<long> g_live_allocs{0};
+std::atomic<long> g_fault_countdown{0};  // > 0: allocations left before the one that fails
+bool fault_now() {
+  long k = g_fault_countdown.load();
+  while (k > 0) {
+    if (g_fault_countdown.compare_exchange_weak(k, k - 1)) return k == 1;
+  }
+  return false;
+}
+}  // namespace
+
+cudaError_t dev_malloc(void** p, size_t bytes) {
+  *p = nullptr;
+  if (fault_now()) return cudaErrorMemoryAllocation;
+  const cudaError_t e = cudaMalloc(p, bytes);
+  if (e == cudaSuccess) g_live_allocs++;
+  else *p = nullptr;
+  return e;
+}
+void dev_free(void* p) {
+  if (!p) return;
+  cudaFree(p);
+  g_live_allocs--;
+}
+cudaError_t host_malloc_pinned(void** p, size_t bytes) {
+  *p = nullptr;
+  if (fault_now()) return cudaErrorMemoryAllocation;
+  const cudaError_t e = cudaMallocHost(p, bytes);
+  if (e == cudaSuccess) g_live_allocs++;
+  else *p = nullptr;
+  return e;
+}
+void host_free_pinned(void* p) {
+  if (!p) return;
+  cudaFreeHost(p);
+  g_live_allocs--;
+}
+
 bool cuda_ok(tp_ctx* c, cudaError_t e, const char* what) {
   if (e == cudaSuccess) return true;
   c->err = std::string(what) + ": " + cudaGetErrorString(e);
@@ -23,7 +63,7 @@ template <typename T>
 static T* dalloc(tp_ctx* c, long n) {
   if (n <= 0) n = 1;
   T* p = nullptr;
-  if (cudaMalloc(&p, sizeof(T) * (size_t)n) != cudaSuccess) {
+  if (dev_malloc(&p, sizeof(T) * (size_t)n) != cudaSuccess) {
     c->err = "cudaMalloc of " + std::to_string(sizeof(T) * n) + " bytes failed";
     return nullptr;
   }
@@ -170,7 +210,10 @@ static void precondition(tp_ctx* c, const double* r, double* z, int nr = 1) {
 }
 
 // ---------------------------------------------------------------------------
-static tp_status assemble(tp_ctx* c) {
+// Enqueues the assembly of every level and the coarse factorisation; the
+// factor's status word is checked by assemble_status (or, in the design
+// iteration without host round trips, read once at the iteration's end).
+static void assemble_enqueue(tp_ctx* c) {
   compute_E(c);
   fine_inv_diag(c, c->invD[0]);
   if (mixed(c)) cast_d2f(c, c->L[0].ndof, c->invD[0], c->invDf[0]);
@@ -187,24 +230,35 @@ static tp_status assemble(tp_ctx* c) {
   }
   coarse_assemble(c);
   coarse_factor(c);
-  tp_status st = check(c);
-  if (st != TP_OK) return st;
-  int info = 0;
-  cudaMemcpyAsync(&info, c->coarse.info, sizeof(int), cudaMemcpyDeviceToHost, c->s);
-  st = sync_check(c);
-  if (st != TP_OK) return st;
-  c->assembled = true;
   for (int l = 0; l < TP_MAXL; l++) c->st_sub_valid[l] = false;
+}
+
+// the coarse factor's status word `info` -> the assembly's status
+static tp_status assemble_status(tp_ctx* c, int info) {
+  // the operators count as assembled only with a usable coarse factor: after
+  // a timeout or a non-positive pivot every later call assembles again (and
+  // reports the same status) instead of solving with the failed factor
+  c->assembled = false;
   if (info & kCoarseWaitGaveUp) {
-    c->assembled = false;
     c->note = "coarse Cholesky: a bounded wait gave up";
     return TP_ERR_TIMEOUT;
   }
   if (info != 0) {
-    c->err = "coarse Cholesky: non-positive pivot at column " + std::to_string(info - 1);
+    c->note = "coarse Cholesky: non-positive pivot at column " + std::to_string(info - 1);
     return TP_ERR_NOT_SPD;
   }
+  c->assembled = true;
   return TP_OK;
+}
+
+static tp_status assemble(tp_ctx* c) {
+  assemble_enqueue(c);
+  tp_status st = check(c);
+  if (st != TP_OK) return st;
+  cudaMemcpyAsync(c->h_info, c->coarse.info, sizeof(int), cudaMemcpyDeviceToHost, c->s);
+  st = sync_check(c);
+  if (st != TP_OK) return st;
+  return assemble_status(c, *c->h_info);
 }
 
 // PCG set-up: r = b - K u, |b|^2 per column, converged marks cleared
@@ -254,7 +308,7 @@ static tp_status pcg(tp_ctx* c, const double* b, double* u, int* iters, double* 
       *iters = it;
       *relres = rr;
       if (coarse_status(c) != TP_OK) return TP_ERR_TIMEOUT;
-      c->err = "CG: non-finite residual";
+      c->note = "CG: non-finite residual";
       return TP_ERR_NONFINITE;
     }
     if (rr < tol) {
@@ -320,14 +374,22 @@ long tp_ndof(const tp_ctx* c, int level) {
 long tp_nelem(const tp_ctx* c) { return c ? (long)c->L[0].ex * c->L[0].ey * c->L[0].ez : -1; }
 long tp_device_bytes(const tp_ctx* c) { return c ? c->mem_bytes : -1; }
 
+long tp_fault_alloc(long k) {
+  tp::g_fault_countdown.store(k > 0 ? k : 0);
+  return tp::g_live_allocs.load();
+}
+
 tp_status tp_sync(tp_ctx* c) {
   if (!c) return TP_ERR_ARG;
   return sync_check(c);
 }
 
+// frees everything the context holds and clears the pointers, so that a
+// second call (tp_destroy of a context whose tp_create failed) frees nothing
 static void destroy_buffers(tp_ctx* c) {
-  auto F = [](void* p) {
-    if (p) cudaFree(p);
+  auto F = [](auto*& p) {
+    dev_free(p);
+    p = nullptr;
   };
   for (int l = 0; l < TP_MAXL; l++) {
     F(c->d_ke[l]); F(c->d_kef[l]); F(c->d_mgc[l]); F(c->d_mgi[l]);
@@ -339,8 +401,16 @@ static void destroy_buffers(tp_ctx* c) {
   F(c->d_E); F(c->d_Ef); F(c->d_F); F(c->d_U);
   F(c->d_r); F(c->d_z); F(c->d_p); F(c->d_q);
   F(c->d_red); F(c->d_scal); F(c->d_flag); F(c->scratch_invD); F(c->d_fw); F(c->d_mom);
-  if (c->h_scal) cudaFreeHost(c->h_scal);
+  host_free_pinned(c->h_scal);
+  host_free_pinned(c->h_info);
+  c->h_scal = nullptr;
+  c->h_info = nullptr;
+  for (auto& e : c->it_ev) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
+  }
   graph_free(c);
+  oc_graph_free(c);
   coarse_free(c);
   prof_destroy(c);
 }
@@ -438,10 +508,14 @@ tp_status tp_create(const tp_params* p, tp_ctx** out) {
   const long nscal = (long)S_COUNT * p->nrhs;
   ok = ok && (c->d_red = dalloc<double>(c, red)) && (c->d_scal = dalloc<double>(c, nscal)) &&
        (c->d_flag = dalloc<int>(c, 4));
-  if (ok) ok = cuda_ok(c, cudaMallocHost(&c->h_scal, sizeof(double) * nscal), "cudaMallocHost");
+  if (ok) ok = cuda_ok(c, host_malloc_pinned((void**)&c->h_scal, sizeof(double) * nscal), "cudaMallocHost");
+  if (ok) ok = cuda_ok(c, host_malloc_pinned((void**)&c->h_info, sizeof(int) * 4), "cudaMallocHost");
+  if (ok) ok = cuda_ok(c, cudaEventCreate(&c->it_ev[0]), "cudaEventCreate") &&
+               cuda_ok(c, cudaEventCreate(&c->it_ev[1]), "cudaEventCreate");
   if (ok) {
     coarse_alloc(c);
-    ok = c->coarse.band && c->coarse.dinv && c->coarse.dinvT && c->coarse.lrow && c->coarse.vec && c->coarse.info;
+    ok = c->coarse.band && c->coarse.dinv && c->coarse.dinvT && c->coarse.lrow && c->coarse.vec && c->coarse.info &&
+         c->coarse.linv && !c->coarse.alloc_failed;
     if (!ok) c->err = "coarse solver allocation failed";
   }
   if (!ok) {
@@ -463,6 +537,11 @@ tp_status tp_create(const tp_params* p, tp_ctx** out) {
     cudaStreamSynchronize(c->s);
   }
   filter_hs(c, c->d_hs);
+  if (!c->d_fw) {
+    destroy_buffers(c);
+    *out = c;
+    return TP_ERR_ALLOC;
+  }
   ec_default_plans(c);
   c->fine_ds = c->coarse.ds = mixed(c) ? 1 : 0;
   tp_status st = sync_check(c);
@@ -624,7 +703,8 @@ tp_status tp_smooth(tp_ctx* c, int level, int nswp, double omega, const double* 
     std::swap(cur, nxt);
   }
   if (cur != u) cudaMemcpyAsync(u, cur, sizeof(double) * nd, cudaMemcpyDeviceToDevice, c->s);
-  return sync_check(c);
+  tp_status st = sync_check(c);
+  return st != TP_OK ? st : coarse_status(c);
 }
 
 tp_status tp_coarse_solve(tp_ctx* c, const double* rhs, double* x) {
@@ -645,7 +725,8 @@ tp_status tp_vcycle(tp_ctx* c, const double* r, double* z) {
     if (st != TP_OK) return st;
   }
   precondition(c, r, z);
-  return sync_check(c);
+  tp_status st = sync_check(c);
+  return st != TP_OK ? st : coarse_status(c);
 }
 
 tp_status tp_solve(tp_ctx* c, int* iters, double* relres) {
@@ -721,7 +802,7 @@ tp_status tp_volume(tp_ctx* c, double* vol) {
 tp_status tp_oc_update(tp_ctx* c, double g, double* change) {
   if (!c) return TP_ERR_ARG;
   if (oc_update(c, g) != 0) {
-    c->err = "OC bisection did not terminate";
+    c->note = "OC bisection did not terminate";
     return TP_ERR_TIMEOUT;
   }
   tp_status st = check(c);
@@ -749,12 +830,11 @@ tp_status tp_init_design(tp_ctx* c) {
   return sync_check(c);
 }
 
-tp_status tp_design_iteration(tp_ctx* c, tp_iter_info* info) {
-  if (!c) return TP_ERR_ARG;
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  cudaEventRecord(e0, c->s);
+// One design iteration with the host in the loop, as the reference drives it:
+// the CG loop reads the residual each iteration (for one load), the volume is
+// read before the OC update and the bisection is checked every 24 steps.
+static tp_status design_iteration_host(tp_ctx* c, tp_iter_info* info) {
+  cudaEventRecord(c->it_ev[0], c->s);
   int it = 0;
   double rr = 0;
   tp_status st = tp_solve(c, &it, &rr);
@@ -762,35 +842,97 @@ tp_status tp_design_iteration(tp_ctx* c, tp_iter_info* info) {
   double vol = 0;
   st = tp_volume(c, &vol);
   if (st != TP_OK) return st;
-  double comp = 0;
   int nb = 0;
   compliance(c, c->d_U, c->d_dc, &nb, c->p.nrhs);
   finish_sum(c, nb, S_C, 0);
   filter_adj(c, c->d_dc, c->d_xnew);
   const double g = vol - c->p.volfrac;
   if (oc_update(c, g) != 0) {
-    c->err = "OC bisection did not terminate";
+    c->note = "OC bisection did not terminate";
     return TP_ERR_TIMEOUT;
   }
   filter_fwd(c, c->d_x, c->d_xphys);
   c->assembled = false;
-  cudaEventRecord(e1, c->s);
+  cudaEventRecord(c->it_ev[1], c->s);
   cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, c->s);
   st = sync_check(c);
   if (st != TP_OK) return st;
-  comp = c->h_scal[S_C];
   float ms = 0;
-  cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  cudaEventElapsedTime(&ms, c->it_ev[0], c->it_ev[1]);
   if (info) {
-    info->c = comp;
+    info->c = c->h_scal[S_C];
     info->vol = vol;
     info->change = (double)(float)c->h_scal[S_CHANGE];
     info->cgiters = it;
     info->relres = rr;
     info->ms = ms;
   }
+  return TP_OK;
+}
+
+// The same iteration with one host wait, at its end: assembly and factor,
+// the CG loop (one graph launch), volume, constraint value, compliance,
+// filter adjoint, the OC bisection (one graph launch), change and filter are
+// all enqueued first; the scalars and the coarse factor's status word come
+// back together and are checked then. The arithmetic and its order are the
+// host-driven form's, so both give the same bits.
+static tp_status design_iteration_device(tp_ctx* c, tp_iter_info* info) {
+  cudaEventRecord(c->it_ev[0], c->s);
+  assemble_enqueue(c);
+  tp_status st = pcg_graph_enqueue(c);
+  if (st != TP_OK) return st;
+  int nb = 0;
+  volume_partials(c, c->d_xphys, &nb);
+  finish_sum(c, nb, S_VOL, 0);
+  constraint_from_volume(c);
+  compliance(c, c->d_U, c->d_dc, &nb, c->p.nrhs);
+  finish_sum(c, nb, S_C, 0);
+  filter_adj(c, c->d_dc, c->d_xnew);
+  if (!oc_update_graph(c)) {
+    c->err = "OC bisection graph: capture or instantiation failed";
+    return TP_ERR_CUDA;
+  }
+  filter_fwd(c, c->d_x, c->d_xphys);
+  cudaEventRecord(c->it_ev[1], c->s);
+  cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(double) * S_COUNT * c->p.nrhs, cudaMemcpyDeviceToHost, c->s);
+  cudaMemcpyAsync(c->h_info, c->coarse.info, sizeof(int), cudaMemcpyDeviceToHost, c->s);
+  st = sync_check(c);
+  if (st != TP_OK) return st;
+  // the factor's status first: a failed factor makes every later value moot
+  st = assemble_status(c, *c->h_info);
+  c->assembled = false;  // xPhys has changed
+  if (st != TP_OK) return st;
+  int it = 0;
+  double rr = 0;
+  st = pcg_graph_status(c, &it, &rr);
+  if (st != TP_OK && st != TP_ERR_NOT_CONVERGED) return st;
+  if (c->h_scal[S_OCDONE] == 0.0) {
+    c->note = "OC bisection did not terminate";
+    return TP_ERR_TIMEOUT;
+  }
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->it_ev[0], c->it_ev[1]);
+  if (info) {
+    info->c = c->h_scal[S_C];
+    info->vol = c->h_scal[S_VOL] / (double)tp_nelem(c);
+    info->change = (double)(float)c->h_scal[S_CHANGE];
+    info->cgiters = it;
+    info->relres = rr;
+    info->ms = ms;
+  }
+  return TP_OK;
+}
+
+tp_status tp_design_iteration(tp_ctx* c, tp_iter_info* info) {
+  if (!c) return TP_ERR_ARG;
+  // per-kernel timing needs every kernel launched from the host
+  if (c->device_loop && !c->prof) return design_iteration_device(c, info);
+  return design_iteration_host(c, info);
+}
+
+tp_status tp_set_device_loop(tp_ctx* c, int on) {
+  if (!c || on < 0 || on > 1) return TP_ERR_ARG;
+  c->device_loop = on;
   return TP_OK;
 }
 

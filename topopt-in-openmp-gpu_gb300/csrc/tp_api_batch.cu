@@ -78,8 +78,9 @@ static bool graph_build(tp_ctx* c, int nr) {
   return true;
 }
 
-// K U = F for the context's nrhs columns, warm start from U
-tp_status pcg_graph(tp_ctx* c, int* iters, double* relres) {
+// K U = F for the context's nrhs columns, warm start from U: set-up and the
+// graph launch, enqueued only
+tp_status pcg_graph_enqueue(tp_ctx* c) {
   const int nr = c->p.nrhs;
   if (!c->cg_exec || c->cg_exec_nr != nr) {
     if (!graph_build(c, nr)) return TP_ERR_CUDA;
@@ -87,12 +88,12 @@ tp_status pcg_graph(tp_ctx* c, int* iters, double* relres) {
   pcg_prologue(c, c->d_F, c->d_U, nr);
   cg_counter_reset_kernel<<<1, 1, 0, c->s>>>(c->d_scal);
   cudaGraphLaunch(c->cg_exec, c->s);
-  cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(double) * S_COUNT * nr, cudaMemcpyDeviceToHost, c->s);
-  cudaError_t e = cudaStreamSynchronize(c->s);
-  if (e != cudaSuccess) {
-    c->err = std::string("CG graph: ") + cudaGetErrorString(e);
-    return TP_ERR_CUDA;
-  }
+  return TP_OK;
+}
+
+// the outcome of the enqueued solve, from the scalars already copied into
+// h_scal (the caller has synchronised the stream)
+tp_status pcg_graph_status(tp_ctx* c, int* iters, double* relres) {
   if (!c->err.empty()) return TP_ERR_CUDA;
   if (coarse_status(c) != TP_OK) return TP_ERR_TIMEOUT;
   const double* s = c->h_scal;
@@ -100,10 +101,22 @@ tp_status pcg_graph(tp_ctx* c, int* iters, double* relres) {
   *iters = (int)s[S_IT] - 1;  // index of the last iteration, as the reference reports it
   *relres = (double)(float)rr;
   if (!std::isfinite(rr)) {
-    c->err = "CG: non-finite residual";
+    c->note = "CG: non-finite residual";
     return TP_ERR_NONFINITE;
   }
   return rr < c->p.cgtol ? TP_OK : TP_ERR_NOT_CONVERGED;
+}
+
+tp_status pcg_graph(tp_ctx* c, int* iters, double* relres) {
+  tp_status st = pcg_graph_enqueue(c);
+  if (st != TP_OK) return st;
+  cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(double) * S_COUNT * c->p.nrhs, cudaMemcpyDeviceToHost, c->s);
+  cudaError_t e = cudaStreamSynchronize(c->s);
+  if (e != cudaSuccess) {
+    c->err = std::string("CG graph: ") + cudaGetErrorString(e);
+    return TP_ERR_CUDA;
+  }
+  return pcg_graph_status(c, iters, relres);
 }
 
 }  // namespace tp

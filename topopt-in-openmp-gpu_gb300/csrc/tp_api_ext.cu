@@ -30,11 +30,11 @@ tp_status sync_status(tp_ctx* c) {
 const double* api_stencil(tp_ctx* c, int l) {
   if (c->assembled && c->st[l]) return c->st[l];
   if (!c->st_sub[l]) {
-    if (cudaMalloc(&c->st_sub[l], sizeof(double) * kStencilCoef * c->L[l].nnodes) != cudaSuccess) return nullptr;
+    if (dev_malloc(&c->st_sub[l], sizeof(double) * kStencilCoef * c->L[l].nnodes) != cudaSuccess) return nullptr;
     c->mem_bytes += 8L * kStencilCoef * c->L[l].nnodes;
   }
   if (!c->st_sub_valid[l]) {
-    if (!c->scratch_invD) cudaMalloc(&c->scratch_invD, sizeof(double) * c->L[0].ndof);
+    if (!c->scratch_invD) dev_malloc(&c->scratch_invD, sizeof(double) * c->L[0].ndof);
     compute_E(c);
     assemble_stencil<double>(c, l, c->d_E, c->d_ke[l], c->st_sub[l], c->scratch_invD);
     c->st_sub_valid[l] = true;
@@ -172,11 +172,11 @@ tp_status tp_download_stencil(tp_ctx* c, int level, int subspace, double* host) 
   if (!A) return TP_ERR_STATE;
   const long nc = 243L * c->L[level].nnodes;
   double* full = nullptr;
-  if (cudaMalloc(&full, sizeof(double) * nc) != cudaSuccess) return TP_ERR_ALLOC;
+  if (dev_malloc(&full, sizeof(double) * nc) != cudaSuccess) return TP_ERR_ALLOC;
   stencil_expand(c, level, A, full, (level >= 2 && !subspace) ? 1 : 0);
   cudaMemcpyAsync(host, full, sizeof(double) * nc, cudaMemcpyDeviceToHost, c->s);
   tp_status st = sync_status(c);
-  cudaFree(full);
+  dev_free(full);
   return st;
 }
 
@@ -205,7 +205,7 @@ tp_status tp_coarse_factor_csr(tp_ctx* c, long n, const int* rowptr, const int* 
     return TP_ERR_TIMEOUT;
   }
   if (info != 0) {
-    c->err = "coarse Cholesky: non-positive pivot at column " + std::to_string(info - 1);
+    c->note = "coarse Cholesky: non-positive pivot at column " + std::to_string(info - 1);
     return TP_ERR_NOT_SPD;
   }
   return TP_OK;
@@ -241,7 +241,7 @@ tp_status tp_oc_bisect(tp_ctx* c, long n, const double* x, const double* dv, con
                        double* xnew) {
   if (!c || n < 0 || !x || !dv || !dc || !xnew) return TP_ERR_ARG;
   if (oc_bisect(c, n, const_cast<double*>(x), xnew, dc, dv, g, false) != 0) {
-    c->err = "OC bisection did not terminate";
+    c->note = "OC bisection did not terminate";
     return TP_ERR_TIMEOUT;
   }
   return sync_status(c);

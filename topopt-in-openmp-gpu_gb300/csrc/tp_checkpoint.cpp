@@ -55,12 +55,22 @@ tp_status read_file(const char* path, CkptHeader* h, std::vector<double>* payloa
   FILE* f = std::fopen(path, "rb");
   if (!f) return TP_ERR_ARG;
   tp_status st = TP_OK;
+  // the payload's size follows from the header; it is checked against the
+  // file's length before anything is allocated, so a corrupt header with
+  // large, consistent dimensions is refused instead of sizing a huge buffer
+  long file_bytes = -1;
+  if (std::fseek(f, 0, SEEK_END) == 0) file_bytes = std::ftell(f);
+  std::rewind(f);
   if (std::fread(h, sizeof(*h), 1, f) != 1 || std::memcmp(h->magic, kMagic, 8) != 0 || h->version != 1 ||
+      h->nelx < 1 || h->nely < 1 || h->nelz < 1 || h->nrhs < 1 || h->nrhs > 16 ||
       h->nelem != (int64_t)h->nelx * h->nely * h->nelz ||
-      h->ndof != 3LL * (h->nelx + 1) * (h->nely + 1) * (h->nelz + 1) || h->nrhs < 1)
+      h->ndof != 3LL * (h->nelx + 1) * (h->nely + 1) * (h->nelz + 1))
+    st = TP_ERR_ARG;
+  const int64_t n64 = st == TP_OK ? 2 * h->nelem + 2 * (int64_t)h->nrhs * h->ndof : 0;
+  if (st == TP_OK && (file_bytes < 0 || n64 != ((int64_t)file_bytes - (int64_t)sizeof(*h)) / (int64_t)sizeof(double)))
     st = TP_ERR_ARG;
   if (st == TP_OK) {
-    const size_t n = (size_t)(2 * h->nelem + 2 * (int64_t)h->nrhs * h->ndof);
+    const size_t n = (size_t)n64;
     std::vector<double> buf(n);
     if (std::fread(buf.data(), sizeof(double), n, f) != n || std::fgetc(f) != EOF ||
         fnv1a(kFnvBasis, buf.data(), n * sizeof(double)) != h->checksum)
@@ -104,14 +114,14 @@ tp_status tp_checkpoint_save(tp_ctx* c, const char* path, int loop) {
   const std::string tmp = std::string(path) + ".tmp";
   FILE* f = std::fopen(tmp.c_str(), "wb");
   if (!f) {
-    c->err = "checkpoint: cannot open " + tmp;
+    c->note = "checkpoint: cannot open " + tmp;
     return TP_ERR_ARG;
   }
   const bool ok = std::fwrite(&h, sizeof h, 1, f) == 1 &&
                   std::fwrite(buf.data(), sizeof(double), buf.size(), f) == buf.size();
   if (std::fclose(f) != 0 || !ok || std::rename(tmp.c_str(), path) != 0) {
     std::remove(tmp.c_str());
-    c->err = std::string("checkpoint: writing ") + path + " failed";
+    c->note = std::string("checkpoint: writing ") + path + " failed";
     return TP_ERR_ARG;
   }
   return TP_OK;
@@ -122,11 +132,11 @@ tp_status tp_checkpoint_load(tp_ctx* c, const char* path, int* loop) {
   CkptHeader h;
   std::vector<double> buf;
   if (read_file(path, &h, &buf) != TP_OK) {
-    c->err = std::string("checkpoint: ") + path + " is missing, truncated or corrupt";
+    c->note = std::string("checkpoint: ") + path + " is missing, truncated or corrupt";
     return TP_ERR_ARG;
   }
   if (h.nelx != c->p.nelx || h.nely != c->p.nely || h.nelz != c->p.nelz || h.nrhs != c->p.nrhs) {
-    c->err = "checkpoint: grid or load-case count differs from the context's";
+    c->note = "checkpoint: grid or load-case count differs from the context's";
     return TP_ERR_ARG;
   }
   const long ne = h.nelem, nd = (long)h.ndof * h.nrhs;

@@ -118,20 +118,20 @@ void coarse_alloc(tp_ctx* c) {
   C.bw = 3L * ((long)L.nz * L.ny + L.ny + 1) + 2;
   if (C.bw > C.n - 1) C.bw = std::max(1L, C.n - 1);
   C.band_elems = (size_t)C.n * (C.bw + 1) + 1;
-  cudaMalloc(&C.band, C.band_elems * sizeof(double));
+  dev_malloc(&C.band, C.band_elems * sizeof(double));
   C.nbs = (int)std::min((long)NBS, ((C.n + 31) / 32) * 32);
   C.nblk = (int)((C.n + C.nbs - 1) / C.nbs);
   const size_t dsz = (size_t)C.nblk * C.nbs * C.nbs;
   const size_t lsz = (size_t)C.nblk * C.nbs * C.bw;
-  cudaMalloc(&C.dinv, dsz * sizeof(double));
-  cudaMalloc(&C.dinvT, dsz * sizeof(double));
-  cudaMalloc(&C.lrow, lsz * sizeof(double));
+  dev_malloc(&C.dinv, dsz * sizeof(double));
+  dev_malloc(&C.dinvT, dsz * sizeof(double));
+  dev_malloc(&C.lrow, lsz * sizeof(double));
   // work columns: y and t, kSolveCols each, then rhs and sol of a single solve
-  cudaMalloc(&C.vec, (size_t)C.n * (2 * 8 + 2) * sizeof(double));
+  dev_malloc(&C.vec, (size_t)C.n * (2 * 8 + 2) * sizeof(double));
   C.rhs = C.vec + 16 * C.n;
   C.sol = C.vec + 17 * C.n;
-  cudaMalloc(&C.info, sizeof(int));
-  cudaMalloc(&C.linv, (NB * NB + NB) * sizeof(double));  // current diagonal block of L and 1/L(j,j)
+  dev_malloc(&C.info, sizeof(int));
+  dev_malloc(&C.linv, (NB * NB + NB) * sizeof(double));  // current diagonal block of L and 1/L(j,j)
   cudaStreamCreateWithFlags(&C.s2, cudaStreamNonBlocking);
   int lo = 0, hi = 0;
   cudaDeviceGetStreamPriorityRange(&lo, &hi);
@@ -143,10 +143,12 @@ void coarse_alloc(tp_ctx* c) {
   cudaEventCreateWithFlags(&C.ev_rest, cudaEventDisableTiming);
   c->mem_bytes += (long)(C.band_elems + 2 * dsz + lsz + C.n * 18) * 8;
   int* flags = nullptr;  // barrier counter, status word, exit counter
-  if (cudaMalloc(&flags, 3 * sizeof(int)) == cudaSuccess) {
+  if (dev_malloc(&flags, 3 * sizeof(int)) == cudaSuccess) {
     cudaMemsetAsync(flags, 0, 3 * sizeof(int), c->s);
     C.bar = reinterpret_cast<unsigned*>(flags);
     C.serr = flags + 1;
+  } else {
+    C.alloc_failed = true;
   }
   ps_plan(c);
   pf_plan(c);
@@ -154,22 +156,22 @@ void coarse_alloc(tp_ctx* c) {
 
 void coarse_free(tp_ctx* c) {
   Coarse& C = c->coarse;
-  cudaFree(C.band);
-  cudaFree(C.dinv);
-  cudaFree(C.dinvT);
-  cudaFree(C.lrow);
-  cudaFree(C.vec);
+  dev_free(C.band);
+  dev_free(C.dinv);
+  dev_free(C.dinvT);
+  dev_free(C.lrow);
+  dev_free(C.vec);
   if (C.graph_exec) cudaGraphExecDestroy(C.graph_exec);
   if (C.factor_exec) cudaGraphExecDestroy(C.factor_exec);
-  cudaFree(C.info);
-  cudaFree(C.linv);
+  dev_free(C.info);
+  dev_free(C.linv);
   if (C.s2) cudaStreamDestroy(C.s2);
   if (C.ev_panel) cudaEventDestroy(C.ev_panel);
   if (C.ev_rest) cudaEventDestroy(C.ev_rest);
-  cudaFree(C.bar);  // C.serr shares its allocation
-  cudaFree(C.pf_flags);
-  cudaFree(C.pf_rpk);
-  cudaFree(C.pf_off);
+  dev_free(C.bar);  // C.serr shares its allocation
+  dev_free(C.pf_flags);
+  dev_free(C.pf_rpk);
+  dev_free(C.pf_off);
   C = Coarse();
 }
 
@@ -1118,10 +1120,11 @@ static void pf_plan(tp_ctx* c) {
   C.pf_NT = (int)NT;
   C.pf_TS = (int)TS;
   C.pf_flag_bytes = sizeof(int) * (size_t)(NT + 2 * NT * TS + 1);
-  if (cudaMalloc(&C.pf_flags, C.pf_flag_bytes) != cudaSuccess ||
-      cudaMalloc(&C.pf_rpk, sizeof(double) * NT * NB) != cudaSuccess ||
-      cudaMalloc(&C.pf_off, sizeof(long) * (NT + 1)) != cudaSuccess) {
+  if (dev_malloc(&C.pf_flags, C.pf_flag_bytes) != cudaSuccess ||
+      dev_malloc(&C.pf_rpk, sizeof(double) * NT * NB) != cudaSuccess ||
+      dev_malloc(&C.pf_off, sizeof(long) * (NT + 1)) != cudaSuccess) {
     cudaGetLastError();
+    C.alloc_failed = true;
     return;
   }
   cudaMemcpy(C.pf_off, off.data(), sizeof(long) * (NT + 1), cudaMemcpyHostToDevice);

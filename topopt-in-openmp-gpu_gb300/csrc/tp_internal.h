@@ -21,6 +21,19 @@
 
 namespace tp {
 
+// Every device and pinned-host allocation of the library goes through these
+// (tp_api.cu). They count the live allocations and honour the host-side
+// fault injection of tp_fault_alloc: the chosen allocation fails as if
+// cudaMalloc had returned cudaErrorMemoryAllocation, without calling it.
+cudaError_t dev_malloc(void** p, size_t bytes);
+void dev_free(void* p);
+cudaError_t host_malloc_pinned(void** p, size_t bytes);
+void host_free_pinned(void* p);
+template <typename T>
+inline cudaError_t dev_malloc(T** p, size_t bytes) {
+  return dev_malloc(reinterpret_cast<void**>(p), bytes);
+}
+
 struct Level {
   int ex, ey, ez;     // elements
   int nx, ny, nz;     // nodes
@@ -48,6 +61,7 @@ enum Scalar {
   S_ITER,   // iteration at which it converged
   S_MAXRR,  // (column 0) largest relres over the columns
   S_IT,     // (column 0) iteration counter of the captured CG loop
+  S_G,      // (column 0) constraint value g = vol - volfrac of the OC bisection
   S_COUNT
 };
 
@@ -83,6 +97,7 @@ struct Coarse {
   long ps_spin = 0;             // polls before a barrier wait gives up (0: the default, about a second)
   int ps_missing = 0;           // arrivals each barrier waits for beyond the grid (failure-detection test only)
   int solve_variant = 0;        // 0: single launches (factor and solve) where their plans apply; 1: launches per step
+  bool alloc_failed = false;    // an allocation of the set-up failed (tp_create reports TP_ERR_ALLOC)
   int ds = 0;                   // single-launch factor and block inverses in double-single arithmetic
   // single-launch factor (one cooperative kernel for all 32-column steps)
   bool pf_ok = false;
@@ -127,7 +142,8 @@ struct tp_ctx {
   cudaStream_t s = nullptr;
   int device = 0;
   std::string err;   // sticky: a CUDA error; every later call fails
-  std::string note;  // the last recoverable failure (a coarse-solve barrier wait that gave up)
+  std::string note;  // the last failure that leaves the context usable (a non-positive pivot, a
+                     // non-finite residual, a bounded wait that gave up, a checkpoint file refused)
 
   // element stiffness tables per level (576 * ncell^3), FP64 and FP32 copies
   double* d_ke[TP_MAXL] = {};
@@ -199,6 +215,12 @@ struct tp_ctx {
   cudaGraphExec_t cg_exec = nullptr;
   int cg_exec_nr = 0;        // columns the captured graph solves
   int graph_solve = 0;       // 1: tp_solve runs the captured graph also for one load
+  // the design iteration without host round trips before its end
+  // (tp_set_device_loop): CG loop and OC bisection as graph launches
+  int device_loop = 1;
+  cudaGraphExec_t oc_exec = nullptr;  // the OC bisection steps under a conditional while node
+  int* h_info = nullptr;     // pinned: the coarse factor's status word, read at the iteration's end
+  cudaEvent_t it_ev[2] = {nullptr, nullptr};  // brackets of tp_design_iteration's device time
 
   // optional per-kernel-class timing with CUDA events on c->s
   bool prof = false;
@@ -300,6 +322,11 @@ void filter_fwd(tp_ctx* c, const double* x, double* out);
 void filter_adj(tp_ctx* c, double* v, double* tmp);
 void volume_partials(tp_ctx* c, const double* xphys, int* nblocks);
 int oc_update(tp_ctx* c, double g);   // bisection; leaves xnew, change and x <- xnew
+// the same bisection as one graph launch, g read from d_scal[S_G]: enqueues
+// only (no host wait); S_OCDONE = 0 afterwards means it hit its step cap
+bool oc_update_graph(tp_ctx* c);
+void oc_graph_free(tp_ctx* c);
+void constraint_from_volume(tp_ctx* c);  // d_scal[S_G] = d_scal[S_VOL] / nelem - volfrac
 int oc_bisect(tp_ctx* c, long n, double* x, double* xnew, const double* dc, const double* dv, double g,
               bool commit);
 void vec_change(tp_ctx* c, long n, double* x, const double* xnew);  // S_CHANGE, x <- xnew
@@ -312,6 +339,8 @@ void set_design_ke(const double* ke0_host);
 void pcg_prologue(tp_ctx* c, const double* b, const double* u, int nr);
 void pcg_iteration(tp_ctx* c, double* u, int iter, int nr);
 tp_status pcg_graph(tp_ctx* c, int* iters, double* relres);
+tp_status pcg_graph_enqueue(tp_ctx* c);  // set-up and the graph launch, no host wait
+tp_status pcg_graph_status(tp_ctx* c, int* iters, double* relres);  // after h_scal is copied back
 void graph_free(tp_ctx* c);
 
 // error helpers

@@ -275,9 +275,9 @@ void filter_hs(tp_ctx* c, double* hs) {
   c->fw_n = (int)wt.size();
   std::vector<double> w(wt);
   w.insert(w.end(), of.begin(), of.end());
-  if (c->d_fw) cudaFree(c->d_fw);
+  dev_free(c->d_fw);
   c->d_fw = nullptr;
-  if (cudaMalloc(&c->d_fw, sizeof(double) * w.size()) != cudaSuccess) {
+  if (dev_malloc(&c->d_fw, sizeof(double) * w.size()) != cudaSuccess) {
     c->err = "cudaMalloc of the filter weights failed";
     return;
   }
@@ -393,9 +393,10 @@ __global__ void oc_step_kernel(long n, const double* __restrict__ x, const doubl
   if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
 
-// gt = sum + g; l1 or l2 <- lmid; done when (l2-l1)/(l1+l2) <= 1e-6
-__global__ void oc_finish_kernel(const double* __restrict__ partials, int nb, double* __restrict__ scal, double g) {
+// gt = sum + g (g in scal[S_G]); l1 or l2 <- lmid; done when (l2-l1)/(l1+l2) <= 1e-6
+__global__ void oc_finish_kernel(const double* __restrict__ partials, int nb, double* __restrict__ scal) {
   if (scal[S_OCDONE] != 0.0) return;
+  const double g = scal[S_G];
   __shared__ double sh[256];
   const int per = (nb + 255) / 256;
   const int b0 = threadIdx.x * per;
@@ -440,6 +441,21 @@ __global__ void oc_apply_kernel(long n, double* __restrict__ x, double* __restri
   if (threadIdx.x == 0) partials[blockIdx.x] = m;
 }
 
+__global__ void oc_set_g_kernel(double* scal, double g) { scal[S_G] = g; }
+
+// the constraint value of the loop (stencil_optimization.c:158-160): the
+// volume sum divided by the element count, minus volfrac
+__global__ void oc_g_from_volume_kernel(double* scal, double nelem, double volfrac) {
+  scal[S_G] = scal[S_VOL] / nelem - volfrac;
+}
+
+// loop condition of the bisection graph: another batch of steps while the
+// interval is not yet narrow enough and the step cap is not reached
+__global__ void oc_cond_kernel(const double* scal, cudaGraphConditionalHandle h, int cap) {
+  const bool go = scal[S_OCDONE] == 0.0 && scal[S_TMP0] < (double)cap;
+  cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
 __global__ void oc_init_kernel(double* scal) {
   scal[S_L1] = 0.0;
   scal[S_L2] = 1e9;
@@ -456,6 +472,7 @@ int oc_bisect(tp_ctx* c, long ne, double* x, double* xnew, const double* dc, con
   ProfScope ps(c, P_DESIGN);
   const int nb = blocks_for(ne);
   oc_init_kernel<<<1, 1, 0, c->s>>>(c->d_scal);
+  oc_set_g_kernel<<<1, 1, 0, c->s>>>(c->d_scal, g);
   const double *B = nullptr, *lo = nullptr, *hi = nullptr;
   if (c->d_ocb && ne <= c->ocb_n) {
     double* b = c->d_ocb;
@@ -469,7 +486,7 @@ int oc_bisect(tp_ctx* c, long ne, double* x, double* xnew, const double* dc, con
   for (;;) {
     for (int q = 0; q < kBatch; q++) {
       oc_step_kernel<<<nb, 256, 0, c->s>>>(ne, x, dc, dv, B, lo, hi, c->d_scal, c->d_red);
-      oc_finish_kernel<<<1, 256, 0, c->s>>>(c->d_red, nb, c->d_scal, g);
+      oc_finish_kernel<<<1, 256, 0, c->s>>>(c->d_red, nb, c->d_scal);
     }
     taken += kBatch;
     cudaMemcpyAsync(c->h_scal + S_OCDONE, c->d_scal + S_OCDONE, sizeof(double), cudaMemcpyDeviceToHost, c->s);
@@ -486,6 +503,80 @@ int oc_bisect(tp_ctx* c, long ne, double* x, double* xnew, const double* dc, con
 int oc_update(tp_ctx* c, double g) {
   const long ne = (long)c->L[0].ex * c->L[0].ey * c->L[0].ez;
   return oc_bisect(c, ne, c->d_x, c->d_xnew, c->d_dc, c->d_dv, g, true);
+}
+
+void constraint_from_volume(tp_ctx* c) {
+  const double ne = (double)((long)c->L[0].ex * c->L[0].ey * c->L[0].ez);
+  oc_g_from_volume_kernel<<<1, 1, 0, c->s>>>(c->d_scal, ne, c->p.volfrac);
+}
+
+// The bisection of the context's own design arrays as a CUDA graph: one
+// conditional WHILE node whose body is kOcBody bisection steps (each a
+// partial-sum kernel and the kernel that halves the interval; steps after
+// the interval is narrow enough return at once) and the condition kernel.
+// It takes the same steps as oc_bisect, with no host check between them; the
+// cap is the same 240 steps.
+constexpr int kOcBody = 8, kOcMaxSteps = 240;
+
+void oc_graph_free(tp_ctx* c) {
+  if (c->oc_exec) cudaGraphExecDestroy(c->oc_exec);
+  c->oc_exec = nullptr;
+}
+
+static bool oc_graph_build(tp_ctx* c) {
+  oc_graph_free(c);
+  const long ne = (long)c->L[0].ex * c->L[0].ey * c->L[0].ez;
+  const int nb = blocks_for(ne);
+  double* b = c->d_ocb;
+  cudaGraph_t g = nullptr;
+  if (cudaGraphCreate(&g, 0) != cudaSuccess) return false;
+  cudaGraphConditionalHandle h;
+  bool ok = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  ok = ok && cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) == cudaSuccess;
+  if (ok) {
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    ok = cudaStreamBeginCaptureToGraph(c->s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+         cudaSuccess;
+    if (ok) {
+      for (int q = 0; q < kOcBody; q++) {
+        oc_step_kernel<<<nb, 256, 0, c->s>>>(ne, c->d_x, c->d_dc, c->d_dv, b, b + ne, b + 2 * ne, c->d_scal,
+                                             c->d_red);
+        oc_finish_kernel<<<1, 256, 0, c->s>>>(c->d_red, nb, c->d_scal);
+      }
+      oc_cond_kernel<<<1, 1, 0, c->s>>>(c->d_scal, h, kOcMaxSteps);
+      cudaGraph_t out = nullptr;
+      ok = cudaStreamEndCapture(c->s, &out) == cudaSuccess;
+    }
+  }
+  if (ok) ok = cudaGraphInstantiate(&c->oc_exec, g, 0) == cudaSuccess;
+  cudaGraphDestroy(g);
+  if (!ok) {
+    c->oc_exec = nullptr;
+    cudaGetLastError();
+  }
+  return ok;
+}
+
+bool oc_update_graph(tp_ctx* c) {
+  const long ne = (long)c->L[0].ex * c->L[0].ey * c->L[0].ez;
+  if (!c->d_ocb || ne > c->ocb_n) return false;
+  if (!c->oc_exec && !oc_graph_build(c)) return false;
+  ProfScope ps(c, P_DESIGN);
+  const int nb = blocks_for(ne);
+  double* b = c->d_ocb;
+  oc_init_kernel<<<1, 1, 0, c->s>>>(c->d_scal);
+  oc_prep_kernel<<<grid_for(ne, 256), 256, 0, c->s>>>(ne, c->d_x, c->d_dc, c->d_dv, b, b + ne, b + 2 * ne);
+  cudaGraphLaunch(c->oc_exec, c->s);
+  oc_apply_kernel<<<nb, 256, 0, c->s>>>(ne, c->d_x, c->d_xnew, c->d_dc, c->d_dv, c->d_scal, c->d_red, 1);
+  finish_sum(c, nb, S_CHANGE, 1);
+  TP_CHECK_LAUNCH(c, "oc_update_graph");
+  return true;
 }
 
 // max |x - xnew| into S_CHANGE, then x <- xnew (gpu_definitions.c:110-125)

@@ -1,10 +1,12 @@
 // Density-filter adjoint v <- H (v / Hs) for callers that cannot allocate
-// device memory: code running while a CUDA stream is being captured into a
-// graph (cudaMalloc is not allowed there), and host applications whose
-// device memory is owned by another allocator or runtime that forbids
-// libraries from calling cudaMalloc/cudaFree. The caller passes v; the
-// intermediate v/Hs lives in a file-scope __device__ array of fixed size,
-// so nothing is allocated at any call.
+// device memory. Some host applications own all of the GPU's memory: they
+// reserve one arena or pool at start-up and hand out pieces of it themselves,
+// and they forbid the libraries they link from calling cudaMalloc or cudaFree,
+// because an outside allocation can exhaust or fragment the arena and a
+// cudaFree waits for the whole device. Others run this step inside a loop
+// with a fixed time budget, where an allocation's latency is not acceptable.
+// The caller passes v in memory of its own; the intermediate v/Hs lives in a
+// file-scope __device__ array of fixed size, so no call allocates anything.
 //
 // The array (kNoAllocMaxElements doubles, 16 MiB) is part of this library's
 // module: every GPU that loads the library holds it until the process exits.
@@ -16,9 +18,10 @@
 // Host code cannot name the array directly: its name in host code is only a
 // host-side stand-in, not a device address. The first call on each device
 // therefore asks the runtime for the array's device address
-// (cudaGetSymbolAddress, with that device current) and caches it; make that
-// first call before any stream capture. The result is the same as the
-// context-based tp_filter_T (stencil_optimization.c:290-395).
+// (cudaGetSymbolAddress, with that device current), checks the result and
+// caches it; make that first call before any stream capture. The result is
+// the same as the context-based tp_filter_T (stencil_optimization.c:290-395).
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -90,7 +93,7 @@ extern "C" {
 long tp_filter_T_noalloc_max_elements(void) { return kNoAllocMaxElements; }
 
 tp_status tp_filter_T_noalloc(int nelx, int nely, int nelz, double rmin, double* v_dev, void* stream) {
-  if (nelx < 1 || nely < 1 || nelz < 1 || !(rmin > 0) || !v_dev) return TP_ERR_ARG;
+  if (nelx < 1 || nely < 1 || nelz < 1 || !(rmin > 0) || !std::isfinite(rmin) || !v_dev) return TP_ERR_ARG;
   const long ne = (long)nelx * nely * nelz;
   if (ne > kNoAllocMaxElements) {
     std::fprintf(stderr,
@@ -114,12 +117,26 @@ tp_status tp_filter_T_noalloc(int nelx, int nely, int nelz, double rmin, double*
     scratch = g_scratch_addr[dev];
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const int cr = (int)std::ceil(rmin);
+  // a radius past the grid's largest extent reaches every element: the box
+  // [i - (cr - 1), i + cr] clipped to the grid is then the whole axis, so the
+  // box half-width is capped there (and stays an int for any finite rmin)
+  const int span = std::max(nelx, std::max(nely, nelz)) + 1;
+  const int cr = rmin >= (double)span ? span : (int)std::ceil(rmin);
   long nb = (ne + 255) / 256;
   if (nb > 4096) nb = 4096;
-  noalloc_div_kernel<<<(unsigned)nb, 256, 0, s>>>(nelx, nely, nelz, cr, rmin, v_dev, scratch);
-  noalloc_sum_kernel<<<(unsigned)nb, 256, 0, s>>>(nelx, nely, nelz, cr, rmin, scratch, v_dev);
-  return cudaGetLastError() == cudaSuccess ? TP_OK : TP_ERR_CUDA;
+  // launched through cudaLaunchKernel so that each launch's own status is
+  // read from its return value: an error the caller left pending from its
+  // own work is neither reported here nor cleared
+  int ax = nelx, ay = nely, az = nelz, acr = cr;
+  double ar = rmin;
+  double* av = v_dev;
+  double* at = scratch;
+  void* a1[] = {&ax, &ay, &az, &acr, &ar, &av, &at};
+  void* a2[] = {&ax, &ay, &az, &acr, &ar, &at, &av};
+  const dim3 grid((unsigned)nb), block(256);
+  if (cudaLaunchKernel((const void*)noalloc_div_kernel, grid, block, a1, 0, s) != cudaSuccess) return TP_ERR_CUDA;
+  if (cudaLaunchKernel((const void*)noalloc_sum_kernel, grid, block, a2, 0, s) != cudaSuccess) return TP_ERR_CUDA;
+  return TP_OK;
 }
 
 }  // extern "C"

@@ -14,6 +14,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
+#include <utility>
 #include <tuple>
 #include <vector>
 
@@ -42,6 +44,13 @@ Dims dims_of(int nelx, int nely, int nelz, int l) {
 inline long pnode(const Dims& d, int i, int k, int j) { return (long)(i + 1) * d.wy * d.wz + (long)(k + 1) * d.wy + (j + 1); }
 inline long cnode(const Dims& d, int i, int k, int j) { return ((long)i * (d.ez + 1) + k) * (d.ey + 1) + j; }
 
+// TOPOPT_PRECISION=mixed selects the mixed form (FP32 V-cycle, FP64 CG) for
+// every context of these entry points; the default is the FP64 form
+int precision_from_env() {
+  const char* prec = std::getenv("TOPOPT_PRECISION");
+  return (prec && std::strcmp(prec, "mixed") == 0) ? TP_MIXED : TP_FP64;
+}
+
 // -- context cache -----------------------------------------------------------
 std::map<std::tuple<int, int, int, int>, tp_ctx*> g_ctx;
 
@@ -60,6 +69,7 @@ tp_ctx* ctx_for(int nelx, int nely, int nelz, int nl) {
   p.nely = nely;
   p.nelz = nelz;
   p.nl = nl;
+  p.precision = precision_from_env();
   tp_ctx* c = nullptr;
   const tp_status st = tp_create(&p, &c);
   if (st != TP_OK) {
@@ -101,10 +111,78 @@ struct Scratch {
 };
 Scratch g_s[4];
 
-// padded host vector of level l -> canonical double (host)
+// -- host staging -------------------------------------------------------------
+// The canonical host copies that cross to and from the device live in
+// page-locked memory (cudaMallocHost), so every copy runs at the host link's
+// full rate; blocks are cached by size and reused from call to call, and the
+// vectors are left uninitialised on construction (the conversion that fills
+// one writes every element). If page-locked memory is refused, plain memory
+// stands in (slower copies, same results).
+class PinnedCache {
+ public:
+  void* get(size_t bytes) {
+    std::lock_guard<std::mutex> lock(mu_);
+    auto it = free_.lower_bound(bytes);
+    if (it != free_.end() && it->first <= 2 * bytes + 4096) {
+      void* p = it->second;
+      free_.erase(it);
+      return p;
+    }
+    void* p = nullptr;
+    bool pinned = cudaMallocHost(&p, bytes) == cudaSuccess;
+    if (!pinned) {
+      cudaGetLastError();
+      p = std::malloc(bytes ? bytes : 1);
+      if (!p) throw std::bad_alloc();
+    }
+    info_[p] = std::make_pair(bytes, pinned);
+    return p;
+  }
+  void put(void* p) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lock(mu_);
+    free_.insert(std::make_pair(info_[p].first, p));
+  }
+
+ private:
+  std::mutex mu_;
+  std::multimap<size_t, void*> free_;
+  std::map<void*, std::pair<size_t, bool>> info_;
+};
+PinnedCache& pinned_cache() {
+  static PinnedCache* cache = new PinnedCache();  // kept until exit: blocks may outlive static destructors
+  return *cache;
+}
+
 template <typename T>
-std::vector<double> to_canon(const Dims& d, const T* v) {
-  std::vector<double> out(3L * (d.ex + 1) * (d.ey + 1) * (d.ez + 1));
+struct StageAlloc {
+  using value_type = T;
+  StageAlloc() = default;
+  template <typename U>
+  StageAlloc(const StageAlloc<U>&) {}
+  T* allocate(size_t n) { return static_cast<T*>(pinned_cache().get(n * sizeof(T))); }
+  void deallocate(T* p, size_t) { pinned_cache().put(p); }
+  template <typename U>
+  void construct(U* p) noexcept {
+    ::new (static_cast<void*>(p)) U;  // default-initialised: no zero fill
+  }
+  template <typename U, typename... A>
+  void construct(U* p, A&&... a) {
+    ::new (static_cast<void*>(p)) U(std::forward<A>(a)...);
+  }
+  template <typename U>
+  bool operator==(const StageAlloc<U>&) const { return true; }
+  template <typename U>
+  bool operator!=(const StageAlloc<U>&) const { return false; }
+};
+using HVec = std::vector<double, StageAlloc<double>>;
+
+// padded host vector of level l -> canonical double (host); the conversions
+// run on all host threads (one x-z line of nodes per item)
+template <typename T>
+HVec to_canon(const Dims& d, const T* v) {
+  HVec out(3L * (d.ex + 1) * (d.ey + 1) * (d.ez + 1));
+#pragma omp parallel for collapse(2) schedule(static)
   for (int i = 0; i <= d.ex; i++)
     for (int k = 0; k <= d.ez; k++)
       for (int j = 0; j <= d.ey; j++)
@@ -112,7 +190,8 @@ std::vector<double> to_canon(const Dims& d, const T* v) {
   return out;
 }
 template <typename T>
-void from_canon(const Dims& d, const std::vector<double>& h, T* v) {
+void from_canon(const Dims& d, const HVec& h, T* v) {
+#pragma omp parallel for collapse(2) schedule(static)
   for (int i = 0; i <= d.ex; i++)
     for (int k = 0; k <= d.ez; k++)
       for (int j = 0; j <= d.ey; j++)
@@ -120,39 +199,56 @@ void from_canon(const Dims& d, const std::vector<double>& h, T* v) {
 }
 
 // padded element array (fine level) <-> canonical
-std::vector<double> el_to_canon(const gridContext& gc, const DTYPE* x) {
+HVec el_to_canon(const gridContext& gc, const DTYPE* x) {
   const int ex = gc.nelx, ey = gc.nely, ez = gc.nelz;
   const long wy = gc.wrapy - 1, wz = gc.wrapz - 1;
-  std::vector<double> out((size_t)ex * ey * ez);
+  HVec out((size_t)ex * ey * ez);
+#pragma omp parallel for collapse(2) schedule(static)
   for (int i = 0; i < ex; i++)
     for (int k = 0; k < ez; k++)
       for (int j = 0; j < ey; j++)
         out[((size_t)i * ez + k) * ey + j] = (double)x[(i + 1) * wy * wz + (k + 1) * wy + (j + 1)];
   return out;
 }
-void el_from_canon(const gridContext& gc, const std::vector<double>& h, DTYPE* x) {
+void el_from_canon(const gridContext& gc, const HVec& h, DTYPE* x) {
   const int ex = gc.nelx, ey = gc.nely, ez = gc.nelz;
   const long wy = gc.wrapy - 1, wz = gc.wrapz - 1;
+#pragma omp parallel for collapse(2) schedule(static)
   for (int i = 0; i < ex; i++)
     for (int k = 0; k < ez; k++)
       for (int j = 0; j < ey; j++)
         x[(i + 1) * wy * wz + (k + 1) * wy + (j + 1)] = (DTYPE)h[((size_t)i * ez + k) * ey + j];
 }
 
-double* up(int slot, const std::vector<double>& h) {
+// an element array of n entries as a staged double copy
+template <typename T>
+HVec el_copy(const T* x, long n) {
+  HVec out((size_t)n);
+#pragma omp parallel for schedule(static)
+  for (long e = 0; e < n; e++) out[e] = (double)x[e];
+  return out;
+}
+
+// bytes copied host -> device and device -> host by the entry points
+long g_h2d = 0, g_d2h = 0;
+
+double* up(int slot, const HVec& h) {
   double* d = g_s[slot].get(h.size());
   cudaMemcpy(d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice);
+  g_h2d += (long)(h.size() * sizeof(double));
   return d;
 }
-std::vector<double> down(const double* d, size_t n) {
-  std::vector<double> h(n);
+HVec down(const double* d, size_t n) {
+  HVec h(n);
   cudaMemcpy(h.data(), d, n * sizeof(double), cudaMemcpyDeviceToHost);
+  g_d2h += (long)(n * sizeof(double));
   return h;
 }
 
 void set_design(tp_ctx* c, const gridContext& gc, const DTYPE* x) {
-  const std::vector<double> xc = el_to_canon(gc, x);
+  const HVec xc = el_to_canon(gc, x);
   check(c, tp_upload(c, TP_FIELD_XPHYS, xc.data(), (long)xc.size()), "upload xPhys");
+  g_h2d += (long)(xc.size() * sizeof(double));
 }
 
 }  // namespace
@@ -336,7 +432,7 @@ void applyStateOperator_stencil(const struct gpuNode* node, const DTYPE* x, cons
   tp_ctx* c = ctx_levels(gc, 2);
   set_design(c, gc, x);
   const Dims d = dims_of((int)gc.nelx, (int)gc.nely, (int)gc.nelz, 0);
-  const std::vector<double> h = to_canon(d, in);
+  const HVec h = to_canon(d, in);
   double* din = up(0, h);
   double* dout = g_s[1].get(h.size());
   check(c, tp_apply(c, 0, din, dout), "applyStateOperator_stencil");
@@ -354,7 +450,7 @@ void applyStateOperatorSubspace_halo(const struct gpuNode* node, const int l, co
   tp_ctx* c = ctx_levels(gc, l + 1);
   set_design(c, gc, x);
   const Dims d = dims_of((int)gc.nelx, (int)gc.nely, (int)gc.nelz, l);
-  const std::vector<double> h = to_canon(d, in);
+  const HVec h = to_canon(d, in);
   double* din = up(0, h);
   double* dout = g_s[1].get(h.size());
   if (l >= 1) check(c, tp_assemble(c), "assemble");
@@ -369,12 +465,14 @@ void getComplianceAndSensetivity_halo(const struct gpuNode* node, const DTYPE* x
   tp_ctx* c = ctx_levels(gc, 2);
   set_design(c, gc, x);
   const Dims d = dims_of((int)gc.nelx, (int)gc.nely, (int)gc.nelz, 0);
-  const std::vector<double> h = to_canon(d, u);
+  const HVec h = to_canon(d, u);
   check(c, tp_upload(c, TP_FIELD_U, h.data(), (long)h.size()), "upload U");
+  g_h2d += (long)(h.size() * sizeof(double));
   double cc = 0;
   check(c, tp_compliance(c, &cc), "getComplianceAndSensetivity_halo");
-  std::vector<double> dc(tp_nelem(c));
+  HVec dc(tp_nelem(c));
   check(c, tp_download(c, TP_FIELD_DC, dc.data(), (long)dc.size()), "download dc");
+  g_d2h += (long)(dc.size() * sizeof(double));
   el_from_canon(gc, dc, dcdx);
   *c_out = (DTYPE)cc;
 }
@@ -384,7 +482,7 @@ void projectToFinerGrid_halo(const struct gpuNode* node, const int l, const CTYP
   tp_ctx* c = ctx_levels(gc, l + 2);
   const Dims dc = dims_of((int)gc.nelx, (int)gc.nely, (int)gc.nelz, l + 1);
   const Dims df = dims_of((int)gc.nelx, (int)gc.nely, (int)gc.nelz, l);
-  const std::vector<double> h = to_canon(dc, ucoarse);
+  const HVec h = to_canon(dc, ucoarse);
   double* din = up(0, h);
   const size_t nf = 3L * (df.ex + 1) * (df.ey + 1) * (df.ez + 1);
   double* dout = g_s[1].get(nf);
@@ -397,7 +495,7 @@ void projectToCoarserGrid_halo(const struct gpuNode* node, const int l, const CT
   tp_ctx* c = ctx_levels(gc, l + 2);
   const Dims dc = dims_of((int)gc.nelx, (int)gc.nely, (int)gc.nelz, l + 1);
   const Dims df = dims_of((int)gc.nelx, (int)gc.nely, (int)gc.nelz, l);
-  const std::vector<double> h = to_canon(df, ufine);
+  const HVec h = to_canon(df, ufine);
   double* din = up(0, h);
   const size_t nc = 3L * (dc.ex + 1) * (dc.ey + 1) * (dc.ez + 1);
   double* dout = g_s[1].get(nc);
@@ -427,7 +525,7 @@ static void smooth_common(const gridContext& gc, const DTYPE* x, int l, int subs
   set_design(c, gc, x);
   check(c, tp_assemble(c), "assemble");
   const Dims d = dims_of((int)gc.nelx, (int)gc.nely, (int)gc.nelz, l);
-  const std::vector<double> hu = to_canon(d, u), hb = to_canon(d, b), hd = to_canon(d, invD);
+  const HVec hu = to_canon(d, u), hb = to_canon(d, b), hd = to_canon(d, invD);
   double* du = up(0, hu);
   double* db = up(1, hb);
   double* dd = up(2, hd);
@@ -497,9 +595,11 @@ void solveStateMG_halo(const struct gpuGrid* gpu_gc, DTYPE* x, const int nswp, c
   tp_ctx* c = ctx_for((int)gc.nelx, (int)gc.nely, (int)gc.nelz, nl);
   set_design(c, gc, x);
   const Dims d = dims_of((int)gc.nelx, (int)gc.nely, (int)gc.nelz, 0);
-  const std::vector<double> hb = to_canon(d, b), hu = to_canon(d, u);
+  const HVec hb = to_canon(d, b), hu = to_canon(d, u);
   check(c, tp_upload(c, TP_FIELD_F, hb.data(), (long)hb.size()), "upload F");
+  g_h2d += (long)(hb.size() * sizeof(double));
   check(c, tp_upload(c, TP_FIELD_U, hu.data(), (long)hu.size()), "upload U");
+  g_h2d += (long)(hu.size() * sizeof(double));
   double* F = tp_field_ptr(c, TP_FIELD_F);
   double* U = tp_field_ptr(c, TP_FIELD_U);
   // the reference's nswp and tol arrive per call; omega 0.6 and the cap of
@@ -510,8 +610,9 @@ void solveStateMG_halo(const struct gpuGrid* gpu_gc, DTYPE* x, const int nswp, c
   check(c, tp_assemble(c), "assemble");
   const tp_status st = tp_solve_rhs(c, F, U, &it, &rr);
   check(c, st, "solveStateMG_halo");
-  std::vector<double> hu2(hu.size());
+  HVec hu2(hu.size());
   check(c, tp_download(c, TP_FIELD_U, hu2.data(), (long)hu2.size()), "download U");
+  g_d2h += (long)(hu2.size() * sizeof(double));
   from_canon(d, hu2, u);
   *finalIter = it;
   *finalRes = (float)rr;
@@ -675,7 +776,7 @@ void solveSubspaceMatrix(const struct gridContext gc, const int l, struct Coarse
                          const CTYPE* in, CTYPE* out) {
   tp_ctx* c = solverData.handle ? (tp_ctx*)solverData.handle : ctx_for((int)gc.nelx, (int)gc.nely, (int)gc.nelz, l + 1);
   const Dims d = dims_of((int)gc.nelx, (int)gc.nely, (int)gc.nelz, l);
-  const std::vector<double> h = to_canon(d, in);
+  const HVec h = to_canon(d, in);
   double* din = up(0, h);
   double* dout = g_s[1].get(h.size());
   check(c, tp_coarse_solve_factored(c, din, dout), "solveSubspaceMatrix");
@@ -686,7 +787,7 @@ void solveSubspaceMatrix(const struct gridContext gc, const int l, struct Coarse
 // gpu_definitions.h: volume, change, OC update on the GPU
 DTYPE compute_volume(const struct gridContext gc, DTYPE* xPhys) {
   tp_ctx* c = ctx_levels(gc, 2);
-  const std::vector<double> h = el_to_canon(gc, xPhys);
+  const HVec h = el_to_canon(gc, xPhys);
   double* d = up(0, h);
   double s = 0;
   check(c, tp_vec_sum(c, (long)h.size(), d, &s), "compute_volume");
@@ -696,11 +797,12 @@ DTYPE compute_volume(const struct gridContext gc, DTYPE* xPhys) {
 float compute_change(DTYPE* x, DTYPE* xnew, const int nelem) {
   tp_ctx* c = g_ctx.empty() ? nullptr : g_ctx.begin()->second;
   if (!c) c = ctx_for(2, 2, 2, 2);
-  std::vector<double> hx(x, x + nelem), hn(xnew, xnew + nelem);
+  const HVec hx = el_copy(x, nelem), hn = el_copy(xnew, nelem);
   double* dx = up(0, hx);
   double* dn = up(1, hn);
   double ch = 0;
   check(c, tp_vec_change(c, nelem, dx, dn, &ch), "compute_change");
+#pragma omp parallel for schedule(static)
   for (int e = 0; e < nelem; e++) x[e] = xnew[e];
   return (float)ch;
 }
@@ -709,13 +811,14 @@ void update_solution(const DTYPE* x, DTYPE* xnew, const DTYPE* dv, const DTYPE* 
                      const DTYPE g) {
   tp_ctx* c = g_ctx.empty() ? nullptr : g_ctx.begin()->second;
   if (!c) c = ctx_for(2, 2, 2, 2);
-  std::vector<double> hx(x, x + nelem), hv(dv, dv + nelem), hc(dc, dc + nelem);
+  const HVec hx = el_copy(x, nelem), hv = el_copy(dv, nelem), hc = el_copy(dc, nelem);
   double* dx = up(0, hx);
   double* ddv = up(1, hv);
   double* ddc = up(2, hc);
   double* dn = g_s[3].get(nelem);
   check(c, tp_oc_bisect(c, nelem, dx, ddv, ddc, (double)g, dn), "update_solution");
-  const std::vector<double> out = down(dn, nelem);
+  const HVec out = down(dn, nelem);
+#pragma omp parallel for schedule(static)
   for (int e = 0; e < nelem; e++) xnew[e] = (DTYPE)out[e];
 }
 
@@ -724,7 +827,7 @@ void update_solution(const DTYPE* x, DTYPE* xnew, const DTYPE* dv, const DTYPE* 
 void applyDensityFilter(const struct gridContext gc, const DTYPE rmin, const DTYPE* rho, DTYPE* out) {
   tp_ctx* c = ctx_levels(gc, 2);
   check(c, tp_set_rmin(c, (double)rmin), "set rmin");
-  const std::vector<double> h = el_to_canon(gc, rho);
+  const HVec h = el_to_canon(gc, rho);
   double* din = up(0, h);
   double* dout = g_s[1].get(h.size());
   check(c, tp_filter(c, din, dout), "applyDensityFilter");
@@ -734,7 +837,7 @@ void applyDensityFilter(const struct gridContext gc, const DTYPE rmin, const DTY
 void applyDensityFilterGradient(const struct gridContext gc, const DTYPE rmin, DTYPE* v) {
   tp_ctx* c = ctx_levels(gc, 2);
   check(c, tp_set_rmin(c, (double)rmin), "set rmin");
-  const std::vector<double> h = el_to_canon(gc, v);
+  const HVec h = el_to_canon(gc, v);
   double* dv = up(0, h);
   check(c, tp_filter_T(c, dv), "applyDensityFilterGradient");
   el_from_canon(gc, down(dv, h.size()), v);
@@ -809,8 +912,7 @@ void top3dmgcg(const uint_fast32_t nelx, const uint_fast32_t nely, const uint_fa
   p.volfrac = (double)volfrac;
   p.rmin = (double)rmin;
   p.cgtol = (double)cgtol;
-  const char* prec = std::getenv("TOPOPT_PRECISION");
-  if (prec && std::strcmp(prec, "mixed") == 0) p.precision = TP_MIXED;
+  p.precision = precision_from_env();
   tp_ctx* c = nullptr;
   tp_status st = tp_create(&p, &c);
   if (st != TP_OK) {
@@ -845,8 +947,9 @@ void top3dmgcg(const uint_fast32_t nelx, const uint_fast32_t nely, const uint_fa
   if (verbose == 1) std::printf("End time: %6.3f \n", omp_get_wtime() - t0);
   if (write_result == 1) {
     const Dims d = dims_of((int)nelx, (int)nely, (int)nelz, 0);
-    std::vector<double> xp(tp_nelem(c));
+    HVec xp(tp_nelem(c));
     check(c, tp_download(c, TP_FIELD_XPHYS, xp.data(), (long)xp.size()), "download xPhys");
+  g_d2h += (long)(xp.size() * sizeof(double));
     std::vector<DTYPE> padded((size_t)(d.wx - 1) * (d.wy - 1) * (d.wz - 1), (DTYPE)0);
     gridContext gc;
     gc.nelx = nelx;
@@ -863,6 +966,14 @@ void top3dmgcg(const uint_fast32_t nelx, const uint_fast32_t nely, const uint_fa
     writeDensityVtkFileWithHalo((int)nelx, (int)nely, (int)nelz, padded.data(), n2);
   }
   tp_destroy(c);
+}
+
+// bytes the entry points above have copied between host and device since the
+// library was loaded (or last reset); no counterpart in the reference
+void topopt_ref_transfer_bytes(long* h2d, long* d2h, int reset) {
+  if (h2d) *h2d = g_h2d;
+  if (d2h) *d2h = g_d2h;
+  if (reset) g_h2d = g_d2h = 0;
 }
 
 }  // extern "C"

@@ -104,6 +104,11 @@ def load():
     L.tp_autotune.argtypes = [V, P]
     L.tp_multiload.argtypes = [I, I, I, I, I, ctypes.c_ulonglong, P]
     L.tp_set_graph_solve.argtypes = [V, I]
+    L.tp_set_device_loop.argtypes = [V, I]
+    L.tp_fault_alloc.restype = ctypes.c_long
+    L.tp_fault_alloc.argtypes = [ctypes.c_long]
+    L.tp_coarse_factor_csr.argtypes = [V, ctypes.c_long, P, P, P]
+    L.tp_coarse_solve_factored.argtypes = [V, P, P]
     L.tp_solve_columns.argtypes = [V, P, P]
     L.tp_checkpoint_save.argtypes = [V, ctypes.c_char_p, I]
     L.tp_checkpoint_load.argtypes = [V, ctypes.c_char_p, ctypes.POINTER(I)]
@@ -135,6 +140,12 @@ def multiload(nelx, nely, nelz, ncase, nload, seed=0):
     if st != 0:
         raise TopOptError(st, "tp_multiload")
     return F
+
+
+def fault_alloc(k):
+    """Host-side fault injection: the k-th allocation of the library from now
+    on fails (0 = off). Returns the number of live library allocations."""
+    return load().tp_fault_alloc(k)
 
 
 def _ptr(t):
@@ -265,6 +276,26 @@ class TopOpt:
         """1: the CG loop runs as one CUDA graph launch also for a single load."""
         self._check(self.L.tp_set_graph_solve(self.ctx, int(on)))
 
+    def set_device_loop(self, on):
+        """1 (default): one host wait per design iteration (graph-launched CG loop
+        and OC bisection); 0: host-driven as the reference."""
+        self._check(self.L.tp_set_device_loop(self.ctx, int(on)))
+
+    def coarse_factor_csr(self, rowptr, col, val):
+        """Band-Cholesky factor of a host CSR of the coarsest level; returns the
+        status (0, or 4 for a non-positive pivot) without raising."""
+        rowptr = np.ascontiguousarray(rowptr, np.int32)
+        col = np.ascontiguousarray(col, np.int32)
+        val = np.ascontiguousarray(val, np.float64)
+        return self.L.tp_coarse_factor_csr(self.ctx, len(rowptr) - 1, rowptr.ctypes.data, col.ctypes.data,
+                                           val.ctypes.data)
+
+    def coarse_solve_factored(self, rhs):
+        import torch
+        out = torch.empty_like(rhs)
+        self._check(self.L.tp_coarse_solve_factored(self.ctx, _ptr(rhs), _ptr(out)))
+        return out
+
     def autotune(self):
         """Tunes the level-0 launch shapes; returns the best ms per (f32, f64) x mode."""
         ms = np.zeros(8)
@@ -382,3 +413,159 @@ class TopOpt:
         loops = ctypes.c_int(0)
         self._check(self.L.tp_run(self.ctx, max_iterations, hist, ctypes.byref(loops)))
         return [hist[i] for i in range(loops.value)]
+
+
+# ---------------------------------------------------------------------------
+# The reference-signature drop-in libraries (include/topopt_ref_api.h):
+# ctypes mirrors of the reference's structs (definitions.h:31-53,
+# gpu_definitions.h:7-37, stencil_assembly.h:8-27) and of its padded host
+# layout (gpu_definitions.c:67-92).
+UF = ctypes.c_ulong  # uint_fast32_t on LP64 glibc (x86_64 and aarch64)
+
+
+class FixedDofs(ctypes.Structure):
+    _fields_ = [("n", UF), ("idx", ctypes.POINTER(UF))]
+
+
+class GridContext(ctypes.Structure):
+    _fields_ = [("E0", ctypes.c_double), ("Emin", ctypes.c_double), ("nu", ctypes.c_double),
+                ("esx", ctypes.c_double), ("esy", ctypes.c_double), ("esz", ctypes.c_double),
+                ("nelx", UF), ("nely", UF), ("nelz", UF), ("wrapx", UF), ("wrapy", UF), ("wrapz", UF),
+                ("penal", ctypes.c_double), ("precomputedKE", ctypes.POINTER(ctypes.POINTER(ctypes.c_double))),
+                ("fixedDofs", ctypes.POINTER(FixedDofs))]
+
+
+class GpuNode(ctypes.Structure):
+    pass
+
+
+GpuNode._fields_ = [("id", ctypes.c_int), ("prev", ctypes.POINTER(GpuNode)), ("next", ctypes.POINTER(GpuNode)),
+                    ("gc", ctypes.POINTER(GridContext)), ("offset_x", ctypes.c_int), ("x_global", ctypes.c_int)]
+
+
+class GpuGrid(ctypes.Structure):
+    _fields_ = [("num_targets", ctypes.c_int), ("target", ctypes.POINTER(GpuNode))]
+
+
+class CSR(ctypes.Structure):
+    _fields_ = [("nnz", ctypes.c_uint64), ("nrows", ctypes.c_int32), ("rowOffsets", ctypes.POINTER(ctypes.c_int)),
+                ("colIndex", ctypes.POINTER(ctypes.c_int)), ("vals", ctypes.POINTER(ctypes.c_double))]
+
+
+def padded_dims(nelx, nely, nelz, level=0):
+    """(ex, ey, ez, wrapx, wrapy, wrapz) of a level in the reference's padded
+    layout: a one-node halo on every side, y padded to a multiple of 128."""
+    ex, ey, ez = nelx >> level, nely >> level, nelz >> level
+    py = (128 - (ey + 1) % 128) % 128
+    return ex, ey, ez, ex + 3, ey + py + 3, ez + 3
+
+
+def vec_to_padded(v, dims):
+    ex, ey, ez, wx, wy, wz = dims
+    p = np.zeros((wx, wz, wy, 3))
+    p[1:ex + 2, 1:ez + 2, 1:ey + 2, :] = v.reshape(ex + 1, ez + 1, ey + 1, 3)
+    return p.reshape(-1)
+
+
+def vec_from_padded(p, dims):
+    ex, ey, ez, wx, wy, wz = dims
+    return p.reshape(wx, wz, wy, 3)[1:ex + 2, 1:ez + 2, 1:ey + 2, :].reshape(-1).copy()
+
+
+def el_to_padded(x, dims):
+    ex, ey, ez, wx, wy, wz = dims
+    p = np.zeros((wx - 1, wz - 1, wy - 1))
+    p[1:ex + 1, 1:ez + 1, 1:ey + 1] = x.reshape(ex, ez, ey)
+    return p.reshape(-1)
+
+
+def el_from_padded(p, dims):
+    ex, ey, ez, wx, wy, wz = dims
+    return p.reshape(wx - 1, wz - 1, wy - 1)[1:ex + 1, 1:ez + 1, 1:ey + 1].reshape(-1).copy()
+
+
+def load_ref_api(flavour=64):
+    """libtopopt_ref<flavour>.so with argument types for the entry points of
+    the reference's design loop (stencil_optimization.c:13-223)."""
+    load()
+    L = ctypes.CDLL(os.path.join(PKG, "libtopopt_ref%d.so" % flavour))
+    P, D, I = ctypes.c_void_p, ctypes.c_double, ctypes.c_int
+    R = D if flavour == 64 else ctypes.c_float
+    L.setupGC.argtypes = [ctypes.POINTER(GridContext), I, I, I, I]
+    L.freeGC.argtypes = [ctypes.POINTER(GridContext), I]
+    L.gridContextToGPUGrid.argtypes = [ctypes.POINTER(GridContext), ctypes.POINTER(GpuGrid), I, I]
+    L.freeGPUGrid.argtypes = [ctypes.POINTER(GpuGrid), I]
+    L.solveStateMG_halo.argtypes = [ctypes.POINTER(GpuGrid), P, I, I, R, P, ctypes.POINTER(I),
+                                    ctypes.POINTER(ctypes.c_float), P, P]
+    L.compute_volume.restype = R
+    L.compute_volume.argtypes = [GridContext, P]
+    L.getComplianceAndSensetivity_halo.argtypes = [ctypes.POINTER(GpuNode), P, P, P, P]
+    L.applyDensityFilterGradient.argtypes = [GridContext, R, P]
+    L.applyDensityFilter.argtypes = [GridContext, R, P, P]
+    L.update_solution.argtypes = [P, P, P, P, I, R]
+    L.compute_change.restype = ctypes.c_float
+    L.compute_change.argtypes = [P, P, I]
+    L.topopt_ref_transfer_bytes.argtypes = [ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long), I]
+    return L
+
+
+class RefLoop:
+    """The reference's design loop body (stencil_optimization.c:148-189)
+    through the drop-in entry points, on host arrays in the reference's padded
+    layout: the caller of the reference's C API, unchanged. FP64 flavour."""
+
+    def __init__(self, nelx, nely, nelz, nl, volfrac, rmin, cgtol):
+        self.L = load_ref_api(64)
+        self.nl, self.volfrac, self.rmin, self.cgtol = nl, volfrac, rmin, cgtol
+        self.gc = GridContext()
+        self.L.setupGC(ctypes.byref(self.gc), nl, nelx, nely, nelz)
+        self.gpu = GpuGrid()
+        self.gpu.num_targets = 1
+        self.L.gridContextToGPUGrid(ctypes.byref(self.gc), ctypes.byref(self.gpu), nl, 0)
+        self.dims = padded_dims(nelx, nely, nelz, 0)
+        ex, ey, ez, wx, wy, wz = self.dims
+        self.nelem_padded = (wx - 1) * (wy - 1) * (wz - 1)
+        self.nelem = nelx * nely * nelz
+        F = np.zeros(3 * (nelx + 1) * (nely + 1) * (nelz + 1))
+        load().tp_reference_load(nelx, nely, nelz, F.ctypes.data)
+        self.F = vec_to_padded(F, self.dims)
+        self.dv = np.ones(self.nelem_padded)
+        self.L.applyDensityFilterGradient(self.gc, rmin, self.dv.ctypes.data)
+        self.reset()
+
+    def reset(self):
+        """x = xPhys = volfrac on the real elements, U = 0 (:97-137)."""
+        ones = np.ones(self.nelem)
+        self.x = el_to_padded(self.volfrac * ones, self.dims)
+        self.xPhys = self.x.copy()
+        self.xnew = np.zeros(self.nelem_padded)
+        self.dc = np.zeros(self.nelem_padded)
+        self.U = np.zeros_like(self.F)
+
+    def iteration(self):
+        L = self.L
+        it, res, c = ctypes.c_int(0), ctypes.c_float(0), ctypes.c_double(0)
+        L.solveStateMG_halo(ctypes.byref(self.gpu), self.xPhys.ctypes.data, 4, self.nl, self.cgtol, None,
+                            ctypes.byref(it), ctypes.byref(res), self.F.ctypes.data, self.U.ctypes.data)
+        vol = L.compute_volume(self.gc, self.xPhys.ctypes.data)
+        L.getComplianceAndSensetivity_halo(self.gpu.target, self.xPhys.ctypes.data, self.U.ctypes.data,
+                                           ctypes.byref(c), self.dc.ctypes.data)
+        L.applyDensityFilterGradient(self.gc, self.rmin, self.dc.ctypes.data)
+        vol /= float(self.nelem)
+        g = vol - self.volfrac
+        L.update_solution(self.x.ctypes.data, self.xnew.ctypes.data, self.dv.ctypes.data, self.dc.ctypes.data,
+                          self.nelem_padded, g)
+        change = L.compute_change(self.x.ctypes.data, self.xnew.ctypes.data, self.nelem_padded)
+        L.applyDensityFilter(self.gc, self.rmin, self.x.ctypes.data, self.xPhys.ctypes.data)
+        return {"c": c.value, "vol": vol, "change": change, "cgiters": it.value}
+
+    def transfer_bytes(self, reset=False):
+        h, d = ctypes.c_long(0), ctypes.c_long(0)
+        self.L.topopt_ref_transfer_bytes(ctypes.byref(h), ctypes.byref(d), 1 if reset else 0)
+        return h.value, d.value
+
+    def close(self):
+        if getattr(self, "gc", None) is not None:
+            self.L.freeGPUGrid(ctypes.byref(self.gpu), self.nl)
+            self.L.freeGC(ctypes.byref(self.gc), self.nl)
+            self.gc = None

@@ -81,10 +81,36 @@ tp_ctx* ctx_for(int nelx, int nely, int nelz, int nl) {
   return c;
 }
 
-// smallest level count that holds level `need` (and is valid for the grid)
+// A context holding level `need` for the grid. A cached context of the grid
+// with that many levels or more serves (the entry points that need no
+// particular level count -- volume, compliance, filter -- then share the
+// solver's context). Otherwise a new one gets the most levels the grid's
+// divisibility allows while its coarsest level stays above ~5k DOFs, and at
+// least `need`: with too few levels the coarsest level's band Cholesky would
+// hold a band of the fine grid's size.
 tp_ctx* ctx_levels(const gridContext& gc, int need) {
-  int nl = need < 2 ? 2 : need;
-  return ctx_for((int)gc.nelx, (int)gc.nely, (int)gc.nelz, nl);
+  const int nx = (int)gc.nelx, ny = (int)gc.nely, nz = (int)gc.nelz;
+  if (need < 2) need = 2;
+  tp_ctx* best = nullptr;
+  int best_nl = 0;
+  for (auto& kv : g_ctx) {
+    const auto& k = kv.first;
+    if (std::get<0>(k) == nx && std::get<1>(k) == ny && std::get<2>(k) == nz && std::get<3>(k) >= need &&
+        std::get<3>(k) > best_nl) {
+      best = kv.second;
+      best_nl = std::get<3>(k);
+    }
+  }
+  if (best) return best;
+  int nl = need;
+  for (;;) {
+    const int q = 1 << nl;  // the next level count's coarsening factor
+    if (nl + 1 > 8 || nx % q || ny % q || nz % q) break;
+    const long coarse = 3L * (nx / q + 1) * (ny / q + 1) * (nz / q + 1);
+    if (coarse < 5000) break;
+    nl++;
+  }
+  return ctx_for(nx, ny, nz, nl);
 }
 
 void check(tp_ctx* c, tp_status st, const char* what) {

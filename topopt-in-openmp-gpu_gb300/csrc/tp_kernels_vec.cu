@@ -9,6 +9,8 @@
 // scalars at d_scal[r * S_COUNT + slot] and its own reduction partials. A
 // column whose relative residual has dropped below the tolerance is frozen
 // (alpha = beta = 0), so the columns still iterating do not disturb it.
+#include <math_constants.h>
+
 #include "tp_internal.h"
 
 namespace tp {
@@ -183,7 +185,13 @@ __global__ void scalars_kernel(double* scal, int what, int nr, double tol, int i
       s[S_RHOOLD] = s[S_RHO];
     }
     if (what == 2 && !done) {
-      s[S_RELRES] = s[S_BNORM2] > 0.0 ? sqrt(s[S_RNORM2]) / sqrt(s[S_BNORM2]) : 0.0;
+      // a non-finite load or residual norm gives a NaN relres (never "below
+      // tol"), so the loop stops and reports it instead of converging
+      const double bn = s[S_BNORM2], rn = s[S_RNORM2];
+      if (!isfinite(bn) || !isfinite(rn))
+        s[S_RELRES] = CUDART_NAN;
+      else
+        s[S_RELRES] = bn > 0.0 ? sqrt(rn) / sqrt(bn) : 0.0;
       if (s[S_RELRES] < tol) {
         s[S_CONV] = 1.0;
         s[S_ITER] = iter;
@@ -193,7 +201,11 @@ __global__ void scalars_kernel(double* scal, int what, int nr, double tol, int i
   __syncwarp();
   if (what == 2 && r == 0) {
     double m = 0.0;
-    for (int q = 0; q < nr; q++) m = fmax(m, scal[(long)q * S_COUNT + S_RELRES]);
+    for (int q = 0; q < nr; q++) {
+      const double v = scal[(long)q * S_COUNT + S_RELRES];
+      m = (v > m || v != v) ? v : m;  // a NaN column makes the maximum NaN
+      if (m != m) break;
+    }
     scal[S_MAXRR] = m;
   }
 }

@@ -115,12 +115,14 @@ struct EcPlan {
   bool ok = false;
   int nyt = 0, nzg = 1, ngz = 0, zbase = 0, zextra = 0, ncx = 1, cx = 0;
   int own = 0;  // sweep/residual: stage b and invD in shared memory too
+  int occ3 = 0;  // FP32: the form with registers capped for three CTAs per SM
 };
 struct EcGeom {
   int nx, ny, nz, ex, ey, ez, lim;
   int ngz, zbase, zextra, cx;
   long vstride;               // distance between right-hand sides
   int slab_bytes, own_bytes;  // shared memory per stage
+  int e_bytes;                // shared memory per stage of the moduli E
 };
 // fused consumers of the level-0 operator
 enum { FM_APPLY = 0, FM_APPLY_DOT = 1, FM_JACOBI = 2, FM_RESID = 3 };

@@ -22,7 +22,8 @@
 // already holds layer L-1's share, carried in registers) and start plane
 // L+1. Node planes of the CTA's rows (plus one halo row each side) and, for
 // the sweep, the b and invD rows are staged in shared memory by cp.async,
-// two planes ahead of the compute. The y-neighbour exchange is a warp
+// two planes ahead of the compute; the moduli E of the CTA's element rows
+// one layer ahead, so no thread waits on a global load in the compute. The y-neighbour exchange is a warp
 // shuffle; the column shared by two warps goes through shared memory.
 // Halo work: one element row per z group and one element layer per x chunk
 // are computed twice.
@@ -166,8 +167,11 @@ constexpr int EC_APPLY = FM_APPLY, EC_APPLY_DOT = FM_APPLY_DOT, EC_JACOBI = FM_J
 
 // T: the type of the vectors in memory; A: the type the operator is evaluated
 // in (T itself, or Dsf for double vectors)
-template <typename T, typename A, int MODE, int RMAX>
-__global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restrict__ E, const T* __restrict__ in,
+// MINB: CTAs per SM the register allocation is sized for (1: up to 255
+// registers, the double-vector forms; 2: at most 128, the FP32 default;
+// 3: at most 80, with a few spills, for three 256-thread CTAs per SM)
+template <typename T, typename A, int MODE, int RMAX, int MINB>
+__global__ void __launch_bounds__(256, MINB) fine_ec_kernel(EcGeom g, const T* __restrict__ E, const T* __restrict__ in,
                                                       T* __restrict__ out, const T* __restrict__ bv,
                                                       const T* __restrict__ invD, T omega,
                                                       double* __restrict__ partials) {
@@ -204,6 +208,8 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
   const int kmin = max(K0 - 1, 0), kmax = min(K1, nz - 1);
   const long slab_n = (long)(kmax - kmin + 1) * row3;
   const long own_n = (long)(K1 - K0) * row3;
+  const int ekmin = max(K0 - 1, 0), ekmax = min(K1 - 1, ez - 1);  // element rows of the CTA
+  const long e_n = (long)(ekmax - ekmin + 1) * ey;
   const bool stage_own = g.own_bytes > 0;
 
   const int i0 = blockIdx.y * g.cx;
@@ -213,7 +219,8 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
   unsigned char* sl = smem;
   unsigned char* sb = sl + NST * g.slab_bytes;
   unsigned char* sd = sb + 2 * g.own_bytes;
-  A* bnd_nb = reinterpret_cast<A*>(sd + 2 * g.own_bytes);  // [nzg][nwy][RMAX][6]
+  unsigned char* se = sd + 2 * g.own_bytes;
+  A* bnd_nb = reinterpret_cast<A*>(se + 2 * g.e_bytes);    // [nzg][nwy][RMAX][6]
   A* bnd_own = bnd_nb + nzg * nwy * RMAX * 6;              // [nzg][nwy][RMAX][6]
   A* carry_b = bnd_own + nzg * nwy * RMAX * 6;             // [nzg][nwy + 1][RMAX][3]
 
@@ -224,6 +231,8 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
     if (HASB && stage_own) ec_stage<T>(sb + (p & 1) * g.own_bytes, own_src(bv, p), own_n, tid, nthr);
     if (HASD && stage_own) ec_stage<T>(sd + (p & 1) * g.own_bytes, own_src(invD, p), own_n, tid, nthr);
   };
+  auto e_src = [&](int L) { return E + ((long)L * ez + ekmin) * ey; };
+  auto issue_e = [&](int L) { ec_stage<T>(se + (L & 1) * g.e_bytes, e_src(L), e_n, tid, nthr); };
   // views: value of node row kr, column j, component c at [(kr - base row) * row3 + 3 j + c]
   auto slab_at = [&](int p) { return ec_view<T>(sl + (p % NST) * g.slab_bytes, slab_src(p)); };
 
@@ -267,6 +276,7 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
   issue_slab(Ls);
   issue_slab(Ls + 1);
   issue_own(Ls);
+  issue_e(Ls);
   cp_async_commit();
 
   A carry[RMAX][3];
@@ -275,18 +285,14 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
   const bool lact = gact && t < ey;
 
   for (int L = Ls; L < Le; ++L) {
-    A Ev[RMAX + 1];
-    const T* EL = E + ((long)L * ez + (k0 - 1)) * ey + t;
-#pragma unroll
-    for (int q = 0; q <= RMAX; q++) {
-      const int ek = k0 - 1 + q;
-      Ev[q] = (lact && q <= nrow && ek >= 0 && ek < ez) ? Cv::in(EL[(long)q * ey]) : A(0);
-    }
     if (L + 2 <= Le) issue_slab(L + 2);
     if (L + 1 <= Le) issue_own(L + 1);
+    if (L + 1 < Le) issue_e(L + 1);
     cp_async_commit();
     cp_async_wait<1>();
     __syncthreads();
+    // E of element row ek of layer L at EL[(ek - ekmin) * ey + t]
+    const T* EL = ec_view<T>(se + (L & 1) * g.e_bytes, e_src(L)) + t;
     const T* u0 = slab_at(L);
     const T* u1 = slab_at(L + 1);
     const T* bL = HASB ? own_at(sb, bv, L) : nullptr;
@@ -324,7 +330,7 @@ __global__ void __launch_bounds__(256) fine_ec_kernel(EcGeom g, const T* __restr
         const int ek = k0 - 1 + q;
         xrow(ek + 1, Xn);
         if (ek >= 0 && ek < ez) {
-          const A Ee = Ev[q];
+          const A Ee = lact ? Cv::in(EL[(long)(ek - ekmin) * ey]) : A(0);
           A Z[24];
 #pragma unroll
           for (int a = 0; a < 4; a++)
@@ -597,12 +603,13 @@ static EcGeom ec_geom(const tp_ctx* c, const EcPlan& p, size_t tsize, bool own, 
   const long row_bytes = 3L * L.ny * (long)tsize;
   g.slab_bytes = (int)roundup16((rows + 2) * row_bytes + 32);
   g.own_bytes = own ? (int)roundup16(rows * row_bytes + 32) : 0;
+  g.e_bytes = (int)roundup16((rows + 1) * (long)L.ey * (long)tsize + 32);
   return g;
 }
 
 static size_t ec_smem(const EcGeom& g, const EcPlan& p, size_t tsize) {
   const int nwy = p.nyt / 32;
-  return 3 * (size_t)g.slab_bytes + 4 * (size_t)g.own_bytes +
+  return 3 * (size_t)g.slab_bytes + 4 * (size_t)g.own_bytes + 2 * (size_t)g.e_bytes +
          tsize * (size_t)(2 * p.nzg * nwy * kEcRmax * 6 + p.nzg * (nwy + 1) * kEcRmax * 3);
 }
 
@@ -612,15 +619,20 @@ static int ec_launch_as(tp_ctx* c, const EcPlan& p, const T* E, const T* in, T* 
   const bool own = (MODE == EC_JACOBI || MODE == EC_RESID) && p.own;
   const EcGeom g = ec_geom(c, p, sizeof(T), own, vstride);
   const size_t smem = ec_smem(g, p, sizeof(T));
-  auto kern = fine_ec_kernel<T, A, MODE, kEcRmax>;
-  static size_t set_for = 0;  // largest size the attribute was raised to
-  if (smem > 48 * 1024 && smem > set_for) {
+  // the register-capped form exists for FP32 vectors (three CTAs per SM)
+  const bool capped = std::is_same<T, float>::value && p.occ3;
+  constexpr int kMinB = std::is_same<T, float>::value ? 2 : 1;
+  auto kern = fine_ec_kernel<T, A, MODE, kEcRmax, kMinB>;
+  if constexpr (std::is_same<T, float>::value)
+    if (capped) kern = fine_ec_kernel<T, A, MODE, kEcRmax, 3>;
+  static size_t set_for[2] = {0, 0};  // largest size the attribute was raised to, per form
+  if (smem > 48 * 1024 && smem > set_for[capped]) {
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
       cudaGetLastError();  // not sticky: the error is reported through c->err
       c->err = "fine_ec: shared memory request of " + std::to_string(smem) + " bytes refused";
       return 0;
     }
-    set_for = smem;
+    set_for[capped] = smem;
   }
   const dim3 grid((unsigned)((p.ngz + p.nzg - 1) / p.nzg), (unsigned)p.ncx, (unsigned)nrhs);
   kern<<<grid, dim3(p.nyt, p.nzg), smem, c->s>>>(g, E, in, out, b, invD, omega, c->d_red);
@@ -720,14 +732,17 @@ void ec_tune(tp_ctx* c, tp::EcPlan* plans, const T* E, const T* in, T* out, cons
         if (!ec_plan(c, nzg, (mult * sms + zctas - 1) / zctas, &p) || p.ncx == last_ncx) continue;
         last_ncx = p.ncx;
         const int nown = (mode == FM_JACOBI || mode == FM_RESID) ? 2 : 1;
-        for (int own = 0; own < nown; own++) {
-          p.own = own;
-          const float ms = ec_time<T>(c, mode, p, E, in, out, b, d);
-          if (ms < tbest) {
-            tbest = ms;
-            best = p;
+        const int nocc = std::is_same<T, float>::value ? 2 : 1;
+        for (int own = 0; own < nown; own++)
+          for (int occ = 0; occ < nocc; occ++) {
+            p.own = own;
+            p.occ3 = occ;
+            const float ms = ec_time<T>(c, mode, p, E, in, out, b, d);
+            if (ms < tbest) {
+              tbest = ms;
+              best = p;
+            }
           }
-        }
       }
     }
     plans[mode] = best;

@@ -63,6 +63,9 @@ def args_parse():
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the default level-0 launch shapes (short runs under a profiler)")
     ap.add_argument("--passes", default="APCMBHD", help="GPU passes to run (see the module docstring)")
+    ap.add_argument("--host-loop", action="store_true",
+                    help="drive every design iteration from the host (no graph launches): for profilers that "
+                         "skip kernels inside conditional graphs")
     ap.add_argument("--batched-shape", default="384x192x192")
     ap.add_argument("--batched-cases", type=int, default=8)
     ap.add_argument("--batched-steps", type=int, default=4)
@@ -385,6 +388,8 @@ def make_ctx(tp, shape, nl, precision, W, fine_arith=None, coarse_arith=None):
     """A context tuned and warmed up (W design iterations, then the design is
     reset by the timed run)."""
     ctx = tp.TopOpt(shape[0], shape[1], shape[2], nl, precision=precision)
+    if HOST_LOOP:
+        ctx.set_device_loop(0)
     if fine_arith is not None:
         ctx.set_fine_arith(fine_arith)
     if coarse_arith is not None:
@@ -496,12 +501,14 @@ def batched_pass(tp, torch, shape, nl, nrhs, nload, W, K, hbm):
 
 
 TUNE = True
+HOST_LOOP = False
 
 
 def main():
-    global TUNE
+    global TUNE, HOST_LOOP
     a = args_parse()
     TUNE = not a.no_tune
+    HOST_LOOP = a.host_loop
     if a.cpu_sample:
         cpu_sample_child(a.cpu_sample)
         return

@@ -168,7 +168,10 @@ tp_status tp_set_cg(tp_ctx* c, double cgtol, int cgmax, int nswp, double omega);
 /* Level-0 kernel selection (no counterpart in the reference): variant 0 =
  * the element-centric, sum-factorised kernel wherever its launch plan
  * applies (nely <= 256, 16-byte aligned vectors), else the node-centric
- * stencil; variant 1 = the node-centric stencil everywhere. */
+ * stencil; variant 1 = the node-centric stencil everywhere; variant 2 =
+ * variant 0 with the FP32 product, sweep and residual on the packed kernel
+ * (two z groups per thread in f32x2 arithmetic). Variants 0 and 2 reset the
+ * FP32 launch plans to that kernel's defaults (tp_autotune re-tunes them). */
 tp_status tp_set_fine_variant(tp_ctx* c, int variant);
 /* Arithmetic of the element-centric level-0 kernel on double vectors (no
  * counterpart in the reference): 0 = FP64; 1 = double-single, pairs of FP32
@@ -205,6 +208,20 @@ tp_status tp_set_coarse_arith(tp_ctx* c, int arith);
  * every such wait runs out. The factor or solve then reports TP_ERR_TIMEOUT
  * and the context stays usable; (0, 0) restores the defaults. */
 tp_status tp_fault_coarse_barrier(tp_ctx* c, long spin, int missing);
+/* Launch plan of the element-centric level-0 kernel for one vector type and
+ * fused mode (no counterpart in the reference): the one tp_autotune chose, or
+ * one set by the caller -- to keep a tuning between runs, or to pick one by
+ * hand. vec = 0 FP32 vectors (the mixed form's V-cycle), 1 double vectors (in
+ * the arithmetic tp_set_fine_arith selected); mode = 0 product, 1 product
+ * with the dot product, 2 damped-Jacobi sweep, 3 residual. plan[0..5] =
+ * {z groups of node rows per CTA, x chunks, staging of b and invD (0 read
+ * from global memory, 1 staged per CTA in shared memory, 2 copied ahead by
+ * each thread, FP32 only), register cap (FP32: 1 = capped for more CTAs per
+ * SM), packed (FP32 modes 0, 2, 3: two z groups per thread in f32x2
+ * arithmetic; groups even), threads along y (read only)}. tp_set_fine_plan
+ * returns TP_ERR_ARG for a plan the grid or the shared memory does not allow. */
+tp_status tp_get_fine_plan(tp_ctx* c, int vec, int mode, int* plan);
+tp_status tp_set_fine_plan(tp_ctx* c, int vec, int mode, const int* plan);
 /* Failure detection of the set-up (host-side fault injection, for tests; no
  * counterpart in the reference, which checks no allocation): with k > 0, the
  * k-th device or pinned-host allocation the library makes from now on fails

@@ -87,8 +87,9 @@ def test_gradients_match_reference(design, cuda, rmin, tag):
     g.close()
 
 
+@pytest.mark.parametrize("h", [1e-5, 1e-6], ids=["h1e-5", "h1e-6"])
 @pytest.mark.parametrize("rmin", [1.5, 2.5])
-def test_autograd_against_central_differences(design, cuda, rmin):
+def test_autograd_against_central_differences(design, cuda, rmin, h):
     torch = cuda
     x0, _ = design
     g = tp.TopOpt(*SHAPE, NL, rmin=rmin)
@@ -104,9 +105,10 @@ def test_autograd_against_central_differences(design, cuda, rmin):
     vol = g_volume(g, torch, xv)
     vol.backward()
     rng = np.random.default_rng(1)
-    # central differences: truncation O(h^2) ~ 1e-10 relative at h = 1e-5, while
-    # the solve's round-off (CG to 1e-12) enters the quotient as noise / h
-    h = 1e-5
+    # central differences: truncation O(h^2) ~ 1e-10 relative at h = 1e-5 (1e-12
+    # at the configured h = 1e-6), while the solve's round-off (CG to 1e-12)
+    # enters the quotient as noise / h, ten times larger at h = 1e-6
+    noise = 1e-5 * (1e-5 / h)
     for e in rng.choice(g.nelem(), 64, replace=False):
         xp, xm = x0.copy(), x0.copy()
         xp[e] += h
@@ -114,12 +116,12 @@ def test_autograd_against_central_differences(design, cuda, rmin):
         cp = fn.apply(torch.from_numpy(xp), g, u0).item()
         cm = fn.apply(torch.from_numpy(xm), g, u0).item()
         fd = (cp - cm) / (2 * h)
-        assert abs(fd - grad[e]) <= 1e-5 * np.max(np.abs(grad)) + 1e-4 * abs(grad[e]), (e, fd, grad[e])
+        assert abs(fd - grad[e]) <= noise * np.max(np.abs(grad)) + 1e-4 * abs(grad[e]), (e, fd, grad[e])
         fdv = (g_volume(g, torch, torch.from_numpy(xp).cuda()).item() -
                g_volume(g, torch, torch.from_numpy(xm).cuda()).item()) / (2 * h)
         # V is linear in x; its difference quotient is limited only by the round-off
-        # of a 65,536-term sum changed by ~1e-11 (a few 1e-6 relative)
-        assert fdv == pytest.approx(xv.grad[e].item(), rel=1e-4, abs=1e-12)
+        # of a 65,536-term sum changed by ~1e-11 (a few 1e-6 relative at h = 1e-5)
+        assert fdv == pytest.approx(xv.grad[e].item(), rel=1e-4 * (1e-5 / h), abs=1e-12)
     g.close()
 
 

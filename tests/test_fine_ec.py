@@ -171,3 +171,71 @@ def test_autotune_keeps_results(cuda):
     assert st1 == 0 and it1 == it
     assert relerr(u_ec, g.download("U")) < 1e-6
     g.close()
+
+
+PK_SHAPES = SHAPES[:6] + [(8, 128, 16), (6, 40, 22)]
+
+
+@pytest.mark.parametrize("shape", PK_SHAPES, ids=["x".join(map(str, s)) for s in PK_SHAPES])
+def test_packed_fp32_kernel(cuda, shape):
+    """The packed FP32 kernel (two z groups per thread in f32x2 arithmetic,
+    tp_set_fine_variant(2)) against the one-group kernel and the node-centric
+    stencil: the FP32 product, and a V-cycle of the mixed form, whose level-0
+    sweeps and residual it runs. Grids with odd group counts leave the second
+    lane of the last thread row empty."""
+    torch = cuda
+    g = tp.TopOpt(*shape, 2, precision=tp.TP_MIXED)
+    x, u = _rand(g, 11)
+    g.upload("xphys", x)
+    g.assemble()
+    uf = torch.from_numpy(u).cuda().float()
+    r = torch.from_numpy(np.random.default_rng(12).uniform(-1, 1, g.ndof(0))).cuda()
+    out = {}
+    for variant in (0, 2, 1):
+        g.set_fine_variant(variant)
+        out[variant] = (g.apply(0, uf).double().cpu().numpy(), g.vcycle(r).cpu().numpy())
+    y64 = g.apply(0, torch.from_numpy(u).cuda()).cpu().numpy()
+    for variant in (0, 1):
+        assert relerr(out[2][0], out[variant][0]) < 1e-5
+        assert relerr(out[2][1], out[variant][1]) < 1e-4
+    assert relerr(out[2][0], y64) < 1e-5
+    g.close()
+
+
+@pytest.mark.parametrize("shape", [(8, 128, 16), (6, 40, 22), (16, 66, 6)], ids=["8x128x16", "6x40x22", "16x66x6"])
+def test_every_fp32_launch_plan(cuda, shape):
+    """Every FP32 launch plan the grid allows (one or two z groups per thread,
+    b and invD from global memory, staged per CTA or copied ahead per thread,
+    both register caps, several x chunkings), set through tp_set_fine_plan,
+    gives the node-centric stencil's product and V-cycle to FP32 accuracy."""
+    torch = cuda
+    g = tp.TopOpt(*shape, 2, precision=tp.TP_MIXED)
+    x, u = _rand(g, 21)
+    g.upload("xphys", x)
+    g.assemble()
+    uf = torch.from_numpy(u).cuda().float()
+    r = torch.from_numpy(np.random.default_rng(22).uniform(-1, 1, g.ndof(0))).cuda()
+    g.set_fine_variant(1)
+    y_ref, z_ref = g.apply(0, uf).double().cpu().numpy(), g.vcycle(r).cpu().numpy()
+    g.set_fine_variant(0)
+    tried = 0
+    for pk in (0, 1):
+        for groups in ((1, 2, 4) if pk == 0 else (2, 4)):
+            for ncx in (1, 3):
+                for own in (0, 1, 2):
+                    for occ in (0, 1):
+                        plan = [groups, ncx, own, occ, pk]
+                        if g.set_fine_plan(0, 2, plan) != 0:
+                            continue
+                        assert g.set_fine_plan(0, 3, plan) == 0
+                        assert g.set_fine_plan(0, 0, [groups, ncx, 0, occ, pk]) == 0
+                        assert g.fine_plan(0, 2)[:5] == plan
+                        tried += 1
+                        y = g.apply(0, uf).double().cpu().numpy()
+                        z = g.vcycle(r).cpu().numpy()
+                        assert relerr(y, y_ref) < 1e-5, plan
+                        assert relerr(z, z_ref) < 1e-4, plan
+    assert tried >= 8
+    assert g.set_fine_plan(0, 1, [2, 1, 0, 0, 1]) == 1  # no packed product with a dot product
+    assert g.set_fine_plan(1, 2, [1, 1, 2, 0, 0]) == 1  # per-thread copies are FP32 only
+    g.close()

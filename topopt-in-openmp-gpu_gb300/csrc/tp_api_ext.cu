@@ -66,8 +66,11 @@ tp_status tp_set_cg(tp_ctx* c, double cgtol, int cgmax, int nswp, double omega) 
 }
 
 tp_status tp_set_fine_variant(tp_ctx* c, int variant) {
-  if (!c || variant < 0 || variant > 1) return TP_ERR_ARG;
-  c->fine_variant = variant;
+  if (!c || variant < 0 || variant > 2) return TP_ERR_ARG;
+  // 2 is the element-centric kernel with the packed FP32 plans; choosing 0 or
+  // 2 resets the FP32 plans to that kernel's defaults
+  if (variant != 1) ec_select_packed(c, variant == 2);
+  c->fine_variant = variant == 1 ? 1 : 0;
   graph_free(c);
   return TP_OK;
 }

@@ -62,6 +62,7 @@ enum Scalar {
   S_MAXRR,  // (column 0) largest relres over the columns
   S_IT,     // (column 0) iteration counter of the captured CG loop
   S_G,      // (column 0) constraint value g = vol - volfrac of the OC bisection
+  S_RL,     // (column 0) 1/sqrt(lmid) of the next bisection step, formed once per step
   S_COUNT
 };
 
@@ -114,8 +115,10 @@ struct Coarse {
 struct EcPlan {
   bool ok = false;
   int nyt = 0, nzg = 1, ngz = 0, zbase = 0, zextra = 0, ncx = 1, cx = 0;
-  int own = 0;  // sweep/residual: stage b and invD in shared memory too
-  int occ3 = 0;  // FP32: the form with registers capped for three CTAs per SM
+  int own = 0;  // sweep/residual: 1 stage b and invD in shared memory per CTA; 2 (packed
+                //   kernel) each thread copies its own entries ahead into shared memory
+  int occ3 = 0;  // FP32: the form with registers capped for more CTAs per SM
+  int pk = 0;    // FP32: the packed kernel (two z groups per thread, f32x2 arithmetic)
 };
 struct EcGeom {
   int nx, ny, nz, ex, ey, ez, lim;
@@ -123,6 +126,7 @@ struct EcGeom {
   long vstride;               // distance between right-hand sides
   int slab_bytes, own_bytes;  // shared memory per stage
   int e_bytes;                // shared memory per stage of the moduli E
+  int pt_bytes;               // packed kernel: per-thread slots of b and invD (0: not used)
 };
 // fused consumers of the level-0 operator
 enum { FM_APPLY = 0, FM_APPLY_DOT = 1, FM_JACOBI = 2, FM_RESID = 3 };
@@ -277,6 +281,7 @@ bool set_fine_kz(const double* ke0, double* kz_out);
 void set_design_kz(const double* kz45);  // the KZ values for the element energies (tp_kernels_design.cu)
 bool ec_plan(tp_ctx* c, int nzg, int ncx, EcPlan* p);
 void ec_default_plans(tp_ctx* c);
+void ec_select_packed(tp_ctx* c, bool on);  // FP32 plans: packed kernel defaults or one-group defaults
 template <typename T> int fine_ec(tp_ctx* c, int mode, const T* E, const T* in, T* out, const T* b, const T* invD, T omega, int nr = 1);
 
 // levels >= 1 (assembled block stencils)

@@ -382,7 +382,9 @@ __global__ void oc_step_kernel(long n, const double* __restrict__ x, const doubl
                                double* __restrict__ scal, double* __restrict__ partials) {
   if (scal[S_OCDONE] != 0.0) return;
   const double lmid = 0.5 * (scal[S_L2] + scal[S_L1]);
-  const double rl = 1.0 / sqrt(lmid);
+  // 1/sqrt(lmid), formed once per step by the kernel that set l1 and l2 (FP64
+  // division and square root are slow enough here to matter once per thread)
+  const double rl = scal[S_RL];
   double s = 0.0;
   for (long e = blockIdx.x * 256L + threadIdx.x; e < n; e += (long)gridDim.x * 256) {
     const double xe = x[e];
@@ -420,6 +422,7 @@ __global__ void oc_finish_kernel(const double* __restrict__ partials, int nb, do
     scal[S_LMID] = lmid;
     scal[S_GT] = gt;
     scal[S_OCDONE] = ((nl2 - nl1) / (nl1 + nl2) > 1e-6) ? 0.0 : 1.0;
+    scal[S_RL] = 1.0 / sqrt(0.5 * (nl2 + nl1));
     scal[S_TMP0] += 1.0;  // steps taken
   }
 }
@@ -462,6 +465,7 @@ __global__ void oc_init_kernel(double* scal) {
   scal[S_OCDONE] = ((1e9 - 0.0) / (0.0 + 1e9) > 1e-6) ? 0.0 : 1.0;
   scal[S_TMP0] = 0.0;
   scal[S_LMID] = 0.0;
+  scal[S_RL] = 1.0 / sqrt(0.5 * (1e9 + 0.0));
 }
 
 // Bisection over any n design variables; leaves xnew, S_CHANGE and, when

@@ -39,6 +39,7 @@ namespace tp {
 __constant__ double c_kz[45];
 __constant__ float c_kzf[45];
 __constant__ float c_kzd[45][2];  // c_kz as double-single pairs
+__constant__ float2 c_kz2[45];     // c_kzf as (k, k) pairs for the packed FP32 kernel
 
 // storage type T <-> arithmetic type A of the element-centric kernel
 template <typename A, typename T>
@@ -119,6 +120,9 @@ bool set_fine_kz(const double* ke0, double* kz_out) {
   if (ok) {
     cudaMemcpyToSymbol(c_kz, v, sizeof(v));
     cudaMemcpyToSymbol(c_kzf, vf, sizeof(vf));
+    float2 v2[45];
+    for (int i = 0; i < 45; i++) v2[i] = make_float2(vf[i], vf[i]);
+    cudaMemcpyToSymbol(c_kz2, v2, sizeof(v2));
     cudaMemcpyToSymbol(c_kzd, vd, sizeof(vd));
   }
   return ok;
@@ -128,6 +132,10 @@ bool set_fine_kz(const double* ke0, double* kz_out) {
 __device__ __forceinline__ void cp_async16(void* dst, const void* src, int bytes) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
@@ -223,6 +231,11 @@ __global__ void __launch_bounds__(256, MINB) fine_ec_kernel(EcGeom g, const T* _
   A* bnd_nb = reinterpret_cast<A*>(se + 2 * g.e_bytes);    // [nzg][nwy][RMAX][6]
   A* bnd_own = bnd_nb + nzg * nwy * RMAX * 6;              // [nzg][nwy][RMAX][6]
   A* carry_b = bnd_own + nzg * nwy * RMAX * 6;             // [nzg][nwy + 1][RMAX][3]
+  // FP32 sweeps and residuals: b and invD of the thread's own nodes in this
+  // layer, copied by the thread itself when the layer starts, slot i of
+  // thread tid at [i * nthr + tid], i = (r * 2 + array) * 3 + c
+  T* slot = reinterpret_cast<T*>(carry_b + nzg * (nwy + 1) * RMAX * 3);
+  const bool own_pt = HASB && sizeof(T) == 4 && g.pt_bytes > 0;
 
   auto slab_src = [&](int p) { return in + ((long)p * nz + kmin) * row3; };
   auto own_src = [&](const T* v, int p) { return v + ((long)p * nz + K0) * row3; };
@@ -240,7 +253,8 @@ __global__ void __launch_bounds__(256, MINB) fine_ec_kernel(EcGeom g, const T* _
 
   double dot = 0.0;
   // output components [c0, c1) of plane P, node row kr, column j
-  auto epi = [&](const T* uP, const T* bP, const T* dP, int P, int kr, int j, int c0, int c1, const A* y) {
+  auto epi = [&](const T* uP, const T* bP, const T* dP, int P, int kr, int j, int c0, int c1, const A* y,
+                 bool from_slot) {
     if (P < i0) return;
     const long li = (long)(kr - kmin) * row3 + 3 * j;
     const long n3 = ((long)P * nz + kr) * row3 + 3 * j;
@@ -254,10 +268,11 @@ __global__ void __launch_bounds__(256, MINB) fine_ec_kernel(EcGeom g, const T* _
       if (MODE == EC_APPLY || MODE == EC_APPLY_DOT) out[n3 + c] = yc;
       if (MODE == EC_APPLY_DOT) dot += (double)u * (double)yc;
       if (HASB) {
-        const T b = stage_own ? bP[lo + c] : bv[n3 + c];
+        const int r = kr - k0;
+        const T b = from_slot ? slot[((r * 2 + 0) * 3 + c) * nthr + tid] : stage_own ? bP[lo + c] : bv[n3 + c];
         if (MODE == EC_RESID) out[n3 + c] = b - yc;
         if (MODE == EC_JACOBI) {
-          const T d = stage_own ? dP[lo + c] : invD[n3 + c];
+          const T d = from_slot ? slot[((r * 2 + 1) * 3 + c) * nthr + tid] : stage_own ? dP[lo + c] : invD[n3 + c];
           out[n3 + c] = u + omega * d * (b - yc);
         }
       }
@@ -283,13 +298,31 @@ __global__ void __launch_bounds__(256, MINB) fine_ec_kernel(EcGeom g, const T* _
 #pragma unroll
   for (int r = 0; r < RMAX; r++) carry[r][0] = carry[r][1] = carry[r][2] = A(0);
   const bool lact = gact && t < ey;
+  const bool pt_thread = own_pt && lact && lane != 31;
+  auto issue_pt = [&](int L) {
+    if constexpr (sizeof(T) == 4) {
+      if (!pt_thread || L < i0) return;
+#pragma unroll
+      for (int r = 0; r < RMAX; r++) {
+        if (r >= nrow) break;
+        const long n = (((long)L * nz + k0 + r) * ny + t + 1) * 3;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          cp_async4(&slot[((r * 2 + 0) * 3 + c) * nthr + tid], bv + n + c);
+          if (HASD) cp_async4(&slot[((r * 2 + 1) * 3 + c) * nthr + tid], invD + n + c);
+        }
+      }
+    }
+  };
 
   for (int L = Ls; L < Le; ++L) {
+    issue_pt(L);
+    cp_async_commit();
     if (L + 2 <= Le) issue_slab(L + 2);
     if (L + 1 <= Le) issue_own(L + 1);
     if (L + 1 < Le) issue_e(L + 1);
     cp_async_commit();
-    cp_async_wait<1>();
+    cp_async_wait<2>();  // this layer's slot copies and the next stages may still be in flight
     __syncthreads();
     // E of element row ek of layer L at EL[(ek - ekmin) * ey + t]
     const T* EL = ec_view<T>(se + (L & 1) * g.e_bytes, e_src(L)) + t;
@@ -418,6 +451,7 @@ __global__ void __launch_bounds__(256, MINB) fine_ec_kernel(EcGeom g, const T* _
         if (q >= 1) {
           // node row ek = k0 + r is complete: x and y butterflies back
           const int r = q - 1;
+          if (q == 1) cp_async_wait<1>();  // the thread's slot copies of this layer
           A own0[3], own1[3], nb0[3], nb1[3];
 #pragma unroll
           for (int c = 0; c < 3; c++) {
@@ -455,7 +489,7 @@ __global__ void __launch_bounds__(256, MINB) fine_ec_kernel(EcGeom g, const T* _
               y[c] = carry[r][c] + own0[c] + rv0[c];
               carry[r][c] = own1[c] + rv1[c];
             }
-            epi(u0, bL, dL, L, k0 + r, t + 1, 0, 3, y);
+            epi(u0, bL, dL, L, k0 + r, t + 1, 0, 3, y, own_pt);
           }
         }
 #pragma unroll
@@ -498,7 +532,7 @@ __global__ void __launch_bounds__(256, MINB) fine_ec_kernel(EcGeom g, const T* _
       const A v = cr + o0 + n0;
       cr = o1 + n1;
       const A y[3] = {v, v, v};  // only component tc is stored
-      epi(u0, bL, dL, L, k0 + tr, j, tc, tc + 1, y);
+      epi(u0, bL, dL, L, k0 + tr, j, tc, tc + 1, y, false);
     }
     __syncthreads();
   }
@@ -513,12 +547,12 @@ __global__ void __launch_bounds__(256, MINB) fine_ec_kernel(EcGeom g, const T* _
     if (lact && lane != 31) {
 #pragma unroll
       for (int r = 0; r < RMAX; r++)
-        if (r < nrow) epi(uP, bP, dP, P, k0 + r, t + 1, 0, 3, carry[r]);
+        if (r < nrow) epi(uP, bP, dP, P, k0 + r, t + 1, 0, 3, carry[r], false);
     }
     if (tail) {
       const A v = carry_b[((tz * (nwy + 1) + tcb) * RMAX + tr) * 3 + tc];
       const A y[3] = {v, v, v};
-      epi(uP, bP, dP, P, k0 + tr, 32 * tcb, tc, tc + 1, y);
+      epi(uP, bP, dP, P, k0 + tr, 32 * tcb, tc, tc + 1, y, false);
     }
   }
   if (MODE == EC_APPLY_DOT) {
@@ -531,6 +565,359 @@ __global__ void __launch_bounds__(256, MINB) fine_ec_kernel(EcGeom g, const T* _
       double s = 0.0;
       for (int w = 0; w < nthr / 32; w++) s += red[w];
       partials[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = s;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP32 sweep, residual and product with packed arithmetic. The schedule and
+// the arithmetic are those of fine_ec_kernel, but each thread carries two z
+// groups of its CTA (groups 2 tz and 2 tz + 1, "lanes" A and B) as the two
+// halves of float2 values, so every add, multiply and multiply-add of the
+// operator is one f32x2 instruction (sm_100 and later) for two elements. A
+// lane's rows outside its group, and element rows outside the grid, get the
+// modulus E = 0 and read their node values from a clamped (valid) row of the
+// staged slab: they contribute exact zeros, and the arithmetic needs no
+// per-lane branch. Indices are 32-bit (the plan requires 3 * nodes < 2^31).
+__device__ __forceinline__ float2 pk_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 pk_sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ float2 pk_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 pk_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 pk_shfl_down(float2 v, int d) {
+  return make_float2(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d));
+}
+
+template <int MODE, int RMAX, int MINB>
+__global__ void __launch_bounds__(256, MINB) fine_pk_kernel(EcGeom g, const float* __restrict__ E,
+                                                            const float* __restrict__ in, float* __restrict__ out,
+                                                            const float* __restrict__ bv,
+                                                            const float* __restrict__ invD, float omega) {
+  constexpr int NST = 3;  // slab stages: planes L, L+1 in use, L+2 in flight
+  static_assert(3 * RMAX <= 16, "one shared-column item per thread");
+  static_assert(MODE != EC_APPLY_DOT, "the packed kernel has no dot product");
+  constexpr bool HASB = (MODE == EC_JACOBI || MODE == EC_RESID);
+  constexpr bool HASD = (MODE == EC_JACOBI);
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int t = threadIdx.x, tz = threadIdx.y;
+  const int nyt = blockDim.x, npr = blockDim.y, nzg = 2 * npr;
+  const int nthr = nyt * npr, tid = t + nyt * tz;
+  const int lane = t & 31, nwy = nyt >> 5;
+  const int ny = g.ny, nz = g.nz, ey = g.ey, ez = g.ez;
+  const int row3 = 3 * ny;
+  {
+    const long rs = (long)blockIdx.z * g.vstride;
+    in += rs;
+    out += rs;
+    if (HASB) bv += rs;
+  }
+  const int gfirst = blockIdx.x * nzg;
+  const int glast = min(gfirst + nzg, g.ngz) - 1;
+  int K0, K1, dum;
+  ec_rows(g, gfirst, K0, dum);
+  ec_rows(g, glast, dum, K1);
+  // lane A: group gfirst + 2 tz, lane B: the next one; a missing group has
+  // the empty row range [K1, K1)
+  int k0A = K1, k1A = K1, k0B = K1, k1B = K1;
+  if (gfirst + 2 * tz <= glast) ec_rows(g, gfirst + 2 * tz, k0A, k1A);
+  if (gfirst + 2 * tz + 1 <= glast) ec_rows(g, gfirst + 2 * tz + 1, k0B, k1B);
+  const int nrowA = k1A - k0A, nrowB = k1B - k0B;
+  const int nrow = max(nrowA, nrowB);
+  const bool tact = nrow > 0;
+  const int kmin = max(K0 - 1, 0), kmax = min(K1, nz - 1);
+  const int slab_n = (kmax - kmin + 1) * row3;
+  const int own_n = (K1 - K0) * row3;
+  const int ekmin = max(K0 - 1, 0), ekmax = min(K1 - 1, ez - 1);
+  const int e_n = (ekmax - ekmin + 1) * ey;
+  const bool stage_own = g.own_bytes > 0;
+
+  const int i0 = blockIdx.y * g.cx;
+  const int i1 = min(i0 + g.cx, g.nx);
+  const int Ls = max(i0 - 1, 0), Le = min(i1, g.ex);
+
+  unsigned char* sl = smem;
+  unsigned char* sb = sl + NST * g.slab_bytes;
+  unsigned char* sd = sb + 2 * g.own_bytes;
+  unsigned char* se = sd + 2 * g.own_bytes;
+  float2* bnd_nb = reinterpret_cast<float2*>(se + 2 * g.e_bytes);  // [npr][nwy][RMAX][6]
+  float2* bnd_own = bnd_nb + npr * nwy * RMAX * 6;                  // [npr][nwy][RMAX][6]
+  float2* carry_b = bnd_own + npr * nwy * RMAX * 6;                 // [npr][nwy + 1][RMAX][3]
+  // b and invD of the thread's own nodes in this layer, copied by the thread
+  // itself when the layer starts: slot i of thread tid at [i * nthr + tid],
+  // i = ((r * 2 + array) * 3 + c) * 2 + lane
+  float* slot = reinterpret_cast<float*>(carry_b + npr * (nwy + 1) * RMAX * 3);
+  const bool own_pt = HASB && g.pt_bytes > 0;
+
+  auto slab_src = [&](int p) { return in + ((long)p * nz + kmin) * row3; };
+  auto own_src = [&](const float* v, int p) { return v + ((long)p * nz + K0) * row3; };
+  auto e_src = [&](int L) { return E + ((long)L * ez + ekmin) * ey; };
+  auto issue_slab = [&](int p) { ec_stage<float>(sl + (p % NST) * g.slab_bytes, slab_src(p), slab_n, tid, nthr); };
+  auto issue_own = [&](int p) {
+    if (HASB && stage_own) ec_stage<float>(sb + (p & 1) * g.own_bytes, own_src(bv, p), own_n, tid, nthr);
+    if (HASD && stage_own) ec_stage<float>(sd + (p & 1) * g.own_bytes, own_src(invD, p), own_n, tid, nthr);
+  };
+  auto issue_e = [&](int L) { ec_stage<float>(se + (L & 1) * g.e_bytes, e_src(L), e_n, tid, nthr); };
+  auto slab_at = [&](int p) { return ec_view<float>(sl + (p % NST) * g.slab_bytes, slab_src(p)); };
+  auto own_at = [&](unsigned char* base, const float* v, int p) -> const float* {
+    if (!stage_own) return nullptr;
+    return ec_view<float>(base + (p & 1) * g.own_bytes, own_src(v, p));
+  };
+  for (int q = tid; q < npr * (nwy + 1) * RMAX * 3; q += nthr) carry_b[q] = make_float2(0.f, 0.f);
+
+  const float2 om2 = make_float2(omega, omega);
+  // output components [c0, c1) of plane P, node row r of both lanes, column j;
+  // from_slot: b and invD from the thread's slots (its own column t + 1)
+  auto epi = [&](const float* uP, const float* bP, const float* dP, int P, int r, int j, int c0, int c1,
+                 const float2* y, bool from_slot) {
+    if (P < i0) return;
+    const bool vA = r < nrowA, vB = r < nrowB;
+    // rows of a lane past its group are read clamped (and not stored)
+    const int krA = min(k0A + r, K1 - 1), krB = min(k0B + r, K1 - 1);
+    const int liA = (krA - kmin) * row3 + 3 * j, liB = (krB - kmin) * row3 + 3 * j;
+    const int loA = (krA - K0) * row3 + 3 * j, loB = (krB - K0) * row3 + 3 * j;
+    const int nA = ((P * nz + krA) * ny + j) * 3, nB = ((P * nz + krB) * ny + j) * 3;
+    const bool fixed = P == 0 && (j < g.lim || j >= ny - g.lim);  // identity rows
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      if (c < c0 || c >= c1) continue;
+      const float2 u = make_float2(uP[liA + c], uP[liB + c]);
+      const float2 yc = fixed ? u : y[c];
+      float2 o = yc;
+      if (HASB) {
+        const int sb0 = ((r * 2 + 0) * 3 + c) * 2, sd0 = ((r * 2 + 1) * 3 + c) * 2;
+        const float2 b = from_slot ? make_float2(slot[sb0 * nthr + tid], slot[(sb0 + 1) * nthr + tid])
+                         : stage_own ? make_float2(bP[loA + c], bP[loB + c])
+                                     : make_float2(bv[nA + c], bv[nB + c]);
+        const float2 rr = pk_sub(b, yc);
+        if (MODE == EC_RESID) o = rr;
+        if (MODE == EC_JACOBI) {
+          const float2 d = from_slot ? make_float2(slot[sd0 * nthr + tid], slot[(sd0 + 1) * nthr + tid])
+                           : stage_own ? make_float2(dP[loA + c], dP[loB + c])
+                                       : make_float2(invD[nA + c], invD[nB + c]);
+          o = pk_fma(pk_mul(om2, d), rr, u);
+        }
+      }
+      if (vA) out[nA + c] = o.x;
+      if (vB) out[nB + c] = o.y;
+    }
+  };
+  // the columns shared by two warps (0, 32, 64, ...): one (column, row,
+  // component) item per thread of the thread row, both lanes at once
+  const int ncb = ey / 32 + 1;
+  const bool tail = tact && t < ncb * nrow * 3;
+  const int tc = tail ? t % 3 : 0, tr = tail ? (t / 3) % nrow : 0, tcb = tail ? t / (3 * nrow) : 0;
+
+  issue_slab(Ls);
+  issue_slab(Ls + 1);
+  issue_own(Ls);
+  issue_e(Ls);
+  cp_async_commit();
+
+  float2 carry[RMAX][3];
+#pragma unroll
+  for (int r = 0; r < RMAX; r++) carry[r][0] = carry[r][1] = carry[r][2] = make_float2(0.f, 0.f);
+  const bool lact = tact && t < ey;
+  const int tt = min(t, ey - 1);  // column pair read by the thread (an idle thread reads a valid one)
+  // the thread's own b and invD entries of plane L (column t + 1, rows of both lanes)
+  const bool pt_thread = own_pt && lact && lane != 31;
+  auto issue_pt = [&](int L) {
+    if (!pt_thread || L < i0) return;
+#pragma unroll
+    for (int r = 0; r < RMAX; r++)
+#pragma unroll
+      for (int ln = 0; ln < 2; ln++) {
+        if (r >= (ln ? nrowB : nrowA)) continue;
+        const long n = (((long)L * nz + (ln ? k0B : k0A) + r) * ny + t + 1) * 3;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          cp_async4(&slot[(((r * 2 + 0) * 3 + c) * 2 + ln) * nthr + tid], bv + n + c);
+          if (HASD) cp_async4(&slot[(((r * 2 + 1) * 3 + c) * 2 + ln) * nthr + tid], invD + n + c);
+        }
+      }
+  };
+
+  for (int L = Ls; L < Le; ++L) {
+    issue_pt(L);
+    cp_async_commit();
+    if (L + 2 <= Le) issue_slab(L + 2);
+    if (L + 1 <= Le) issue_own(L + 1);
+    if (L + 1 < Le) issue_e(L + 1);
+    cp_async_commit();
+    cp_async_wait<2>();  // this layer's slot copies and the next stages may still be in flight
+    __syncthreads();
+    const float* EL = ec_view<float>(se + (L & 1) * g.e_bytes, e_src(L)) + tt;
+    const float* u0 = slab_at(L);
+    const float* u1 = slab_at(L + 1);
+    const float* bL = HASB ? own_at(sb, bv, L) : nullptr;
+    const float* dL = HASD ? own_at(sd, invD, L) : nullptr;
+
+    if (tact) {
+      // y and x butterflies of node rows krA, krB: X[(bx*2 + by)*3 + c]
+      auto xrow = [&](int krA, int krB, float2* X) {
+        const int oA = (min(max(krA, kmin), kmax) - kmin) * row3 + 3 * tt;
+        const int oB = (min(max(krB, kmin), kmax) - kmin) * row3 + 3 * tt;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          const float2 a0 = make_float2(u0[oA + c], u0[oB + c]), a1 = make_float2(u0[oA + 3 + c], u0[oB + 3 + c]);
+          const float2 b0 = make_float2(u1[oA + c], u1[oB + c]), b1 = make_float2(u1[oA + 3 + c], u1[oB + 3 + c]);
+          const float2 s0 = pk_add(a0, a1), d0 = pk_sub(a1, a0), s1 = pk_add(b0, b1), d1 = pk_sub(b1, b0);
+          X[c] = pk_add(s0, s1);
+          X[3 + c] = pk_add(d0, d1);
+          X[6 + c] = pk_sub(s1, s0);
+          X[9 + c] = pk_sub(d1, d0);
+        }
+      };
+      // modulus of element row k0 - 1 + q of each lane (0 outside its group or the grid)
+      auto emod = [&](int q) {
+        const int eA = k0A - 1 + q, eB = k0B - 1 + q;
+        const bool okA = lact && q <= nrowA && eA >= 0 && eA < ez;
+        const bool okB = lact && q <= nrowB && eB >= 0 && eB < ez;
+        return make_float2(okA ? EL[(eA - ekmin) * ey] : 0.f, okB ? EL[(eB - ekmin) * ey] : 0.f);
+      };
+      float2 Xp[12], Xn[12], accp[12], accn[12];
+      xrow(k0A - 1, k0B - 1, Xp);
+#pragma unroll
+      for (int a = 0; a < 12; a++) accp[a] = make_float2(0.f, 0.f);
+#define PK_K(i) c_kz2[i]
+#define PK_D2(i, a, j, b) pk_fma(PK_K(j), Z[b], pk_mul(PK_K(i), Z[a]))
+#define PK_D3(i, a, j, b, k, c) pk_fma(PK_K(k), Z[c], PK_D2(i, a, j, b))
+#define PK_ONE(q, w1)                  \
+  {                                    \
+    const float2 w = w1;               \
+    accp[q] = pk_fma(nE, w, accp[q]);  \
+    accn[q] = pk_mul(Ee, w);           \
+  }
+#define PK_TWO(q, w0e, w1e)                                \
+  {                                                        \
+    const float2 w0 = w0e, w1 = w1e;                       \
+    accp[q] = pk_fma(Ee, pk_sub(w0, w1), accp[q]);         \
+    accn[q] = pk_mul(Ee, pk_add(w0, w1));                  \
+  }
+#pragma unroll
+      for (int q = 0; q <= RMAX; q++) {
+        if (q > nrow) break;
+        xrow(k0A + q, k0B + q, Xn);
+        const float2 Ee = emod(q);
+        const float2 nE = make_float2(-Ee.x, -Ee.y);
+        float2 Z[24];
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            // a = bx*2 + by  ->  b = bx*4 + by*2 + bz = 2a + bz
+            Z[(2 * a) * 3 + c] = pk_add(Xp[a * 3 + c], Xn[a * 3 + c]);
+            Z[(2 * a + 1) * 3 + c] = pk_sub(Xn[a * 3 + c], Xp[a * 3 + c]);
+          }
+        // w = KZ Z by pairs (bz = 0, 1) of each (bx, by, c): node row ek takes
+        // E (w0 - w1), node row ek + 1 takes E (w0 + w1)
+        PK_ONE(0, PK_D2(0, 3, 1, 14));
+        PK_ONE(1, PK_D2(2, 4, 3, 8));
+        PK_ONE(2, PK_D3(4, 5, 5, 7, 6, 12));
+        PK_TWO(3, PK_D2(7, 6, 8, 13), PK_D3(9, 9, 10, 16, 11, 20));
+        PK_TWO(4, PK_D3(12, 5, 13, 7, 14, 12), PK_D2(15, 10, 16, 15));
+        PK_TWO(5, PK_D2(17, 4, 18, 8), PK_D2(19, 11, 20, 18));
+        PK_TWO(6, PK_D3(21, 5, 22, 7, 23, 12), PK_D2(24, 10, 25, 15));
+        PK_TWO(7, PK_D2(26, 6, 27, 13), PK_D3(28, 9, 29, 16, 30, 20));
+        PK_TWO(8, PK_D2(31, 3, 32, 14), PK_D2(33, 17, 34, 19));
+        PK_TWO(9, PK_D2(35, 11, 36, 18), pk_mul(PK_K(37), Z[21]));
+        PK_TWO(10, PK_D2(38, 17, 39, 19), pk_mul(PK_K(40), Z[22]));
+        PK_TWO(11, PK_D3(41, 9, 42, 16, 43, 20), pk_mul(PK_K(44), Z[23]));
+        if (q >= 1) {
+          // node row k0 + r of each lane is complete: x and y butterflies back
+          const int r = q - 1;
+          if (q == 1) cp_async_wait<1>();  // the thread's slot copies of this layer
+          float2 own0[3], own1[3], nb0[3], nb1[3];
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            const float2 p0s = pk_sub(accp[c], accp[6 + c]), p0d = pk_sub(accp[3 + c], accp[9 + c]);
+            const float2 p1s = pk_add(accp[c], accp[6 + c]), p1d = pk_add(accp[3 + c], accp[9 + c]);
+            own0[c] = pk_add(p0s, p0d);  // plane L,   column t + 1
+            own1[c] = pk_add(p1s, p1d);  // plane L+1, column t + 1
+            nb0[c] = pk_sub(p0s, p0d);   // plane L,   column t
+            nb1[c] = pk_sub(p1s, p1d);   // plane L+1, column t
+          }
+          float2 rv0[3], rv1[3];
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            rv0[c] = pk_shfl_down(nb0[c], 1);
+            rv1[c] = pk_shfl_down(nb1[c], 1);
+          }
+          const int bo = ((tz * nwy + (t >> 5)) * RMAX + r) * 6;
+          if (lane == 0) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+              bnd_nb[bo + c] = nb0[c];
+              bnd_nb[bo + 3 + c] = nb1[c];
+            }
+          }
+          if (lane == 31) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+              bnd_own[bo + c] = own0[c];
+              bnd_own[bo + 3 + c] = own1[c];
+            }
+          } else if (lact) {
+            float2 y[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+              y[c] = pk_add(pk_add(carry[r][c], own0[c]), rv0[c]);
+              carry[r][c] = pk_add(own1[c], rv1[c]);
+            }
+            epi(u0, bL, dL, L, r, t + 1, 0, 3, y, own_pt);
+          }
+        }
+#pragma unroll
+        for (int a = 0; a < 12; a++) {
+          Xp[a] = Xn[a];
+          accp[a] = accn[a];
+        }
+      }
+#undef PK_TWO
+#undef PK_ONE
+#undef PK_D3
+#undef PK_D2
+#undef PK_K
+    }
+    __syncthreads();
+    // columns 0, 32, 64, ...: the own share of lane 31 of the warp on the
+    // left plus the share of lane 0 of the warp on the right
+    if (tail) {
+      const int j = 32 * tcb;
+      float2 o0 = make_float2(0.f, 0.f), o1 = o0, n0 = o0, n1 = o0;
+      if (tcb >= 1) {
+        const int bo = ((tz * nwy + tcb - 1) * RMAX + tr) * 6;
+        o0 = bnd_own[bo + tc];
+        o1 = bnd_own[bo + 3 + tc];
+      }
+      if (j < ey) {
+        const int bo = ((tz * nwy + tcb) * RMAX + tr) * 6;
+        n0 = bnd_nb[bo + tc];
+        n1 = bnd_nb[bo + 3 + tc];
+      }
+      float2& cr = carry_b[((tz * (nwy + 1) + tcb) * RMAX + tr) * 3 + tc];
+      const float2 v = pk_add(pk_add(cr, o0), n0);
+      cr = pk_add(o1, n1);
+      const float2 y[3] = {v, v, v};  // only component tc is stored
+      epi(u0, bL, dL, L, tr, j, tc, tc + 1, y, false);
+    }
+    __syncthreads();
+  }
+  cp_async_wait<0>();
+  __syncthreads();
+  if (i1 == g.nx && tact) {
+    // last plane (x = nelx): only layer nelx-1 touches it, its share is the carry
+    const int P = g.ex;
+    const float* uP = slab_at(P);
+    const float* bP = HASB ? own_at(sb, bv, P) : nullptr;
+    const float* dP = HASD ? own_at(sd, invD, P) : nullptr;
+    if (lact && lane != 31) {
+#pragma unroll
+      for (int r = 0; r < RMAX; r++)
+        if (r < nrow) epi(uP, bP, dP, P, r, t + 1, 0, 3, carry[r], false);
+    }
+    if (tail) {
+      const float2 v = carry_b[((tz * (nwy + 1) + tcb) * RMAX + tr) * 3 + tc];
+      const float2 y[3] = {v, v, v};
+      epi(uP, bP, dP, P, tr, 32 * tcb, tc, tc + 1, y, false);
     }
   }
 }
@@ -562,6 +949,18 @@ bool ec_plan(tp_ctx* c, int nzg, int ncx, EcPlan* P) {
   return true;
 }
 
+// plan of the packed FP32 kernel: npr thread rows of two z groups each
+static bool pk_plan(tp_ctx* c, int npr, int ncx, EcPlan* P) {
+  EcPlan p;
+  if (!ec_plan(c, 1, ncx, &p)) return false;
+  if (3L * c->L[0].nnodes >= (1L << 31)) return false;  // 32-bit indices
+  npr = std::max(1, std::min(npr, std::min(256 / p.nyt, (p.ngz + 1) / 2)));
+  p.nzg = 2 * npr;
+  p.pk = 1;
+  *P = p;
+  return true;
+}
+
 // Defaults before any tuning: FP32 (bandwidth-bound) aims at about three
 // CTAs per SM, FP64 (FP64-pipe-bound) at two; x chunks make up the count.
 void ec_default_plans(tp_ctx* c) {
@@ -584,7 +983,29 @@ void ec_default_plans(tp_ctx* c) {
   for (int m = 0; m < 4; m++) c->ec_ds[m] = c->ec_f64[m];
 }
 
-static EcGeom ec_geom(const tp_ctx* c, const EcPlan& p, size_t tsize, bool own, long vstride) {
+// FP32 plans of the sweep, residual and product: the packed kernel's
+// defaults (on) or the one-group kernel's (off); tp_autotune re-tunes them
+void ec_select_packed(tp_ctx* c, bool on) {
+  if (!c->ec_ok) return;
+  int sms = 148;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  for (int m = 0; m < 4; m++) {
+    if (m == FM_APPLY_DOT) continue;
+    EcPlan p;
+    if (on) {
+      if (!pk_plan(c, 1, 1, &p)) continue;
+      const int zctas = (p.ngz + p.nzg - 1) / p.nzg;
+      pk_plan(c, 1, (2 * sms + zctas - 1) / zctas, &p);
+    } else {
+      if (!ec_plan(c, 2, 1, &p)) continue;
+      const int zctas = (p.ngz + p.nzg - 1) / p.nzg;
+      ec_plan(c, 2, (3 * sms + zctas - 1) / zctas, &p);
+    }
+    c->ec_f32[m] = p;
+  }
+}
+
+static EcGeom ec_geom(const tp_ctx* c, const EcPlan& p, size_t tsize, bool own, long vstride, bool pt = false) {
   const Level& L = c->L[0];
   EcGeom g;
   g.nx = L.nx;
@@ -604,20 +1025,23 @@ static EcGeom ec_geom(const tp_ctx* c, const EcPlan& p, size_t tsize, bool own, 
   g.slab_bytes = (int)roundup16((rows + 2) * row_bytes + 32);
   g.own_bytes = own ? (int)roundup16(rows * row_bytes + 32) : 0;
   g.e_bytes = (int)roundup16((rows + 1) * (long)L.ey * (long)tsize + 32);
+  // b and invD slots: RMAX rows x 2 arrays x 3 components per z group and
+  // column (a packed-kernel thread holds two groups)
+  g.pt_bytes = pt ? (int)(p.nyt * p.nzg * kEcRmax * 6 * sizeof(float)) : 0;
   return g;
 }
 
 static size_t ec_smem(const EcGeom& g, const EcPlan& p, size_t tsize) {
   const int nwy = p.nyt / 32;
-  return 3 * (size_t)g.slab_bytes + 4 * (size_t)g.own_bytes + 2 * (size_t)g.e_bytes +
+  return 3 * (size_t)g.slab_bytes + 4 * (size_t)g.own_bytes + 2 * (size_t)g.e_bytes + (size_t)g.pt_bytes +
          tsize * (size_t)(2 * p.nzg * nwy * kEcRmax * 6 + p.nzg * (nwy + 1) * kEcRmax * 3);
 }
 
 template <typename T, typename A, int MODE>
 static int ec_launch_as(tp_ctx* c, const EcPlan& p, const T* E, const T* in, T* out, const T* b, const T* invD,
                         T omega, int nrhs, long vstride) {
-  const bool own = (MODE == EC_JACOBI || MODE == EC_RESID) && p.own;
-  const EcGeom g = ec_geom(c, p, sizeof(T), own, vstride);
+  const bool hasb = MODE == EC_JACOBI || MODE == EC_RESID;
+  const EcGeom g = ec_geom(c, p, sizeof(T), hasb && p.own == 1, vstride, hasb && p.own == 2 && sizeof(T) == 4);
   const size_t smem = ec_smem(g, p, sizeof(T));
   // the register-capped form exists for FP32 vectors (three CTAs per SM)
   const bool capped = std::is_same<T, float>::value && p.occ3;
@@ -640,6 +1064,31 @@ static int ec_launch_as(tp_ctx* c, const EcPlan& p, const T* E, const T* in, T* 
   return (int)(grid.x * grid.y);  // partials per right-hand side
 }
 
+// the packed FP32 kernel: p.nzg groups per CTA, two per thread row
+template <int MODE>
+static int pk_launch(tp_ctx* c, const EcPlan& p, const float* E, const float* in, float* out, const float* b,
+                     const float* invD, float omega, int nrhs, long vstride) {
+  const bool hasb = MODE == EC_JACOBI || MODE == EC_RESID;
+  const EcGeom g = ec_geom(c, p, sizeof(float), hasb && p.own == 1, vstride, hasb && p.own == 2);
+  const size_t smem = ec_smem(g, p, sizeof(float));
+  // occ3 selects the form whose registers are capped for two 256-thread CTAs per SM
+  auto kern = p.occ3 ? fine_pk_kernel<MODE, kEcRmax, 2> : fine_pk_kernel<MODE, kEcRmax, 1>;
+  static size_t set_for[2] = {0, 0};
+  const int form = p.occ3 ? 1 : 0;
+  if (smem > 48 * 1024 && smem > set_for[form]) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+      cudaGetLastError();
+      c->err = "fine_pk: shared memory request of " + std::to_string(smem) + " bytes refused";
+      return 0;
+    }
+    set_for[form] = smem;
+  }
+  const dim3 grid((unsigned)((p.ngz + p.nzg - 1) / p.nzg), (unsigned)p.ncx, (unsigned)nrhs);
+  kern<<<grid, dim3(p.nyt, p.nzg / 2), smem, c->s>>>(g, E, in, out, b, invD, omega);
+  TP_CHECK_LAUNCH(c, "fine_pk");
+  return (int)(grid.x * grid.y);
+}
+
 // double vectors are worked on in double-single when the context asks for it
 template <typename T, int MODE>
 static int ec_launch(tp_ctx* c, const EcPlan& p, const T* E, const T* in, T* out, const T* b, const T* invD,
@@ -656,6 +1105,27 @@ const EcPlan& ec_plan_for(const tp_ctx* c, int mode) {
 
 static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
+// one launch of plan p for mode (the packed FP32 kernel where the plan says so)
+template <typename T>
+static int ec_run(tp_ctx* c, int mode, const EcPlan& p, const T* E, const T* in, T* out, const T* b,
+                  const T* invD, T omega, int nr, long vs) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (p.pk && mode != EC_APPLY_DOT) {
+      switch (mode) {
+        case EC_APPLY: return pk_launch<EC_APPLY>(c, p, E, in, out, b, invD, omega, nr, vs);
+        case EC_JACOBI: return pk_launch<EC_JACOBI>(c, p, E, in, out, b, invD, omega, nr, vs);
+        default: return pk_launch<EC_RESID>(c, p, E, in, out, b, invD, omega, nr, vs);
+      }
+    }
+  }
+  switch (mode) {
+    case EC_APPLY: return ec_launch<T, EC_APPLY>(c, p, E, in, out, b, invD, omega, nr, vs);
+    case EC_APPLY_DOT: return ec_launch<T, EC_APPLY_DOT>(c, p, E, in, out, b, invD, omega, nr, vs);
+    case EC_JACOBI: return ec_launch<T, EC_JACOBI>(c, p, E, in, out, b, invD, omega, nr, vs);
+    default: return ec_launch<T, EC_RESID>(c, p, E, in, out, b, invD, omega, nr, vs);
+  }
+}
+
 // nr right-hand sides, consecutive columns of ndof(0). Only the first column
 // needs a 16-byte aligned base: the staging of a later column may start up to
 // 15 bytes early, inside the column before it.
@@ -664,12 +1134,7 @@ int fine_ec(tp_ctx* c, int mode, const T* E, const T* in, T* out, const T* b, co
   const EcPlan& p = ec_plan_for<T>(c, mode);
   const long vs = c->L[0].ndof;
   if (!p.ok || !aligned16(in) || (b && !aligned16(b)) || (invD && !aligned16(invD))) return -1;
-  switch (mode) {
-    case EC_APPLY: return ec_launch<T, EC_APPLY>(c, p, E, in, out, b, invD, omega, nr, vs);
-    case EC_APPLY_DOT: return ec_launch<T, EC_APPLY_DOT>(c, p, E, in, out, b, invD, omega, nr, vs);
-    case EC_JACOBI: return ec_launch<T, EC_JACOBI>(c, p, E, in, out, b, invD, omega, nr, vs);
-    default: return ec_launch<T, EC_RESID>(c, p, E, in, out, b, invD, omega, nr, vs);
-  }
+  return ec_run<T>(c, mode, p, E, in, out, b, invD, omega, nr, vs);
 }
 
 template int fine_ec<double>(tp_ctx*, int, const double*, const double*, double*, const double*, const double*,
@@ -690,19 +1155,13 @@ float ec_time(tp_ctx* c, int mode, const tp::EcPlan& p, const T* E, const T* in,
   using namespace tp;
   int smax = 0;
   cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
-  const bool own = (mode == FM_JACOBI || mode == FM_RESID) && p.own;
-  if (ec_smem(ec_geom(c, p, sizeof(T), own, 0), p, sizeof(T)) > (size_t)smax) return 1e30f;  // does not fit
+  const bool hasb = mode == FM_JACOBI || mode == FM_RESID;
+  if (ec_smem(ec_geom(c, p, sizeof(T), hasb && p.own == 1, 0, hasb && p.own == 2), p, sizeof(T)) > (size_t)smax)
+    return 1e30f;  // does not fit
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  auto run = [&]() {
-    switch (mode) {
-      case FM_APPLY: return ec_launch<T, FM_APPLY>(c, p, E, in, out, b, d, T(0.6), 1, 0);
-      case FM_APPLY_DOT: return ec_launch<T, FM_APPLY_DOT>(c, p, E, in, out, b, d, T(0.6), 1, 0);
-      case FM_JACOBI: return ec_launch<T, FM_JACOBI>(c, p, E, in, out, b, d, T(0.6), 1, 0);
-      default: return ec_launch<T, FM_RESID>(c, p, E, in, out, b, d, T(0.6), 1, 0);
-    }
-  };
+  auto run = [&]() { return ec_run<T>(c, mode, p, E, in, out, b, d, T(0.6), 1, 0); };
   run();
   cudaEventRecord(e0, c->s);
   const int reps = 3;
@@ -720,31 +1179,37 @@ template <typename T>
 void ec_tune(tp_ctx* c, tp::EcPlan* plans, const T* E, const T* in, T* out, const T* b, const T* d, int sms,
              double* ms_out) {
   using namespace tp;
+  constexpr bool f32 = std::is_same<T, float>::value;
   for (int mode = 0; mode < 4; mode++) {
     EcPlan best = plans[mode];
     float tbest = 1e30f;
-    for (int nzg = 1; nzg <= 4; nzg *= 2) {
-      EcPlan p;
-      if (!ec_plan(c, nzg, 1, &p) || p.nzg != nzg) continue;
-      const int zctas = (p.ngz + p.nzg - 1) / p.nzg;
-      int last_ncx = -1;
-      for (int mult = 1; mult <= 6; mult++) {
-        if (!ec_plan(c, nzg, (mult * sms + zctas - 1) / zctas, &p) || p.ncx == last_ncx) continue;
-        last_ncx = p.ncx;
-        const int nown = (mode == FM_JACOBI || mode == FM_RESID) ? 2 : 1;
-        const int nocc = std::is_same<T, float>::value ? 2 : 1;
-        for (int own = 0; own < nown; own++)
-          for (int occ = 0; occ < nocc; occ++) {
-            p.own = own;
-            p.occ3 = occ;
-            const float ms = ec_time<T>(c, mode, p, E, in, out, b, d);
-            if (ms < tbest) {
-              tbest = ms;
-              best = p;
+    // family 0: one z group per thread row; family 1 (FP32 sweeps, residuals
+    // and products): the packed kernel, two z groups per thread row
+    const int nfam = (f32 && mode != FM_APPLY_DOT) ? 2 : 1;
+    for (int fam = 0; fam < nfam; fam++)
+      for (int nz1 = 1; nz1 <= 4; nz1 *= 2) {
+        EcPlan p;
+        auto plan = [&](int ncx) { return fam ? pk_plan(c, nz1, ncx, &p) : ec_plan(c, nz1, ncx, &p); };
+        if (!plan(1) || p.nzg != (fam ? 2 * nz1 : nz1)) continue;
+        const int zctas = (p.ngz + p.nzg - 1) / p.nzg;
+        int last_ncx = -1;
+        for (int mult = 1; mult <= 6; mult++) {
+          if (!plan((mult * sms + zctas - 1) / zctas) || p.ncx == last_ncx) continue;
+          last_ncx = p.ncx;
+          const int nown = (mode == FM_JACOBI || mode == FM_RESID) ? (f32 ? 3 : 2) : 1;
+          const int nocc = f32 ? 2 : 1;
+          for (int own = 0; own < nown; own++)
+            for (int occ = 0; occ < nocc; occ++) {
+              p.own = own;
+              p.occ3 = occ;
+              const float ms = ec_time<T>(c, mode, p, E, in, out, b, d);
+              if (ms < tbest) {
+                tbest = ms;
+                best = p;
+              }
             }
-          }
+        }
       }
-    }
     plans[mode] = best;
     if (ms_out) ms_out[mode] = tbest;
   }
@@ -772,4 +1237,51 @@ extern "C" tp_status tp_autotune(tp_ctx* c, double* ms_out) {
     return TP_ERR_CUDA;
   }
   return c->err.empty() ? TP_OK : TP_ERR_CUDA;
+}
+
+// ---------------------------------------------------------------------------
+// Launch plans of the element-centric level-0 kernel, read and set by the
+// caller (to keep a tuning between runs, or to choose one by hand).
+namespace {
+tp::EcPlan* plan_slot(tp_ctx* c, int vec, int mode) {
+  if (vec == 0) return &c->ec_f32[mode];
+  return c->fine_ds ? &c->ec_ds[mode] : &c->ec_f64[mode];
+}
+}  // namespace
+
+extern "C" tp_status tp_get_fine_plan(tp_ctx* c, int vec, int mode, int* plan) {
+  using namespace tp;
+  if (!c || vec < 0 || vec > 1 || mode < 0 || mode > 3 || !plan) return TP_ERR_ARG;
+  const EcPlan& p = *plan_slot(c, vec, mode);
+  if (!p.ok) return TP_ERR_STATE;
+  plan[0] = p.nzg;
+  plan[1] = p.ncx;
+  plan[2] = p.own;
+  plan[3] = p.occ3;
+  plan[4] = p.pk;
+  plan[5] = p.nyt;
+  return TP_OK;
+}
+
+extern "C" tp_status tp_set_fine_plan(tp_ctx* c, int vec, int mode, const int* plan) {
+  using namespace tp;
+  if (!c || vec < 0 || vec > 1 || mode < 0 || mode > 3 || !plan || !c->ec_ok) return TP_ERR_ARG;
+  const int groups = plan[0], ncx = plan[1], own = plan[2], occ = plan[3], pk = plan[4];
+  const bool hasb = mode == FM_JACOBI || mode == FM_RESID;
+  if (groups < 1 || ncx < 1 || own < 0 || own > (vec == 0 ? 2 : 1) || (own && !hasb) || occ < 0 || occ > 1 ||
+      pk < 0 || pk > 1 || (pk && (vec != 0 || mode == FM_APPLY_DOT || groups % 2)) || (occ && vec != 0))
+    return TP_ERR_ARG;
+  EcPlan p;
+  const bool ok = pk ? pk_plan(c, groups / 2, ncx, &p) : ec_plan(c, groups, ncx, &p);
+  if (!ok || p.nzg != groups || p.ncx != ncx) return TP_ERR_ARG;
+  p.own = own;
+  p.occ3 = occ;
+  const size_t tsize = vec == 0 ? sizeof(float) : sizeof(double);
+  int smax = 0;
+  cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+  if (ec_smem(ec_geom(c, p, tsize, hasb && own == 1, 0, hasb && own == 2), p, tsize) > (size_t)smax)
+    return TP_ERR_ARG;
+  *plan_slot(c, vec, mode) = p;
+  graph_free(c);  // a captured CG loop keeps the launch shapes it was recorded with
+  return TP_OK;
 }

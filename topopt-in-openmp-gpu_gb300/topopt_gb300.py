@@ -105,6 +105,8 @@ def load():
     L.tp_multiload.argtypes = [I, I, I, I, I, ctypes.c_ulonglong, P]
     L.tp_set_graph_solve.argtypes = [V, I]
     L.tp_set_device_loop.argtypes = [V, I]
+    L.tp_get_fine_plan.argtypes = [V, I, I, P]
+    L.tp_set_fine_plan.argtypes = [V, I, I, P]
     L.tp_fault_alloc.restype = ctypes.c_long
     L.tp_fault_alloc.argtypes = [ctypes.c_long]
     L.tp_coarse_factor_csr.argtypes = [V, ctypes.c_long, P, P, P]
@@ -295,6 +297,18 @@ class TopOpt:
         out = torch.empty_like(rhs)
         self._check(self.L.tp_coarse_solve_factored(self.ctx, _ptr(rhs), _ptr(out)))
         return out
+
+    def fine_plan(self, vec, mode):
+        """Level-0 launch plan (groups, x chunks, b/invD staging, register cap,
+        packed, threads in y) for vec 0 = FP32 / 1 = double vectors, mode 0-3."""
+        plan = np.zeros(6, np.int32)
+        self._check(self.L.tp_get_fine_plan(self.ctx, vec, mode, plan.ctypes.data))
+        return [int(v) for v in plan]
+
+    def set_fine_plan(self, vec, mode, plan):
+        """Sets a level-0 launch plan; returns the status (1 if the plan does not apply)."""
+        a = np.ascontiguousarray(plan[:5], np.int32)
+        return self.L.tp_set_fine_plan(self.ctx, vec, mode, a.ctypes.data)
 
     def autotune(self):
         """Tunes the level-0 launch shapes; returns the best ms per (f32, f64) x mode."""

@@ -203,28 +203,43 @@ struct StageAlloc {
 };
 using HVec = std::vector<double, StageAlloc<double>>;
 
-// padded host vector of level l -> canonical double (host); the conversions
-// run on all host threads (one x-z line of nodes per item)
+// padded host vector of level l -> canonical double (host). A y line of
+// nodes is contiguous in both layouts (3 (ey + 1) values), so each (x, z)
+// line is one copy; the lines are shared out over all host threads.
+template <typename T>
+static inline void line_copy(double* dst, const T* src, long n) {
+  if constexpr (sizeof(T) == sizeof(double)) {
+    std::memcpy(dst, src, sizeof(double) * n);
+  } else {
+    for (long q = 0; q < n; q++) dst[q] = (double)src[q];
+  }
+}
+template <typename T>
+static inline void line_copy_out(T* dst, const double* src, long n) {
+  if constexpr (sizeof(T) == sizeof(double)) {
+    std::memcpy(dst, src, sizeof(double) * n);
+  } else {
+    for (long q = 0; q < n; q++) dst[q] = (T)src[q];
+  }
+}
 template <typename T>
 HVec to_canon(const Dims& d, const T* v) {
   HVec out(3L * (d.ex + 1) * (d.ey + 1) * (d.ez + 1));
+  const long nl = 3L * (d.ey + 1);
 #pragma omp parallel for collapse(2) schedule(static)
   for (int i = 0; i <= d.ex; i++)
-    for (int k = 0; k <= d.ez; k++)
-      for (int j = 0; j <= d.ey; j++)
-        for (int c = 0; c < 3; c++) out[3 * cnode(d, i, k, j) + c] = (double)v[3 * pnode(d, i, k, j) + c];
+    for (int k = 0; k <= d.ez; k++) line_copy(&out[3 * cnode(d, i, k, 0)], v + 3 * pnode(d, i, k, 0), nl);
   return out;
 }
 template <typename T>
 void from_canon(const Dims& d, const HVec& h, T* v) {
+  const long nl = 3L * (d.ey + 1);
 #pragma omp parallel for collapse(2) schedule(static)
   for (int i = 0; i <= d.ex; i++)
-    for (int k = 0; k <= d.ez; k++)
-      for (int j = 0; j <= d.ey; j++)
-        for (int c = 0; c < 3; c++) v[3 * pnode(d, i, k, j) + c] = (T)h[3 * cnode(d, i, k, j) + c];
+    for (int k = 0; k <= d.ez; k++) line_copy_out(v + 3 * pnode(d, i, k, 0), &h[3 * cnode(d, i, k, 0)], nl);
 }
 
-// padded element array (fine level) <-> canonical
+// padded element array (fine level) <-> canonical, one y line per copy
 HVec el_to_canon(const gridContext& gc, const DTYPE* x) {
   const int ex = gc.nelx, ey = gc.nely, ez = gc.nelz;
   const long wy = gc.wrapy - 1, wz = gc.wrapz - 1;
@@ -232,8 +247,7 @@ HVec el_to_canon(const gridContext& gc, const DTYPE* x) {
 #pragma omp parallel for collapse(2) schedule(static)
   for (int i = 0; i < ex; i++)
     for (int k = 0; k < ez; k++)
-      for (int j = 0; j < ey; j++)
-        out[((size_t)i * ez + k) * ey + j] = (double)x[(i + 1) * wy * wz + (k + 1) * wy + (j + 1)];
+      line_copy(&out[((size_t)i * ez + k) * ey], x + (i + 1) * wy * wz + (k + 1) * wy + 1, ey);
   return out;
 }
 void el_from_canon(const gridContext& gc, const HVec& h, DTYPE* x) {
@@ -242,8 +256,7 @@ void el_from_canon(const gridContext& gc, const HVec& h, DTYPE* x) {
 #pragma omp parallel for collapse(2) schedule(static)
   for (int i = 0; i < ex; i++)
     for (int k = 0; k < ez; k++)
-      for (int j = 0; j < ey; j++)
-        x[(i + 1) * wy * wz + (k + 1) * wy + (j + 1)] = (DTYPE)h[((size_t)i * ez + k) * ey + j];
+      line_copy_out(x + (i + 1) * wy * wz + (k + 1) * wy + 1, &h[((size_t)i * ez + k) * ey], ey);
 }
 
 // an element array of n entries as a staged double copy

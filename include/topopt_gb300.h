@@ -197,10 +197,9 @@ tp_status tp_set_coarse_solve_variant(tp_ctx* c, int variant);
 /* Arithmetic of the coarsest-level band Cholesky (its single-launch factor
  * and the diagonal-block inverses; no counterpart in the reference): 0 =
  * FP64; 1 = double-single (pairs of FP32 numbers, about 48 significant bits)
- * on the same FP64 storage; with 1 the row sums of the single-launch
- * triangular sweeps are double-single too (the block-step variant's sweeps
- * stay FP64). The default is 1 for TP_MIXED, whose V-cycle is FP32, and 0
- * for TP_FP64. The factor is redone at the next solve. */
+ * on the same FP64 storage. The triangular sweeps are FP64 either way. The
+ * default is 1 for TP_MIXED, whose V-cycle is FP32, and 0 for TP_FP64. The
+ * factor is redone at the next solve. */
 tp_status tp_set_coarse_arith(tp_ctx* c, int arith);
 /* Failure detection of the single-launch coarse factor and solve (host-side
  * fault injection, for tests): each of their waits in global memory gives up

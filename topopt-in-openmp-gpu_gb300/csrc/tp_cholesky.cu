@@ -1459,10 +1459,7 @@ __device__ __forceinline__ bool ps_barrier(unsigned* bar, int* err, unsigned tar
   return s_ok != 0;
 }
 
-// A: the arithmetic of the row sums -- double, or Dsf (pairs of floats, the
-// mixed form's: FP64 on this part issues one warp instruction per ~67
-// cycles per sub-partition, FP32 one per cycle); storage stays FP64 either way
-template <int NR, typename A>
+template <int NR>
 __global__ void __launch_bounds__(kPsWarps * 32) ps_solve_kernel(PsArgs a) {
   extern __shared__ double sm[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1485,9 +1482,9 @@ __global__ void __launch_bounds__(kPsWarps * 32) ps_solve_kernel(PsArgs a) {
     int kind, k;
     ps_phase(a, h, kind, k);
     PsRow r;
-    A acc[NR];
+    double acc[NR];
 #pragma unroll
-    for (int v = 0; v < NR; v++) acc[v] = A(0.f);
+    for (int v = 0; v < NR; v++) acc[v] = 0.0;
     if (ps_row(a, kind, k, i, p, r)) {
       // U positions per lane per round: all their L2 loads are issued before
       // the first multiply-add, so a round costs one L2 latency; the sum
@@ -1507,12 +1504,12 @@ __global__ void __launch_bounds__(kPsWarps * 32) ps_solve_kernel(PsArgs a) {
 #pragma unroll
         for (int u = 0; u < U; u++)
 #pragma unroll
-          for (int v = 0; v < NR; v++) acc[v] += ds_in<A>(mv[u]) * ds_in<A>(vv[u][v]);
+          for (int v = 0; v < NR; v++) acc[v] += mv[u] * vv[u][v];
       }
     }
 #pragma unroll
     for (int v = 0; v < NR; v++) {
-      const double sv = wsum(ds_out(acc[v]));
+      const double sv = wsum(acc[v]);
       if (lane == 0) part[w * NR + v] = sv;
     }
     __syncthreads();
@@ -1575,10 +1572,8 @@ static void ps_plan(tp_ctx* c) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, kPsWarps * 32, smem) != cudaSuccess) return false;
     return per >= 1;
   };
-  const bool ok = fits((const void*)ps_solve_kernel<1, double>) && fits((const void*)ps_solve_kernel<2, double>) &&
-                  fits((const void*)ps_solve_kernel<4, double>) && fits((const void*)ps_solve_kernel<8, double>) &&
-                  fits((const void*)ps_solve_kernel<1, Dsf>) && fits((const void*)ps_solve_kernel<2, Dsf>) &&
-                  fits((const void*)ps_solve_kernel<4, Dsf>) && fits((const void*)ps_solve_kernel<8, Dsf>);
+  const bool ok = fits((const void*)ps_solve_kernel<1>) && fits((const void*)ps_solve_kernel<2>) &&
+                  fits((const void*)ps_solve_kernel<4>) && fits((const void*)ps_solve_kernel<8>);
   cudaGetLastError();
   if (!ok) return;
   C.ps_R = R;
@@ -1603,10 +1598,7 @@ static void ps_launch(tp_ctx* c, const double* rhs, double* sol, double* y, doub
   cfg.stream = c->s;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  if (C.ds)
-    cudaLaunchKernelEx(&cfg, ps_solve_kernel<NR, Dsf>, a);
-  else
-    cudaLaunchKernelEx(&cfg, ps_solve_kernel<NR, double>, a);
+  cudaLaunchKernelEx(&cfg, ps_solve_kernel<NR>, a);
 }
 
 tp_status coarse_status(tp_ctx* c) {

@@ -478,6 +478,21 @@ int oc_bisect(tp_ctx* c, long ne, double* x, double* xnew, const double* dc, con
   oc_init_kernel<<<1, 1, 0, c->s>>>(c->d_scal);
   oc_set_g_kernel<<<1, 1, 0, c->s>>>(c->d_scal, g);
   const double *B = nullptr, *lo = nullptr, *hi = nullptr;
+  if (ne > c->ocb_n) {
+    // a longer array than the context's design (the reference-signature
+    // update_solution passes the padded element count): the scratch grows
+    // once; without it every step evaluates the reference's expression per
+    // element (an FP64 division and square root each)
+    double* nb = nullptr;
+    if (dev_malloc(&nb, sizeof(double) * 3 * (size_t)ne) == cudaSuccess) {
+      cudaStreamSynchronize(c->s);
+      dev_free(c->d_ocb);
+      c->mem_bytes += 24L * (ne - c->ocb_n);
+      c->d_ocb = nb;
+      c->ocb_n = ne;
+      oc_graph_free(c);  // the captured bisection holds the old scratch
+    }
+  }
   if (c->d_ocb && ne <= c->ocb_n) {
     double* b = c->d_ocb;
     oc_prep_kernel<<<grid_for(ne, 256), 256, 0, c->s>>>(ne, x, dc, dv, b, b + ne, b + 2 * ne);

@@ -175,3 +175,34 @@ def test_mixed_precision_fine_operator(cuda):
     y = ctx.apply(0, dev(cuda, g["u_0"]).float()).double().cpu().numpy()
     assert relerr(y, g["apply_0"]) < 1e-5
     ctx.close()
+
+
+def _final_design_samples(ctx, g):
+    xp = ctx.download("xphys")
+    return xp[g["xphys_idx"]], xp.sum(), np.linalg.norm(xp)
+
+
+def test_design_history_headline_grid(cuda):
+    """The headline grid, 256x128x128 (-l 4, 12.8M DOFs), against the
+    reference's own 20-iteration FP64 history (its C, recorded by
+    tests/golden/make_golden.py --config4; the final design is kept as 256
+    seeded samples, its sum and its 2-norm): the FP64 form within 1e-8 with
+    the same CG counts, the mixed form within 1e-6."""
+    g = golden("history_256x128x128_l4.npz")
+    ctx = tp.TopOpt(256, 128, 128, 4)
+    hist = ctx.run(20)
+    assert len(hist) == int(g["loops"])
+    c = np.array([h.c for h in hist])
+    assert np.max(np.abs(c - g["c"]) / g["c"]) < HIST_TOL
+    assert [h.cgiters for h in hist] == list(g["cgiters"])
+    assert np.max(np.abs(np.array([h.vol for h in hist]) - g["vol"])) < 1e-10
+    samples, total, norm = _final_design_samples(ctx, g)
+    assert np.max(np.abs(samples - g["xphys_val"])) < 1e-6
+    assert abs(total - g["xphys_sum"]) / g["xphys_sum"] < 1e-9
+    assert abs(norm - g["xphys_norm"]) / g["xphys_norm"] < 1e-7
+    ctx.close()
+    ctx = tp.TopOpt(256, 128, 128, 4, precision=tp.TP_MIXED)
+    hist = ctx.run(20)
+    c = np.array([h.c for h in hist])
+    assert np.max(np.abs(c - g["c"]) / g["c"]) < MIXED_TOL
+    ctx.close()

@@ -213,13 +213,16 @@ tp_status tp_fault_coarse_barrier(tp_ctx* c, long spin, int missing);
  * one set by the caller -- to keep a tuning between runs, or to pick one by
  * hand. vec = 0 FP32 vectors (the mixed form's V-cycle), 1 double vectors (in
  * the arithmetic tp_set_fine_arith selected); mode = 0 product, 1 product
- * with the dot product, 2 damped-Jacobi sweep, 3 residual. plan[0..5] =
+ * with the dot product, 2 damped-Jacobi sweep, 3 residual. plan[0..6] =
  * {z groups of node rows per CTA, x chunks, staging of b and invD (0 read
  * from global memory, 1 staged per CTA in shared memory, 2 copied ahead by
  * each thread, FP32 only), register cap (FP32: 1 = capped for more CTAs per
  * SM), packed (FP32 modes 0, 2, 3: two z groups per thread in f32x2
- * arithmetic; groups even), threads along y (read only)}. tp_set_fine_plan
- * returns TP_ERR_ARG for a plan the grid or the shared memory does not allow. */
+ * arithmetic; groups even), moduli staged in shared memory one layer ahead
+ * (1; 0 = loaded into registers per layer, FP32 one-group kernel only),
+ * threads along y (read only)} -- tp_get_fine_plan fills plan[0..6],
+ * tp_set_fine_plan reads plan[0..5] and returns TP_ERR_ARG for a plan the
+ * grid or the shared memory does not allow. */
 tp_status tp_get_fine_plan(tp_ctx* c, int vec, int mode, int* plan);
 tp_status tp_set_fine_plan(tp_ctx* c, int vec, int mode, const int* plan);
 /* Failure detection of the set-up (host-side fault injection, for tests; no

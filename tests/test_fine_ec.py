@@ -206,7 +206,8 @@ def test_packed_fp32_kernel(cuda, shape):
 def test_every_fp32_launch_plan(cuda, shape):
     """Every FP32 launch plan the grid allows (one or two z groups per thread,
     b and invD from global memory, staged per CTA or copied ahead per thread,
-    both register caps, several x chunkings), set through tp_set_fine_plan,
+    both register caps, the moduli staged or in registers, several x
+    chunkings), set through tp_set_fine_plan,
     gives the node-centric stencil's product and V-cycle to FP32 accuracy."""
     torch = cuda
     g = tp.TopOpt(*shape, 2, precision=tp.TP_MIXED)
@@ -223,19 +224,20 @@ def test_every_fp32_launch_plan(cuda, shape):
         for groups in ((1, 2, 4) if pk == 0 else (2, 4)):
             for ncx in (1, 3):
                 for own in (0, 1, 2):
-                    for occ in (0, 1):
-                        plan = [groups, ncx, own, occ, pk]
+                    for occ, es in ((0, 1), (1, 1), (0, 0), (1, 0)):
+                        plan = [groups, ncx, own, occ, pk, es]
                         if g.set_fine_plan(0, 2, plan) != 0:
                             continue
                         assert g.set_fine_plan(0, 3, plan) == 0
-                        assert g.set_fine_plan(0, 0, [groups, ncx, 0, occ, pk]) == 0
-                        assert g.fine_plan(0, 2)[:5] == plan
+                        assert g.set_fine_plan(0, 0, [groups, ncx, 0, occ, pk, es]) == 0
+                        assert g.fine_plan(0, 2)[:6] == plan
                         tried += 1
                         y = g.apply(0, uf).double().cpu().numpy()
                         z = g.vcycle(r).cpu().numpy()
                         assert relerr(y, y_ref) < 1e-5, plan
                         assert relerr(z, z_ref) < 1e-4, plan
     assert tried >= 8
-    assert g.set_fine_plan(0, 1, [2, 1, 0, 0, 1]) == 1  # no packed product with a dot product
-    assert g.set_fine_plan(1, 2, [1, 1, 2, 0, 0]) == 1  # per-thread copies are FP32 only
+    assert g.set_fine_plan(0, 1, [2, 1, 0, 0, 1, 1]) == 1  # no packed product with a dot product
+    assert g.set_fine_plan(1, 2, [1, 1, 2, 0, 0, 1]) == 1  # per-thread copies are FP32 only
+    assert g.set_fine_plan(0, 2, [2, 1, 0, 0, 1, 0]) == 1  # the packed kernel stages its moduli
     g.close()

@@ -119,6 +119,8 @@ struct EcPlan {
                 //   kernel) each thread copies its own entries ahead into shared memory
   int occ3 = 0;  // FP32: the form with registers capped for more CTAs per SM
   int pk = 0;    // FP32: the packed kernel (two z groups per thread, f32x2 arithmetic)
+  int estage = 1;  // the moduli E staged in shared memory one layer ahead (FP32 one-group
+                   //   kernel: 0 loads them into registers when a layer starts)
 };
 struct EcGeom {
   int nx, ny, nz, ex, ey, ez, lim;

@@ -178,7 +178,7 @@ constexpr int EC_APPLY = FM_APPLY, EC_APPLY_DOT = FM_APPLY_DOT, EC_JACOBI = FM_J
 // MINB: CTAs per SM the register allocation is sized for (1: up to 255
 // registers, the double-vector forms; 2: at most 128, the FP32 default;
 // 3: at most 80, with a few spills, for three 256-thread CTAs per SM)
-template <typename T, typename A, int MODE, int RMAX, int MINB>
+template <typename T, typename A, int MODE, int RMAX, int MINB, bool ES>
 __global__ void __launch_bounds__(256, MINB) fine_ec_kernel(EcGeom g, const T* __restrict__ E, const T* __restrict__ in,
                                                       T* __restrict__ out, const T* __restrict__ bv,
                                                       const T* __restrict__ invD, T omega,
@@ -245,7 +245,11 @@ __global__ void __launch_bounds__(256, MINB) fine_ec_kernel(EcGeom g, const T* _
     if (HASD && stage_own) ec_stage<T>(sd + (p & 1) * g.own_bytes, own_src(invD, p), own_n, tid, nthr);
   };
   auto e_src = [&](int L) { return E + ((long)L * ez + ekmin) * ey; };
-  auto issue_e = [&](int L) { ec_stage<T>(se + (L & 1) * g.e_bytes, e_src(L), e_n, tid, nthr); };
+  // ES: the moduli staged in shared memory one layer ahead; otherwise each
+  // thread loads its own into registers when the layer starts
+  auto issue_e = [&](int L) {
+    if (ES) ec_stage<T>(se + (L & 1) * g.e_bytes, e_src(L), e_n, tid, nthr);
+  };
   // views: value of node row kr, column j, component c at [(kr - base row) * row3 + 3 j + c]
   auto slab_at = [&](int p) { return ec_view<T>(sl + (p % NST) * g.slab_bytes, slab_src(p)); };
 
@@ -325,7 +329,15 @@ __global__ void __launch_bounds__(256, MINB) fine_ec_kernel(EcGeom g, const T* _
     cp_async_wait<2>();  // this layer's slot copies and the next stages may still be in flight
     __syncthreads();
     // E of element row ek of layer L at EL[(ek - ekmin) * ey + t]
-    const T* EL = ec_view<T>(se + (L & 1) * g.e_bytes, e_src(L)) + t;
+    const T* EL = ES ? ec_view<T>(se + (L & 1) * g.e_bytes, e_src(L)) + t : e_src(L) + t;
+    A Ev[RMAX + 1];
+    if (!ES) {
+#pragma unroll
+      for (int q = 0; q <= RMAX; q++) {
+        const int ek = k0 - 1 + q;
+        Ev[q] = (lact && q <= nrow && ek >= 0 && ek < ez) ? Cv::in(EL[(long)(ek - ekmin) * ey]) : A(0);
+      }
+    }
     const T* u0 = slab_at(L);
     const T* u1 = slab_at(L + 1);
     const T* bL = HASB ? own_at(sb, bv, L) : nullptr;
@@ -363,7 +375,7 @@ __global__ void __launch_bounds__(256, MINB) fine_ec_kernel(EcGeom g, const T* _
         const int ek = k0 - 1 + q;
         xrow(ek + 1, Xn);
         if (ek >= 0 && ek < ez) {
-          const A Ee = lact ? Cv::in(EL[(long)(ek - ekmin) * ey]) : A(0);
+          const A Ee = ES ? (lact ? Cv::in(EL[(long)(ek - ekmin) * ey]) : A(0)) : Ev[q];
           A Z[24];
 #pragma unroll
           for (int a = 0; a < 4; a++)
@@ -978,6 +990,7 @@ void ec_default_plans(tp_ctx* c) {
     const int zctas = (p.ngz + p.nzg - 1) / p.nzg;
     const int want = (prec == 0 ? 3 : 2) * sms;
     ec_plan(c, nzg, (want + zctas - 1) / zctas, &p);
+    p.estage = prec == 0 ? 0 : 1;
     for (int m = 0; m < 4; m++) (prec == 0 ? c->ec_f32 : c->ec_f64)[m] = p;
   }
   for (int m = 0; m < 4; m++) c->ec_ds[m] = c->ec_f64[m];
@@ -1000,6 +1013,7 @@ void ec_select_packed(tp_ctx* c, bool on) {
       if (!ec_plan(c, 2, 1, &p)) continue;
       const int zctas = (p.ngz + p.nzg - 1) / p.nzg;
       ec_plan(c, 2, (3 * sms + zctas - 1) / zctas, &p);
+      p.estage = 0;
     }
     c->ec_f32[m] = p;
   }
@@ -1024,7 +1038,7 @@ static EcGeom ec_geom(const tp_ctx* c, const EcPlan& p, size_t tsize, bool own, 
   const long row_bytes = 3L * L.ny * (long)tsize;
   g.slab_bytes = (int)roundup16((rows + 2) * row_bytes + 32);
   g.own_bytes = own ? (int)roundup16(rows * row_bytes + 32) : 0;
-  g.e_bytes = (int)roundup16((rows + 1) * (long)L.ey * (long)tsize + 32);
+  g.e_bytes = (p.estage || tsize != sizeof(float)) ? (int)roundup16((rows + 1) * (long)L.ey * (long)tsize + 32) : 0;
   // b and invD slots: RMAX rows x 2 arrays x 3 components per z group and
   // column (a packed-kernel thread holds two groups)
   g.pt_bytes = pt ? (int)(p.nyt * p.nzg * kEcRmax * 6 * sizeof(float)) : 0;
@@ -1046,17 +1060,20 @@ static int ec_launch_as(tp_ctx* c, const EcPlan& p, const T* E, const T* in, T* 
   // the register-capped form exists for FP32 vectors (three CTAs per SM)
   const bool capped = std::is_same<T, float>::value && p.occ3;
   constexpr int kMinB = std::is_same<T, float>::value ? 2 : 1;
-  auto kern = fine_ec_kernel<T, A, MODE, kEcRmax, kMinB>;
-  if constexpr (std::is_same<T, float>::value)
-    if (capped) kern = fine_ec_kernel<T, A, MODE, kEcRmax, 3>;
-  static size_t set_for[2] = {0, 0};  // largest size the attribute was raised to, per form
-  if (smem > 48 * 1024 && smem > set_for[capped]) {
+  auto kern = fine_ec_kernel<T, A, MODE, kEcRmax, kMinB, true>;
+  if constexpr (std::is_same<T, float>::value) {
+    if (capped) kern = p.estage ? fine_ec_kernel<T, A, MODE, kEcRmax, 3, true> : fine_ec_kernel<T, A, MODE, kEcRmax, 3, false>;
+    else if (!p.estage) kern = fine_ec_kernel<T, A, MODE, kEcRmax, kMinB, false>;
+  }
+  const int form = (capped ? 2 : 0) + (p.estage ? 1 : 0);
+  static size_t set_for[4] = {0, 0, 0, 0};  // largest size the attribute was raised to, per form
+  if (smem > 48 * 1024 && smem > set_for[form]) {
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
       cudaGetLastError();  // not sticky: the error is reported through c->err
       c->err = "fine_ec: shared memory request of " + std::to_string(smem) + " bytes refused";
       return 0;
     }
-    set_for[capped] = smem;
+    set_for[form] = smem;
   }
   const dim3 grid((unsigned)((p.ngz + p.nzg - 1) / p.nzg), (unsigned)p.ncx, (unsigned)nrhs);
   kern<<<grid, dim3(p.nyt, p.nzg), smem, c->s>>>(g, E, in, out, b, invD, omega, c->d_red);
@@ -1198,16 +1215,19 @@ void ec_tune(tp_ctx* c, tp::EcPlan* plans, const T* E, const T* in, T* out, cons
           last_ncx = p.ncx;
           const int nown = (mode == FM_JACOBI || mode == FM_RESID) ? (f32 ? 3 : 2) : 1;
           const int nocc = f32 ? 2 : 1;
+          const int nes = (f32 && !fam) ? 2 : 1;  // FP32 one-group kernel: E staged or in registers
           for (int own = 0; own < nown; own++)
-            for (int occ = 0; occ < nocc; occ++) {
-              p.own = own;
-              p.occ3 = occ;
-              const float ms = ec_time<T>(c, mode, p, E, in, out, b, d);
-              if (ms < tbest) {
-                tbest = ms;
-                best = p;
+            for (int occ = 0; occ < nocc; occ++)
+              for (int es = 0; es < nes; es++) {
+                p.own = own;
+                p.occ3 = occ;
+                p.estage = nes == 2 ? es : 1;
+                const float ms = ec_time<T>(c, mode, p, E, in, out, b, d);
+                if (ms < tbest) {
+                  tbest = ms;
+                  best = p;
+                }
               }
-            }
         }
       }
     plans[mode] = best;
@@ -1259,23 +1279,26 @@ extern "C" tp_status tp_get_fine_plan(tp_ctx* c, int vec, int mode, int* plan) {
   plan[2] = p.own;
   plan[3] = p.occ3;
   plan[4] = p.pk;
-  plan[5] = p.nyt;
+  plan[5] = p.estage;
+  plan[6] = p.nyt;
   return TP_OK;
 }
 
 extern "C" tp_status tp_set_fine_plan(tp_ctx* c, int vec, int mode, const int* plan) {
   using namespace tp;
   if (!c || vec < 0 || vec > 1 || mode < 0 || mode > 3 || !plan || !c->ec_ok) return TP_ERR_ARG;
-  const int groups = plan[0], ncx = plan[1], own = plan[2], occ = plan[3], pk = plan[4];
+  const int groups = plan[0], ncx = plan[1], own = plan[2], occ = plan[3], pk = plan[4], es = plan[5];
   const bool hasb = mode == FM_JACOBI || mode == FM_RESID;
   if (groups < 1 || ncx < 1 || own < 0 || own > (vec == 0 ? 2 : 1) || (own && !hasb) || occ < 0 || occ > 1 ||
-      pk < 0 || pk > 1 || (pk && (vec != 0 || mode == FM_APPLY_DOT || groups % 2)) || (occ && vec != 0))
+      pk < 0 || pk > 1 || (pk && (vec != 0 || mode == FM_APPLY_DOT || groups % 2)) || (occ && vec != 0) ||
+      es < 0 || es > 1 || (!es && (vec != 0 || pk)))
     return TP_ERR_ARG;
   EcPlan p;
   const bool ok = pk ? pk_plan(c, groups / 2, ncx, &p) : ec_plan(c, groups, ncx, &p);
   if (!ok || p.nzg != groups || p.ncx != ncx) return TP_ERR_ARG;
   p.own = own;
   p.occ3 = occ;
+  p.estage = es;
   const size_t tsize = vec == 0 ? sizeof(float) : sizeof(double);
   int smax = 0;
   cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);

@@ -300,14 +300,16 @@ class TopOpt:
 
     def fine_plan(self, vec, mode):
         """Level-0 launch plan (groups, x chunks, b/invD staging, register cap,
-        packed, threads in y) for vec 0 = FP32 / 1 = double vectors, mode 0-3."""
-        plan = np.zeros(6, np.int32)
+        packed, E staged, threads in y) for vec 0 = FP32 / 1 = double vectors, mode 0-3."""
+        plan = np.zeros(7, np.int32)
         self._check(self.L.tp_get_fine_plan(self.ctx, vec, mode, plan.ctypes.data))
         return [int(v) for v in plan]
 
     def set_fine_plan(self, vec, mode, plan):
-        """Sets a level-0 launch plan; returns the status (1 if the plan does not apply)."""
-        a = np.ascontiguousarray(plan[:5], np.int32)
+        """Sets a level-0 launch plan (groups, x chunks, staging, register cap, packed,
+        E staged); returns the status (1 if the plan does not apply)."""
+        p = list(plan[:6]) + [1] * (6 - len(plan[:6]))
+        a = np.ascontiguousarray(p, np.int32)
         return self.L.tp_set_fine_plan(self.ctx, vec, mode, a.ctypes.data)
 
     def autotune(self):

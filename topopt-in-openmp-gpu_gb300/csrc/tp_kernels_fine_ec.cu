@@ -178,7 +178,7 @@ constexpr int EC_APPLY = FM_APPLY, EC_APPLY_DOT = FM_APPLY_DOT, EC_JACOBI = FM_J
 // MINB: CTAs per SM the register allocation is sized for (1: up to 255
 // registers, the double-vector forms; 2: at most 128, the FP32 default;
 // 3: at most 80, with a few spills, for three 256-thread CTAs per SM)
-template <typename T, typename A, int MODE, int RMAX, int MINB, bool ES>
+template <typename T, typename A, int MODE, int RMAX, int MINB, bool ES, bool PT>
 __global__ void __launch_bounds__(256, MINB) fine_ec_kernel(EcGeom g, const T* __restrict__ E, const T* __restrict__ in,
                                                       T* __restrict__ out, const T* __restrict__ bv,
                                                       const T* __restrict__ invD, T omega,
@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(256, MINB) fine_ec_kernel(EcGeom g, const T* _
   // layer, copied by the thread itself when the layer starts, slot i of
   // thread tid at [i * nthr + tid], i = (r * 2 + array) * 3 + c
   T* slot = reinterpret_cast<T*>(carry_b + nzg * (nwy + 1) * RMAX * 3);
-  const bool own_pt = HASB && sizeof(T) == 4 && g.pt_bytes > 0;
+  constexpr bool own_pt = PT && HASB && sizeof(T) == 4;  // PT: the per-thread copies (plan staging 2)
 
   auto slab_src = [&](int p) { return in + ((long)p * nz + kmin) * row3; };
   auto own_src = [&](const T* v, int p) { return v + ((long)p * nz + K0) * row3; };
@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(256, MINB) fine_ec_kernel(EcGeom g, const T* _
   const bool lact = gact && t < ey;
   const bool pt_thread = own_pt && lact && lane != 31;
   auto issue_pt = [&](int L) {
-    if constexpr (sizeof(T) == 4) {
+    if constexpr (own_pt) {
       if (!pt_thread || L < i0) return;
 #pragma unroll
       for (int r = 0; r < RMAX; r++) {
@@ -320,13 +320,16 @@ __global__ void __launch_bounds__(256, MINB) fine_ec_kernel(EcGeom g, const T* _
   };
 
   for (int L = Ls; L < Le; ++L) {
-    issue_pt(L);
-    cp_async_commit();
+    if constexpr (own_pt) {
+      issue_pt(L);
+      cp_async_commit();
+    }
     if (L + 2 <= Le) issue_slab(L + 2);
     if (L + 1 <= Le) issue_own(L + 1);
     if (L + 1 < Le) issue_e(L + 1);
     cp_async_commit();
-    cp_async_wait<2>();  // this layer's slot copies and the next stages may still be in flight
+    // the next stages (and this layer's slot copies) may still be in flight
+    cp_async_wait<own_pt ? 2 : 1>();
     __syncthreads();
     // E of element row ek of layer L at EL[(ek - ekmin) * ey + t]
     const T* EL = ES ? ec_view<T>(se + (L & 1) * g.e_bytes, e_src(L)) + t : e_src(L) + t;
@@ -463,7 +466,8 @@ __global__ void __launch_bounds__(256, MINB) fine_ec_kernel(EcGeom g, const T* _
         if (q >= 1) {
           // node row ek = k0 + r is complete: x and y butterflies back
           const int r = q - 1;
-          if (q == 1) cp_async_wait<1>();  // the thread's slot copies of this layer
+          if constexpr (own_pt)
+            if (q == 1) cp_async_wait<1>();  // the thread's slot copies of this layer
           A own0[3], own1[3], nb0[3], nb1[3];
 #pragma unroll
           for (int c = 0; c < 3; c++) {
@@ -1060,13 +1064,28 @@ static int ec_launch_as(tp_ctx* c, const EcPlan& p, const T* E, const T* in, T* 
   // the register-capped form exists for FP32 vectors (three CTAs per SM)
   const bool capped = std::is_same<T, float>::value && p.occ3;
   constexpr int kMinB = std::is_same<T, float>::value ? 2 : 1;
-  auto kern = fine_ec_kernel<T, A, MODE, kEcRmax, kMinB, true>;
+  auto kern = fine_ec_kernel<T, A, MODE, kEcRmax, kMinB, true, false>;
+  const bool pt = std::is_same<T, float>::value && hasb && p.own == 2;
   if constexpr (std::is_same<T, float>::value) {
-    if (capped) kern = p.estage ? fine_ec_kernel<T, A, MODE, kEcRmax, 3, true> : fine_ec_kernel<T, A, MODE, kEcRmax, 3, false>;
-    else if (!p.estage) kern = fine_ec_kernel<T, A, MODE, kEcRmax, kMinB, false>;
+    constexpr bool HB = MODE == EC_JACOBI || MODE == EC_RESID;
+    if (pt) {
+      if constexpr (HB) {
+        if (capped)
+          kern = p.estage ? fine_ec_kernel<T, A, MODE, kEcRmax, 3, true, true>
+                          : fine_ec_kernel<T, A, MODE, kEcRmax, 3, false, true>;
+        else
+          kern = p.estage ? fine_ec_kernel<T, A, MODE, kEcRmax, kMinB, true, true>
+                          : fine_ec_kernel<T, A, MODE, kEcRmax, kMinB, false, true>;
+      }
+    } else if (capped) {
+      kern = p.estage ? fine_ec_kernel<T, A, MODE, kEcRmax, 3, true, false>
+                      : fine_ec_kernel<T, A, MODE, kEcRmax, 3, false, false>;
+    } else if (!p.estage) {
+      kern = fine_ec_kernel<T, A, MODE, kEcRmax, kMinB, false, false>;
+    }
   }
-  const int form = (capped ? 2 : 0) + (p.estage ? 1 : 0);
-  static size_t set_for[4] = {0, 0, 0, 0};  // largest size the attribute was raised to, per form
+  const int form = (pt ? 4 : 0) + (capped ? 2 : 0) + (p.estage ? 1 : 0);
+  static size_t set_for[8] = {};  // largest size the attribute was raised to, per form
   if (smem > 48 * 1024 && smem > set_for[form]) {
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
       cudaGetLastError();  // not sticky: the error is reported through c->err

@@ -306,6 +306,35 @@ template <typename T> void prolong_set(tp_ctx* c, int l, const T* coarse, T* fin
 // vectors
 template <typename T> void vscale(tp_ctx* c, long n, const T* a, const T* b, T* out, T omega, int nr = 1);  // out = omega*a*b
 void dot_partials(tp_ctx* c, long n, const double* a, const double* b, int* nblocks, int nr = 1);
+#ifdef __CUDACC__
+// The 256 values of a block (one per thread) folded in a fixed tree --
+// pairs (i, i + 128), then (i, i + 64), (i, i + 32), then a warp's shuffles
+// -- so that the result is the same at every run; the value is thread 0's.
+// On this part an FP64 add holds its unit for ~67 cycles, so the serial fold
+// of 256 values by one thread took ~8 us.
+__device__ __forceinline__ double fold256(double v, bool is_max, double* sh) {
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int w = 128; w >= 32; w >>= 1) {
+    if (threadIdx.x < w) {
+      const double a = sh[threadIdx.x], b = sh[threadIdx.x + w];
+      sh[threadIdx.x] = is_max ? fmax(a, b) : a + b;
+    }
+    __syncthreads();
+  }
+  double r = 0.0;
+  if (threadIdx.x < 32) {
+    r = sh[threadIdx.x];
+    for (int o = 16; o > 0; o >>= 1) {
+      const double b = __shfl_down_sync(0xffffffffu, r, o);
+      r = is_max ? fmax(r, b) : r + b;
+    }
+  }
+  return r;
+}
+
+// (sh: 256 doubles of shared memory; every thread of the block calls it)
+#endif
 void finish_sum(tp_ctx* c, int nblocks, int slot, int op, int nr = 1);  // column r: partials -> d_scal[r*S_COUNT + slot]
 void cast_d2f(tp_ctx* c, long n, const double* a, float* b);
 void cast_f2d(tp_ctx* c, long n, const float* a, double* b);

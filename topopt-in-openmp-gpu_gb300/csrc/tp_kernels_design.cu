@@ -404,11 +404,8 @@ __global__ void oc_finish_kernel(const double* __restrict__ partials, int nb, do
   const int b0 = threadIdx.x * per;
   double s = 0.0;
   for (int i = b0; i < b0 + per && i < nb; i++) s += partials[i];
-  sh[threadIdx.x] = s;
-  __syncthreads();
+  const double t = fold256(s, false, sh);
   if (threadIdx.x == 0) {
-    double t = sh[0];
-    for (int i = 1; i < 256; i++) t += sh[i];
     const double l1 = scal[S_L1], l2 = scal[S_L2];
     const double lmid = 0.5 * (l2 + l1);
     const double gt = t + g;

@@ -75,13 +75,8 @@ __global__ void finish_kernel(const double* __restrict__ partials, int nb, doubl
   const int per = (nb + 255) / 256;
   const int b0 = threadIdx.x * per;
   for (int i = b0; i < b0 + per && i < nb; i++) s = (op == 1) ? fmax(s, partials[i]) : s + partials[i];
-  sh[threadIdx.x] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = sh[0];
-    for (int i = 1; i < 256; i++) t = (op == 1) ? fmax(t, sh[i]) : t + sh[i];
-    out[(long)blockIdx.x * S_COUNT] = t;
-  }
+  const double t = fold256(s, op == 1, sh);
+  if (threadIdx.x == 0) out[(long)blockIdx.x * S_COUNT] = t;
 }
 
 void finish_sum(tp_ctx* c, int nblocks, int slot, int op, int nr) {

@@ -194,3 +194,45 @@ def test_reciprocal_square_root_and_reciprocal():
             assert abs(float(val(r)) - float(exact_rs)) <= 2.0 ** -42 * float(exact_rs)
         q = ds_rcp(d)
         assert abs(val(q) * val(d) - 1) <= Fr(2) ** -42
+
+
+def test_float_to_double_bits_on_the_host(tmp_path):
+    """f32_to_f64_bits (the integer float -> double conversion that ds_to
+    uses instead of FP64 conversions) compiled for the host with nvcc, against
+    the exact conversion, on every exponent class: zeros, subnormals, normals,
+    infinities and NaN."""
+    import os
+    import shutil
+    import subprocess
+
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    csrc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                        "topopt-in-openmp-gpu_gb300", "csrc")
+    src = tmp_path / "cvt.cu"
+    src.write_text(
+        '#include <cstdio>\n#include "tp_dsf.cuh"\n'
+        "int main(int argc, char** argv) {\n"
+        '  FILE* fi = fopen(argv[1], "rb"); FILE* fo = fopen(argv[2], "wb");\n'
+        "  unsigned u;\n"
+        "  while (fread(&u, 4, 1, fi) == 1) { unsigned long long b = tp::f32_to_f64_bits(u); fwrite(&b, 8, 1, fo); }\n"
+        "  fclose(fi); fclose(fo); return 0;\n}\n")
+    exe = tmp_path / "cvt"
+    subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-std=c++17", "-I", csrc, str(src),
+                    "-o", str(exe)], check=True,
+                   capture_output=True)
+    rng = np.random.default_rng(7)
+    edge = np.array([0, 0x80000000, 1, 0x80000001, 0x007fffff, 0x00400000, 0x00000100, 0x00800000,
+                     0x7f7fffff, 0xff7fffff, 0x3f800000, 0x7f800000, 0xff800000, 0x7fc00000, 0x7f800001],
+                    dtype=np.uint32)
+    subn = rng.integers(0, 1 << 23, 20000, dtype=np.uint32) | (rng.integers(0, 2, 20000, dtype=np.uint32) << 31)
+    bits = np.concatenate([edge, subn, rng.integers(0, 1 << 32, 200000, dtype=np.uint64).astype(np.uint32)])
+    (tmp_path / "in.bin").write_bytes(bits.tobytes())
+    subprocess.run([str(exe), str(tmp_path / "in.bin"), str(tmp_path / "out.bin")], check=True)
+    got = np.frombuffer((tmp_path / "out.bin").read_bytes(), dtype=np.uint64)
+    assert got.size == bits.size
+    want = bits.view(np.float32).astype(np.float64)
+    nan = np.isnan(want)
+    assert np.array_equal(got[~nan], want[~nan].view(np.uint64))
+    assert np.all(np.isnan(got[nan].view(np.float64)))

@@ -22,11 +22,13 @@
 // The mixed form runs the single-launch factor and the block inverses in
 // double-single arithmetic (tp_dsf.cuh) on the same FP64 storage: its V-cycle
 // is FP32, so the last bits of FP64 buy its coarse correction nothing, while
-// FP64 instructions hold the FP64 unit ~67 cycles each (at 256x128x128 the
-// factor takes 28 ms instead of 33, the inverses 2.2 ms instead of 5.2; the
-// chain's serial pivot work and hand-offs then bound the factor). The sweeps
-// stay FP64: their phases wait on grid barriers and L2 reads, not on their
-// few multiply-adds.
+// FP64 instructions hold the FP64 unit ~67 cycles each. Its factor kernel
+// (pf_chain_ds / pf_bulk_ds) is laid out for FP32 latency rather than FP64
+// throughput: at 256x128x128 it takes 18 ms per factorisation against 28 ms
+// for the same double-single operations in the FP64 layout (and 33 ms in
+// FP64), with the same result bit for bit; the inverses take 2.2 ms instead
+// of 5.2. The sweeps stay FP64: their phases wait on grid barriers and L2
+// reads, not on their few multiply-adds.
 #include <algorithm>
 #include <type_traits>
 
@@ -273,43 +275,8 @@ __device__ __forceinline__ void diag_columns(V (*S)[NB + 1], V* rp, volatile int
   }
 }
 
-// Double-single form of the panel-tile solve, same column ownership: at FP32
-// speed the per-column hand-off dominates, and a named barrier over the four
-// warps (bar.sync 1, 128; it orders their shared-memory accesses) costs less
-// than the flag, fences and polls (16k against 21k cycles per tile). The
-// owner of the next column updates that column first. (For the diagonal
-// factor the flags stay ahead, 22k against 35k: there the warps that do not
-// own the pivot run ahead into their updates.)
+// named barrier 1 over warps 0-3 (orders their shared-memory accesses)
 __device__ __forceinline__ void bar_warps0to3() { asm volatile("bar.sync 1, 128;\n" ::: "memory"); }
-
-template <int W, bool FULL>
-__device__ __forceinline__ void trsm_columns_ds(Dsf (*A)[NB + 1], int nb, const Dsf (*Lb)[NB + 1], const Dsf* rp,
-                                                int t) {
-  Dsf v[8];
-#pragma unroll
-  for (int q = 0; q < 8; q++) {
-    const int c = W + 4 * q;
-    v[q] = (FULL || c < nb) ? A[t][c] : Dsf(0.f);
-  }
-#pragma unroll
-  for (int p = 0; p < NB; p++) {
-    if (!FULL && p >= nb) break;
-    if ((p & 3) == W) {
-      const Dsf x = v[p >> 2] * rp[p];
-      v[p >> 2] = x;
-      A[t][p] = x;
-    }
-    bar_warps0to3();
-    const Dsf xt = A[t][p];
-    if (((p + 1) & 3) == W && p + 1 < NB && (FULL || p + 1 < nb)) v[(p + 1) >> 2] -= xt * Lb[p + 1][p];
-#pragma unroll
-    for (int q = 0; q < 8; q++) {
-      const int c = W + 4 * q;
-      if (c > p + 1 && (FULL || c < nb)) v[q] -= xt * Lb[c][p];
-    }
-  }
-  // each column was stored in the step that finished it
-}
 
 template <typename V, bool FULL>
 __device__ __forceinline__ void diag_columns_of(int w, V (*S)[NB + 1], V* rp, volatile int* ready, int nb, long k,
@@ -423,24 +390,6 @@ __device__ __forceinline__ void trsm_tile(V (*A)[NB + 1], int nb, const V (*Lb)[
                                           volatile int* ready, int* info) {
   const int w = threadIdx.x >> 5, t = threadIdx.x & 31;
   if (w >= 4) return;
-  if constexpr (std::is_same<V, Dsf>::value) {
-    if (nb == NB) {
-      switch (w) {
-        case 0: trsm_columns_ds<0, true>(A, nb, Lb, rp, t); break;
-        case 1: trsm_columns_ds<1, true>(A, nb, Lb, rp, t); break;
-        case 2: trsm_columns_ds<2, true>(A, nb, Lb, rp, t); break;
-        default: trsm_columns_ds<3, true>(A, nb, Lb, rp, t); break;
-      }
-    } else {
-      switch (w) {
-        case 0: trsm_columns_ds<0, false>(A, nb, Lb, rp, t); break;
-        case 1: trsm_columns_ds<1, false>(A, nb, Lb, rp, t); break;
-        case 2: trsm_columns_ds<2, false>(A, nb, Lb, rp, t); break;
-        default: trsm_columns_ds<3, false>(A, nb, Lb, rp, t); break;
-      }
-    }
-    return;
-  }
   if (nb == NB) {
     switch (w) {
       case 0: trsm_columns<V, 0, true>(A, nb, Lb, rp, ready, info, t); break;
@@ -777,7 +726,9 @@ __device__ void pf_item(const PfArgs& a, long g, long& k, PfItem& it) {
     it.J = k + 1;
   } else {
     u -= T - 1;
-    long q = (long)((sqrt(8.0 * (double)u + 1.0) - 1.0) / 2.0);
+    // FP32 estimate (u < T (T + 1) / 2, a few hundred), corrected below: the
+    // FP64 square root is a long sequence on this part's FP64 pipe
+    long q = (long)((sqrtf(8.0f * (float)u + 1.0f) - 1.0f) * 0.5f);
     while ((q + 1) * (q + 2) / 2 <= u) q++;
     while (q * (q + 1) / 2 > u) q--;
     it.I = k + 2 + q;
@@ -923,13 +874,377 @@ __device__ void pf_bulk(const PfArgs& a, double* smem) {
   }
 }
 
+// ----------------------------------------------------------------------------
+// Double-single form of the single-launch factor. The schedule, the items and
+// the flags are those of pf_chain / pf_bulk, and every entry goes through the
+// same double-single operations in the same order, so the factor is the same
+// bit for bit (up to the sign of exact zeros); the work is arranged for the
+// latency of FP32 arithmetic instead of FP64 throughput. Measured on one CTA
+// (cycles per 32 x 32 tile): a pivot hand-off through a shared-memory flag
+// takes ~220 cycles, through a named barrier ~36; a double-single multiply,
+// shuffle and multiply-add chain ~40; and code that runs once per tile and
+// does not fit the instruction cache runs at a fraction of its warm speed
+// (the unrolled column factor: 19k warm, 31k cold). Hence:
+//  - the diagonal tile is factored by warps 0-3 with named-barrier hand-offs
+//    and a loop over pivots whose slot indices are compile-time (13k);
+//  - a panel tile is solved by four warps, each lane one row and every fourth
+//    column, a column's solved entry reaching the row's other lanes by
+//    shuffle (6.4k, no barrier per column); the chain's panel solve runs on
+//    warps 4-7 one column behind the factor;
+//  - fdone is released as soon as the factor is stored, ahead of the chain's
+//    own panel solve, which waits on the other CTAs;
+//  - tile products carry two outputs per f32x2 instruction (Dsf2);
+//  - conversions to FP64 storage use integer operations plus one add (ds_to).
+
+// wait of one warp (lane 0 polls, bounded); false if the factorisation is
+// being abandoned. __syncwarp orders the warp's later loads after the acquire.
+__device__ bool pf_wait_warp(const PfArgs& a, const int* flag, int target) {
+  int ok = 1;
+  if ((threadIdx.x & 31) == 0) {
+    for (long it = 0; ld_acquire(flag) < target; it++) {
+      if (*(volatile int*)a.abort_flag) {
+        ok = 0;
+        break;
+      }
+      if (it >= a.spin) {
+        atomicOr(a.info, kCoarseWaitGaveUp);
+        atomicExch(a.abort_flag, 1);
+        ok = 0;
+        break;
+      }
+    }
+  }
+  __syncwarp();
+  return __shfl_sync(0xffffffffu, ok, 0) != 0;
+}
+
+// tile (I, J) into A[r][c] as pairs (zero outside the matrix, above the
+// diagonal and outside the band) by nthr threads, thread i of them
+__device__ __forceinline__ void pf_load_ds(const PfArgs& a, long I, long J, Dsf (*A)[NB + 1], int i, int nthr) {
+  for (int idx = i; idx < NB * NB; idx += nthr) {
+    const int r = idx & 31, c = idx >> 5;
+    const long gr = 32 * I + r, gc = 32 * J + c;
+    const bool in = gr < a.n && gr >= gc && gr - gc <= a.bw;
+    A[r][c] = ds_from(in ? __ldcg(a.B + gc * a.bw + gr) : 0.0);
+  }
+}
+
+// Operand layouts of the tile product s(r, c) = sum_t a(r, t) b(c, t), one
+// CTA of 256 threads, thread (r = lane, warp ty) computing c = ty + 8q:
+//   PA[t][r] = (h, h, -h, -h), PL[t][r] = (-l, -l)      a(r, t)
+//   QB[t][c & 7][c >> 4] = (h(c0), h(c0 + 8), l(c0), l(c0 + 8)),
+//                          c0 = (c & 7) + 16 (c >> 4)    b(c, t)
+__device__ __forceinline__ void put_a(float4* PA, float2* PL, int t, int r, Dsf x) {
+  PA[t * 32 + r] = make_float4(x.h, x.h, -x.h, -x.h);
+  PL[t * 32 + r] = make_float2(-x.l, -x.l);
+}
+__device__ __forceinline__ void put_b(float4* QB, int t, int c, Dsf x) {
+  float* q = reinterpret_cast<float*>(QB + (t * 8 + (c & 7)) * 2 + (c >> 4));
+  const int half = (c >> 3) & 1;
+  q[half] = x.h;
+  q[2 + half] = x.l;
+}
+
+// s[q] = sum over t = 0..31, in order, of a(r, t) * b(ty + 8q, t), each as
+// Dsf's  s += a * b  from s = 0
+__device__ __forceinline__ void pf_products_ds(const float4* PA, const float2* PL, const float4* QB, Dsf s[4]) {
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  Dsf2 s01 = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)}, s23 = s01;
+#pragma unroll 8
+  for (int t = 0; t < NB; t++) {
+    const float4 pa = PA[t * 32 + tx];
+    const float2 pl = PL[t * 32 + tx];
+    const float4 q0 = QB[(t * 8 + ty) * 2], q1 = QB[(t * 8 + ty) * 2 + 1];
+    const float2 ah = make_float2(pa.x, pa.y), nah = make_float2(pa.z, pa.w);
+    ds2_add_prod(s01, ah, nah, pl, make_float2(q0.x, q0.y), make_float2(q0.z, q0.w));
+    ds2_add_prod(s23, ah, nah, pl, make_float2(q1.x, q1.y), make_float2(q1.z, q1.w));
+  }
+  s[0] = Dsf(s01.h.x, s01.l.x);
+  s[1] = Dsf(s01.h.y, s01.l.y);
+  s[2] = Dsf(s23.h.x, s23.l.x);
+  s[3] = Dsf(s23.h.y, s23.l.y);
+}
+
+// ready[j] == epoch (the step's number + 1, so nothing needs resetting
+// between steps), polled at most kFlagSpin times; a wait that gives up sets
+// kCoarseWaitGaveUp in *info.
+__device__ __forceinline__ void flag_wait_epoch(volatile int* flag, int epoch, int* info) {
+  int it = 0;
+  while (*flag != epoch && ++it < kFlagSpin) {
+  }
+  if (it >= kFlagSpin) atomicOr(info, kCoarseWaitGaveUp);
+  __threadfence_block();
+}
+
+// Factor of the diagonal tile by warps 0-3: warp W owns columns W + 4q
+// (v[q], lane t = row t). The owner of pivot j forms d = A(j, j) (a
+// non-positive one sets *info and is replaced by 1), r = 1/sqrt(d),
+// L(t, j) = A(t, j) r, writes Lcol[j][t] = L(t, j) and rp[j] = r, raises
+// ready[j] = epoch for warps outside the factor, and arrives on named
+// barrier 3 + (j & 3), on which the other three warps wait; then every warp
+// takes L(t, j) L(c, j) off its columns c > j. The loop over the four
+// pivots of a slot group is not unrolled and the group's slot is a
+// compile-time index, so the code is small and each step's updates form one
+// block the compiler can interleave. (Barrier 3 + (j & 3) is reused at pivot
+// j + 4 only after all four warps have passed pivots j + 1 .. j + 3, each of
+// which they reach through barrier j's phase.)
+__device__ __forceinline__ void diag_cols_ds(const Dsf (*Dt)[NB + 1], Dsf (*Lcol)[NB + 1], Dsf* rp,
+                                             volatile int* ready, int epoch, int nb, long k0, int* info) {
+  const int W = threadIdx.x >> 5, t = threadIdx.x & 31;
+  Dsf v[8];
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const int c = W + 4 * q;
+    v[q] = (t >= c && c < nb && t < nb) ? Dt[t][c] : Dsf(0.f);
+  }
+#pragma unroll
+  for (int qj = 0; qj < 8; qj++) {
+#pragma unroll 1
+    for (int jj = 0; jj < 4; jj++) {
+      const int j = 4 * qj + jj;
+      if (j >= nb) break;
+      if (jj == W) {
+        Dsf d = ds_shfl(v[qj], j);
+        if (!vpos(d)) {
+          if (t == 0) atomicCAS(info, 0, (int)(k0 + j + 1));
+          d = Dsf(1.f);
+        }
+        const Dsf r = ds_rsqrt(d);
+        const Dsf l = (t >= j) ? v[qj] * r : Dsf(0.f);
+        Lcol[j][t] = l;
+        if (t == 0) rp[j] = r;
+        __threadfence_block();
+        __syncwarp();
+        if (t == 0) ready[j] = epoch;
+        asm volatile("bar.arrive %0, 128;\n" ::"r"(3 + jj) : "memory");
+      } else {
+        asm volatile("bar.sync %0, 128;\n" ::"r"(3 + jj) : "memory");
+      }
+      const Dsf lt = Lcol[j][t];
+      const Dsf y = v[qj] - lt * Lcol[j][W + 4 * qj];
+      v[qj] = ds_sel(W > jj, y, v[qj]);
+#pragma unroll
+      for (int q = qj + 1; q < 8; q++) v[q] -= lt * Lcol[j][W + 4 * q];
+    }
+  }
+}
+
+// Panel tile solve X L_kk^T = A by four warps: lane (row r, g = lane >> 3)
+// holds v[q] = entry (r, g + 4q), rl = r & 7 its lane within the row's group
+// of lanes rl, rl + 8, rl + 16, rl + 24. Column p is finished by the lane of
+// group p & 3 (x = v / L(p, p), as v * rp[p]) and reaches the row's other
+// lanes by shuffle; each lane then takes x L(c, p) off its columns c > p.
+// wait(p) precedes column p (the chain's solve follows the factor column by
+// column). L(c, p) = LT ? Lm[p][c] : Lm[c][p]. Unrolled: every slot index
+// and column test is resolved at compile time (about 3.5k instructions,
+// executed once per panel tile).
+template <bool LT, typename Wait>
+__device__ __forceinline__ void trsm_rows_ds(const Dsf (*Lm)[NB + 1], const Dsf* rp, Dsf v[8], int rl, Wait wait) {
+  const int g = (threadIdx.x & 31) >> 3;
+#pragma unroll
+  for (int p = 0; p < NB; p++) {
+    wait(p);
+    const int qp = p >> 2;
+    const Dsf x = v[qp] * rp[p];
+    v[qp] = ds_sel(g == (p & 3), x, v[qp]);
+    const Dsf xt = ds_shfl(x, rl + 8 * (p & 3));
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      if (4 * q + 3 <= p) continue;  // columns all finished
+      const int c = g + 4 * q;
+      const Dsf y = v[q] - xt * (LT ? Lm[p][c] : Lm[c][p]);
+      v[q] = 4 * q > p ? y : ds_sel(c > p, y, v[q]);
+    }
+  }
+}
+
+__device__ __forceinline__ void bar_warps4to7() { asm volatile("bar.sync 2, 128;\n" ::: "memory"); }
+
+// smem offsets (in doubles) of the chain's and the other CTAs' buffers
+constexpr int kTile = NB * (NB + 1);  // a 32 x 33 tile of pairs
+constexpr int kPA = 2 * NB * NB, kPL = NB * NB, kQB = NB * NB;
+
+// The chain CTA, step k: warps 0-3 factor tile (k,k) and store it; warps 4-7
+// wait for and load the panel tile (k+1,k), solve it column by column as the
+// factor's columns appear, store it and lay it out as the product's
+// operands, and load tile (k+1,k+1); then all eight warps apply
+// (k+1,k+1) -= X X^T, which the next step factors.
+__device__ void pf_chain_ds(const PfArgs& a, double* smem) {
+  Dsf(*Lcol)[NB + 1] = reinterpret_cast<Dsf(*)[NB + 1]>(smem + 2 * kTile);
+  Dsf(*Xa)[NB + 1] = reinterpret_cast<Dsf(*)[NB + 1]>(smem + 3 * kTile);
+  Dsf* rp = reinterpret_cast<Dsf*>(smem + 4 * kTile);
+  float4* PA = reinterpret_cast<float4*>(smem + 4 * kTile + NB);
+  float2* PL = reinterpret_cast<float2*>(smem + 4 * kTile + NB + kPA);
+  float4* QB = reinterpret_cast<float4*>(smem + 4 * kTile + NB + kPA + kPL);
+  volatile int* ready = reinterpret_cast<volatile int*>(smem + 4 * kTile + NB + kPA + kPL + kQB);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x < NB) ready[threadIdx.x] = 0;
+  pf_load_ds(a, 0, 0, reinterpret_cast<Dsf(*)[NB + 1]>(smem), threadIdx.x, blockDim.x);
+  __syncthreads();
+  for (long k = 0; k < a.NT; k++) {
+    Dsf(*D)[NB + 1] = reinterpret_cast<Dsf(*)[NB + 1]>(smem + (k & 1) * kTile);  // tiles (k,k), (k+1,k+1)
+    Dsf(*Dn)[NB + 1] = reinterpret_cast<Dsf(*)[NB + 1]>(smem + ((k + 1) & 1) * kTile);
+    const int nb = (int)lmin(NB, a.n - 32 * k);
+    const bool more = pf_imax(a.n, a.bw, k) >= k + 1;
+    const bool prev = k >= 1 && k + 1 <= pf_imax(a.n, a.bw, k - 1);  // tiles (k+1, *) hold a step k-1 update
+    const int epoch = (int)k + 1;
+    int ok = 1;
+    if (w < 4) {
+      diag_cols_ds(D, Lcol, rp, ready, epoch, nb, 32 * k, a.info);
+      bar_warps0to3();
+      for (int idx = threadIdx.x; idx < NB * NB; idx += 128) {  // L_kk, lower part
+        const int r = idx & 31, c = idx >> 5;
+        const long gr = 32 * k + r, gc = 32 * k + c;
+        if (gr < a.n && gr >= gc && gr - gc <= a.bw) a.B[gc * a.bw + gr] = ds_to(Lcol[c][r]);
+      }
+      if (threadIdx.x < NB) a.rpk[k * NB + threadIdx.x] = threadIdx.x < nb ? ds_to(rp[threadIdx.x]) : 0.0;
+      // the four warps' stores happen before the barrier, the barrier before
+      // thread 0's release (cumulative): the other CTAs' panel solves of step k
+      // start now, not after this CTA's own panel solve
+      bar_warps0to3();
+      if (threadIdx.x == 0) asm volatile("st.release.gpu.global.s32 [%0], %1;\n" ::"l"(a.fdone + k), "r"(1) : "memory");
+    } else if (more) {
+      const int i4 = threadIdx.x - 128;
+      if (prev) ok = pf_wait_warp(a, a.tver + k * a.TS + 1, (int)k);
+      if (ok) pf_load_ds(a, k + 1, k, Xa, i4, 128);
+      bar_warps4to7();
+      if (ok && prev) ok = pf_wait_warp(a, a.tver + (k + 1) * a.TS, (int)k);
+      double dn[8];  // entries i4 + 128 m of tile (k+1, k+1), in flight during the solve
+#pragma unroll
+      for (int m = 0; m < 8; m++) {
+        const int idx = i4 + 128 * m, r = idx & 31, c = idx >> 5;
+        const long gr = 32 * (k + 1) + r, gc = 32 * (k + 1) + c;
+        dn[m] = (ok && gr < a.n && gr >= gc && gr - gc <= a.bw) ? __ldcg(a.B + gc * a.bw + gr) : 0.0;
+      }
+      const int r = 8 * (w - 4) + (lane & 7), g = lane >> 3;
+      Dsf v[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) v[q] = Xa[r][g + 4 * q];
+      trsm_rows_ds<true>(Lcol, rp, v, lane & 7, [&](int p) { flag_wait_epoch(&ready[p], epoch, a.info); });
+      const long gr = 32 * (k + 1) + r;
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const int c = g + 4 * q;
+        const long gc = 32 * k + c;
+        if (gr < a.n && gr - gc <= a.bw) a.B[gc * a.bw + gr] = ds_to(v[q]);
+        put_a(PA, PL, c, r, v[q]);
+        put_b(QB, c, r, v[q]);
+      }
+#pragma unroll
+      for (int m = 0; m < 8; m++) {
+        const int idx = i4 + 128 * m;
+        Dn[idx & 31][idx >> 5] = ds_from(dn[m]);
+      }
+    }
+    // the stores of the panel tile happen before the barrier, the barrier
+    // before thread 0's release (cumulative)
+    if (!__syncthreads_and(ok)) return;
+    if (!more) break;
+    if (threadIdx.x == 0) asm volatile("st.release.gpu.global.s32 [%0], %1;\n" ::"l"(a.sdone + k * a.TS + 1), "r"(1) : "memory");
+    // tile (k+1, k+1) -= X X^T, lower part
+    Dsf s[4];
+    pf_products_ds(PA, PL, QB, s);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int c = w + 8 * q;
+      if (lane >= c) Dn[lane][c] -= s[q];
+    }
+    __syncthreads();
+  }
+}
+
+__device__ void pf_bulk_ds(const PfArgs& a, double* smem) {
+  Dsf(*P)[NB + 1] = reinterpret_cast<Dsf(*)[NB + 1]>(smem);
+  Dsf(*Q)[NB + 1] = reinterpret_cast<Dsf(*)[NB + 1]>(smem + kTile);
+  Dsf* rp = reinterpret_cast<Dsf*>(smem + 2 * kTile);
+  float4* PA = reinterpret_cast<float4*>(smem + 2 * kTile + NB);
+  float2* PL = reinterpret_cast<float2*>(smem + 2 * kTile + NB + kPA);
+  float4* QB = reinterpret_cast<float4*>(smem + 2 * kTile + NB + kPA + kPL);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long nbulk = gridDim.x - 1, total = a.off[a.NT];
+  long g = blockIdx.x - 1, kk = 0;
+  if (g >= total) return;
+  PfItem cur, nxt;
+  PfRegs R;
+  pf_item(a, g, kk, cur);
+  bool have = false;
+  for (; g < total; g += nbulk) {
+    if (!have) {
+      if (!pf_wait_item(a, cur)) return;
+      pf_fetch(a, cur, R);
+    }
+#pragma unroll
+    for (int m = 0; m < 4; m++) {  // S: tile (I,k) and L_kk row-major; U: the product's operands
+      const int idx = threadIdx.x + 256 * m, r = idx & 31, c = idx >> 5;
+      const Dsf p = ds_from(R.p[m]), q = ds_from(R.q[m]);
+      if (cur.solve) {
+        P[r][c] = p;
+        Q[r][c] = q;
+      } else {
+        put_a(PA, PL, c, r, p);
+        put_b(QB, c, r, q);
+      }
+    }
+    if (cur.solve && threadIdx.x < NB) rp[threadIdx.x] = ds_from(R.r);
+    __syncthreads();
+    have = false;
+    if (g + nbulk < total) {
+      pf_item(a, g + nbulk, kk, nxt);
+      if (pf_ready(nxt)) {
+        pf_fetch(a, nxt, R);  // in flight while this item is computed
+        have = true;
+      }
+    }
+    if (cur.solve) {
+      if (w < 4) {
+        const int r = 8 * w + (lane & 7), gq = lane >> 3;
+        Dsf v[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) v[q] = P[r][gq + 4 * q];
+        trsm_rows_ds<false>(Q, rp, v, lane & 7, [](int) {});
+        const long gr = 32 * cur.I + r;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          const long gc = 32 * cur.k + gq + 4 * q;
+          if (gr < a.n && gr - gc <= a.bw) a.B[gc * a.bw + gr] = ds_to(v[q]);
+        }
+      }
+      pf_release(a.sdone + cur.k * a.TS + (cur.I - cur.k), 1);
+    } else {
+      const long gr = 32 * cur.I + lane;
+      double old[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {  // the tile's current values, loaded before the products
+        const long gc = 32 * cur.J + w + 8 * q;
+        old[q] = (gr < a.n && gc <= gr && gr - gc <= a.bw) ? __ldcg(a.B + gc * a.bw + gr) : 0.0;
+      }
+      Dsf s[4];
+      pf_products_ds(PA, PL, QB, s);
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const long gc = 32 * cur.J + w + 8 * q;
+        if (gr < a.n && gc <= gr && gr - gc <= a.bw) a.B[gc * a.bw + gr] = ds_to(ds_from(old[q]) - s[q]);
+      }
+      pf_release(a.tver + cur.J * a.TS + (cur.I - cur.J), (int)cur.k + 1);
+    }
+    cur = nxt;
+  }
+}
+
 template <typename V>
 __global__ void __launch_bounds__(256) pf_kernel(PfArgs a) {
   extern __shared__ double sm[];
-  if (blockIdx.x == 0)
-    pf_chain<V>(a, sm);
-  else
-    pf_bulk<V>(a, sm);
+  if constexpr (std::is_same<V, Dsf>::value) {
+    if (blockIdx.x == 0)
+      pf_chain_ds(a, sm);
+    else
+      pf_bulk_ds(a, sm);
+  } else {
+    if (blockIdx.x == 0)
+      pf_chain<V>(a, sm);
+    else
+      pf_bulk<V>(a, sm);
+  }
 }
 
 // Inverse of each diagonal NBSxNBS block of L, one CTA per (block, 32-column

@@ -69,7 +69,28 @@ __device__ __forceinline__ Dsf ds_from(double v) {
                             __uint_as_float((unsigned)(e - 896) << 23));
   return Dsf(h, sg ? -l : l);
 }
-__device__ __forceinline__ double ds_to(Dsf a) { return (double)a.h + (double)a.l; }
+// float -> double bits with integer operations, exact as the conversion is:
+// on this part a conversion to FP64 holds the FP64 pipe as long as an add
+// does (~67 cycles per warp instruction), so ds_to would otherwise cost three
+// FP64 instructions instead of one. Subnormal floats are normalised; NaN
+// keeps its payload with the quiet bit set.
+__host__ __device__ __forceinline__ unsigned long long f32_to_f64_bits(unsigned u) {
+  const unsigned long long sg = (unsigned long long)(u >> 31) << 63;
+  const unsigned e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  if (e == 0xffu) return sg | (0x7ffULL << 52) | ((unsigned long long)m << 29) | (m ? (1ULL << 51) : 0ULL);
+  if (e != 0u) return sg | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29);
+  if (m == 0u) return sg;
+#ifdef __CUDA_ARCH__
+  const int p = 31 - __clz((int)m);  // top bit of a subnormal's mantissa, 0..22: value 2^(p-149) * 1.f
+#else
+  const int p = 31 - __builtin_clz(m);
+#endif
+  return sg | ((unsigned long long)(p + 874) << 52) | (((unsigned long long)m << (52 - p)) & 0xfffffffffffffULL);
+}
+__device__ __forceinline__ double ds_to(Dsf a) {
+  return __longlong_as_double((long long)f32_to_f64_bits(__float_as_uint(a.h))) +
+         __longlong_as_double((long long)f32_to_f64_bits(__float_as_uint(a.l)));
+}
 
 // 1/sqrt(d): the FP32 estimate h = rsqrtf(d) refined by one Newton step for
 // the reciprocal square root, r = h + h (1 - d h^2) / 2, with 1 - d h^2
@@ -100,8 +121,34 @@ __device__ __forceinline__ Dsf ds_rcp(Dsf d) {
 }
 __device__ __forceinline__ Dsf& operator*=(Dsf& a, Dsf b) { return a = a * b; }
 __device__ __forceinline__ float ds_val(Dsf a) { return __fadd_rn(a.h, a.l); }
+__device__ __forceinline__ Dsf ds_sel(bool c, Dsf a, Dsf b) { return Dsf(c ? a.h : b.h, c ? a.l : b.l); }
 __device__ __forceinline__ Dsf ds_shfl(Dsf v, int src) {
   return Dsf(__shfl_sync(0xffffffffu, v.h, src), __shfl_sync(0xffffffffu, v.l, src));
+}
+
+// Two double-single values in the halves of float2 registers: each FP32 step
+// of Dsf's + and * becomes one f32x2 instruction for both values. The halves
+// round to nearest independently, so each is the scalar result bit for bit.
+// The operand a is the same in both halves and comes with its negated parts,
+// so that the product's error terms can be formed negated where the scalar
+// form negates an operand: fma(-x, y, z) = -fma(x, y, -z) exactly (round to
+// nearest is odd-symmetric), and the sum never waits on a negation.
+struct Dsf2 {
+  float2 h, l;
+};
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+
+// acc + (a * b), a = (ah, -nah, -nal): p = a.h b.h, ne = -(the product's error)
+__device__ __forceinline__ void ds2_add_prod(Dsf2& acc, float2 ah, float2 nah, float2 nal, float2 bh, float2 bl) {
+  const float2 p = __fmul2_rn(ah, bh);
+  float2 ne = __ffma2_rn(nah, bh, p);
+  ne = __ffma2_rn(nah, bl, ne);
+  ne = __ffma2_rn(nal, bh, ne);
+  const float2 s = __fadd2_rn(acc.h, p);
+  const float2 bb = f2sub(s, acc.h);
+  const float2 e = __fadd2_rn(f2sub(acc.h, f2sub(s, bb)), f2sub(p, bb));
+  acc.l = __fadd2_rn(e, f2sub(acc.l, ne));
+  acc.h = s;
 }
 
 // storage (double) <-> value type V of a kernel written for both

@@ -137,6 +137,81 @@ def test_band_cholesky_schedule(grid):
     assert k >= NT and all(p >= total for p in pos), "the schedule stalls"
 
 
+@pytest.mark.parametrize("grid", list(GRIDS), ids=list(GRIDS))
+def test_band_cholesky_schedule_double_single(grid):
+    """The double-single form of the factor (pf_chain_ds / pf_bulk_ds) takes
+    the same items in the same round-robin order, but its chain waits
+    differently: fdone[k] is released right after the factor is stored, and
+    the panel solve waits for step k-1's updates of tiles (k+1,k) and
+    (k+1,k+1) together. A replay with these waits runs to the end."""
+    n, bw = GRIDS[grid]
+    NT = (n + 31) // 32
+    off = [0]
+    for k in range(NT):
+        T = pf_imax(n, bw, k) - k
+        off.append(off[-1] + ((T - 1) + T * (T + 1) // 2 - 1 if T >= 1 else 0))
+    total, nbulk = off[-1], NSM - 1
+
+    def deps_of(g, k):
+        while off[k + 1] <= g:
+            k += 1
+        idx = g - off[k]
+        T = pf_imax(n, bw, k) - k
+        prev = pf_imax(n, bw, k - 1) if k >= 1 else -1
+        if idx < T - 1:
+            I = k + 2 + idx
+            return k, [("f", k)] + ([("t", k, I - k, k)] if I <= prev else []), [("s", k, I - k)]
+        u = idx - (T - 1)
+        if u < T - 1:
+            I, J = k + 2 + u, k + 1
+        else:
+            u -= T - 1
+            q = 0
+            while (q + 1) * (q + 2) // 2 <= u:
+                q += 1
+            I, J = k + 2 + q, k + 2 + (u - q * (q + 1) // 2)
+        deps = [("s", k, I - k)] + ([("s", k, J - k)] if J != I else []) + ([("t", J, I - J, k)] if I <= prev else [])
+        return k, deps, [("t", J, I - J, k + 1)]
+
+    done, tver = set(), {}
+
+    def sat(d):
+        return tver.get((d[1], d[2]), 0) >= d[3] if d[0] == "t" else d in done
+
+    pos, kpos = list(range(nbulk)), [0] * nbulk
+    k, ph, progress = 0, 0, True
+    while progress:
+        progress = False
+        while k < NT:
+            prev = k >= 1 and k + 1 <= pf_imax(n, bw, k - 1)
+            if ph == 0:  # factor tile (k, k), store it, release fdone[k]
+                done.add(("f", k))
+                progress = True
+                if pf_imax(n, bw, k) < k + 1:
+                    k = NT
+                    break
+                ph = 1
+            if ph == 1:  # tiles (k+1, k) and (k+1, k+1) after step k-1's updates
+                if prev and not (sat(("t", k, 1, k)) and sat(("t", k + 1, 0, k))):
+                    break
+                done.add(("s", k, 1))
+                tver[(k + 1, 0)] = k + 1
+                k, ph, progress = k + 1, 0, True
+        for b in range(nbulk):
+            while pos[b] < total:
+                kpos[b], deps, outs = deps_of(pos[b], kpos[b])
+                if not all(sat(d) for d in deps):
+                    break
+                for o in outs:
+                    if o[0] == "t":
+                        tver[(o[1], o[2])] = o[3]
+                    else:
+                        done.add(o)
+                pos[b] += nbulk
+                progress = True
+    assert k >= NT and all(p >= total for p in pos), "the schedule stalls"
+
+
 def ps_warp_row(w, R, P):
     if R == 4:
         return ((w >> 1) if w < 4 else 3 - ((w - 4) >> 1)), w & 1

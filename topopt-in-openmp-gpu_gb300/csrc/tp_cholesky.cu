@@ -979,17 +979,17 @@ __device__ __forceinline__ void flag_wait_epoch(volatile int* flag, int epoch, i
 // Factor of the diagonal tile by warps 0-3: warp W owns columns W + 4q
 // (v[q], lane t = row t). The owner of pivot j forms d = A(j, j) (a
 // non-positive one sets *info and is replaced by 1), r = 1/sqrt(d),
-// L(t, j) = A(t, j) r, writes Lcol[j][t] = L(t, j) and rp[j] = r, raises
-// ready[j] = epoch for warps outside the factor, and arrives on named
-// barrier 3 + (j & 3), on which the other three warps wait; then every warp
+// L(t, j) = A(t, j) r, writes Lcol[j][t] = L(t, j) and rp[j] = r, and
+// arrives on named barrier 3 + (j & 3), on which the other three warps
+// wait; then every warp
 // takes L(t, j) L(c, j) off its columns c > j. The loop over the four
 // pivots of a slot group is not unrolled and the group's slot is a
 // compile-time index, so the code is small and each step's updates form one
 // block the compiler can interleave. (Barrier 3 + (j & 3) is reused at pivot
 // j + 4 only after all four warps have passed pivots j + 1 .. j + 3, each of
 // which they reach through barrier j's phase.)
-__device__ __forceinline__ void diag_cols_ds(const Dsf (*Dt)[NB + 1], Dsf (*Lcol)[NB + 1], Dsf* rp,
-                                             volatile int* ready, int epoch, int nb, long k0, int* info) {
+__device__ __forceinline__ void diag_cols_ds(const Dsf (*Dt)[NB + 1], Dsf (*Lcol)[NB + 1], Dsf* rp, int nb, long k0,
+                                             int* info) {
   const int W = threadIdx.x >> 5, t = threadIdx.x & 31;
   Dsf v[8];
 #pragma unroll
@@ -1013,9 +1013,6 @@ __device__ __forceinline__ void diag_cols_ds(const Dsf (*Dt)[NB + 1], Dsf (*Lcol
         const Dsf l = (t >= j) ? v[qj] * r : Dsf(0.f);
         Lcol[j][t] = l;
         if (t == 0) rp[j] = r;
-        __threadfence_block();
-        __syncwarp();
-        if (t == 0) ready[j] = epoch;
         asm volatile("bar.arrive %0, 128;\n" ::"r"(3 + jj) : "memory");
       } else {
         asm volatile("bar.sync %0, 128;\n" ::"r"(3 + jj) : "memory");
@@ -1029,46 +1026,43 @@ __device__ __forceinline__ void diag_cols_ds(const Dsf (*Dt)[NB + 1], Dsf (*Lcol
   }
 }
 
-// Panel tile solve X L_kk^T = A by four warps: lane (row r, g = lane >> 3)
-// holds v[q] = entry (r, g + 4q), rl = r & 7 its lane within the row's group
-// of lanes rl, rl + 8, rl + 16, rl + 24. Column p is finished by the lane of
-// group p & 3 (x = v / L(p, p), as v * rp[p]) and reaches the row's other
-// lanes by shuffle; each lane then takes x L(c, p) off its columns c > p.
-// wait(p) precedes column p (the chain's solve follows the factor column by
-// column). L(c, p) = LT ? Lm[p][c] : Lm[c][p]. Unrolled: every slot index
-// and column test is resolved at compile time (about 3.5k instructions,
-// executed once per panel tile).
-template <bool LT, typename Wait>
-__device__ __forceinline__ void trsm_rows_ds(const Dsf (*Lm)[NB + 1], const Dsf* rp, Dsf v[8], int rl, Wait wait) {
-  const int g = (threadIdx.x & 31) >> 3;
+// Panel tile solve X L_kk^T = A by the CTA's eight warps: lane (row
+// r = 4w + (lane & 3), g = lane >> 2) holds v[q] = entry (r, g + 8q). Column p
+// is finished by the lane of group p & 7 (x = v / L(p, p), as v * rp[p]) and
+// reaches the row's other lanes (lane & 3) + 4g by shuffle; each lane then
+// takes x L(c, p) off its columns c > p. L(c, p) = LT ? Lm[p][c] : Lm[c][p].
+// Unrolled: every slot index and column test is resolved at compile time
+// (about 2.5k instructions, run once per panel tile); with two warps per
+// scheduler the column chain (multiply, shuffle, multiply-add) overlaps the
+// other columns' updates.
+template <bool LT>
+__device__ __forceinline__ void trsm_rows_ds(const Dsf (*Lm)[NB + 1], const Dsf* rp, Dsf v[4]) {
+  const int lane = threadIdx.x & 31, rl = lane & 3, g = lane >> 2;
 #pragma unroll
   for (int p = 0; p < NB; p++) {
-    wait(p);
-    const int qp = p >> 2;
+    const int qp = p >> 3;
     const Dsf x = v[qp] * rp[p];
-    v[qp] = ds_sel(g == (p & 3), x, v[qp]);
-    const Dsf xt = ds_shfl(x, rl + 8 * (p & 3));
+    v[qp] = ds_sel(g == (p & 7), x, v[qp]);
+    const Dsf xt = ds_shfl(x, rl + 4 * (p & 7));
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
-      if (4 * q + 3 <= p) continue;  // columns all finished
-      const int c = g + 4 * q;
+    for (int q = 0; q < 4; q++) {
+      if (8 * q + 7 <= p) continue;  // columns all finished
+      const int c = g + 8 * q;
       const Dsf y = v[q] - xt * (LT ? Lm[p][c] : Lm[c][p]);
-      v[q] = 4 * q > p ? y : ds_sel(c > p, y, v[q]);
+      v[q] = 8 * q > p ? y : ds_sel(c > p, y, v[q]);
     }
   }
 }
 
-__device__ __forceinline__ void bar_warps4to7() { asm volatile("bar.sync 2, 128;\n" ::: "memory"); }
-
 // smem offsets (in doubles) of the chain's and the other CTAs' buffers
 constexpr int kTile = NB * (NB + 1);  // a 32 x 33 tile of pairs
-constexpr int kPA = 2 * NB * NB, kPL = NB * NB, kQB = NB * NB;
+constexpr int kPA = 2 * NB * NB, kPL = NB * NB;  // PA, PL; then QB (NB * NB doubles)
 
-// The chain CTA, step k: warps 0-3 factor tile (k,k) and store it; warps 4-7
-// wait for and load the panel tile (k+1,k), solve it column by column as the
-// factor's columns appear, store it and lay it out as the product's
-// operands, and load tile (k+1,k+1); then all eight warps apply
-// (k+1,k+1) -= X X^T, which the next step factors.
+// The chain CTA, step k: warps 0-3 factor tile (k,k), store it and release
+// fdone[k]; meanwhile warps 4-7 wait for and load the panel tile (k+1,k) and
+// start loading tile (k+1,k+1). Then all eight warps solve the panel tile,
+// store it, release sdone and lay it out as the product's operands, and
+// apply (k+1,k+1) -= X X^T, which the next step factors.
 __device__ void pf_chain_ds(const PfArgs& a, double* smem) {
   Dsf(*Lcol)[NB + 1] = reinterpret_cast<Dsf(*)[NB + 1]>(smem + 2 * kTile);
   Dsf(*Xa)[NB + 1] = reinterpret_cast<Dsf(*)[NB + 1]>(smem + 3 * kTile);
@@ -1076,9 +1070,7 @@ __device__ void pf_chain_ds(const PfArgs& a, double* smem) {
   float4* PA = reinterpret_cast<float4*>(smem + 4 * kTile + NB);
   float2* PL = reinterpret_cast<float2*>(smem + 4 * kTile + NB + kPA);
   float4* QB = reinterpret_cast<float4*>(smem + 4 * kTile + NB + kPA + kPL);
-  volatile int* ready = reinterpret_cast<volatile int*>(smem + 4 * kTile + NB + kPA + kPL + kQB);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (threadIdx.x < NB) ready[threadIdx.x] = 0;
   pf_load_ds(a, 0, 0, reinterpret_cast<Dsf(*)[NB + 1]>(smem), threadIdx.x, blockDim.x);
   __syncthreads();
   for (long k = 0; k < a.NT; k++) {
@@ -1087,10 +1079,10 @@ __device__ void pf_chain_ds(const PfArgs& a, double* smem) {
     const int nb = (int)lmin(NB, a.n - 32 * k);
     const bool more = pf_imax(a.n, a.bw, k) >= k + 1;
     const bool prev = k >= 1 && k + 1 <= pf_imax(a.n, a.bw, k - 1);  // tiles (k+1, *) hold a step k-1 update
-    const int epoch = (int)k + 1;
     int ok = 1;
+    double dn[8];  // entries i4 + 128 m of tile (k+1, k+1), in flight during the panel solve
     if (w < 4) {
-      diag_cols_ds(D, Lcol, rp, ready, epoch, nb, 32 * k, a.info);
+      diag_cols_ds(D, Lcol, rp, nb, 32 * k, a.info);
       bar_warps0to3();
       for (int idx = threadIdx.x; idx < NB * NB; idx += 128) {  // L_kk, lower part
         const int r = idx & 31, c = idx >> 5;
@@ -1107,39 +1099,42 @@ __device__ void pf_chain_ds(const PfArgs& a, double* smem) {
       const int i4 = threadIdx.x - 128;
       if (prev) ok = pf_wait_warp(a, a.tver + k * a.TS + 1, (int)k);
       if (ok) pf_load_ds(a, k + 1, k, Xa, i4, 128);
-      bar_warps4to7();
       if (ok && prev) ok = pf_wait_warp(a, a.tver + (k + 1) * a.TS, (int)k);
-      double dn[8];  // entries i4 + 128 m of tile (k+1, k+1), in flight during the solve
 #pragma unroll
       for (int m = 0; m < 8; m++) {
         const int idx = i4 + 128 * m, r = idx & 31, c = idx >> 5;
         const long gr = 32 * (k + 1) + r, gc = 32 * (k + 1) + c;
         dn[m] = (ok && gr < a.n && gr >= gc && gr - gc <= a.bw) ? __ldcg(a.B + gc * a.bw + gr) : 0.0;
       }
-      const int r = 8 * (w - 4) + (lane & 7), g = lane >> 3;
-      Dsf v[8];
+    }
+    if (!__syncthreads_and(ok)) return;
+    if (!more) break;
+    {  // panel tile (k+1, k): into the band and into the product's operands
+      const int r = 4 * w + (lane & 3), g = lane >> 2;
+      Dsf v[4];
 #pragma unroll
-      for (int q = 0; q < 8; q++) v[q] = Xa[r][g + 4 * q];
-      trsm_rows_ds<true>(Lcol, rp, v, lane & 7, [&](int p) { flag_wait_epoch(&ready[p], epoch, a.info); });
+      for (int q = 0; q < 4; q++) v[q] = Xa[r][g + 8 * q];
+      trsm_rows_ds<true>(Lcol, rp, v);
       const long gr = 32 * (k + 1) + r;
 #pragma unroll
-      for (int q = 0; q < 8; q++) {
-        const int c = g + 4 * q;
+      for (int q = 0; q < 4; q++) {
+        const int c = g + 8 * q;
         const long gc = 32 * k + c;
         if (gr < a.n && gr - gc <= a.bw) a.B[gc * a.bw + gr] = ds_to(v[q]);
         put_a(PA, PL, c, r, v[q]);
         put_b(QB, c, r, v[q]);
       }
+    }
+    if (w >= 4) {
 #pragma unroll
       for (int m = 0; m < 8; m++) {
-        const int idx = i4 + 128 * m;
+        const int idx = threadIdx.x - 128 + 128 * m;
         Dn[idx & 31][idx >> 5] = ds_from(dn[m]);
       }
     }
     // the stores of the panel tile happen before the barrier, the barrier
     // before thread 0's release (cumulative)
-    if (!__syncthreads_and(ok)) return;
-    if (!more) break;
+    __syncthreads();
     if (threadIdx.x == 0) asm volatile("st.release.gpu.global.s32 [%0], %1;\n" ::"l"(a.sdone + k * a.TS + 1), "r"(1) : "memory");
     // tile (k+1, k+1) -= X X^T, lower part
     Dsf s[4];
@@ -1173,6 +1168,14 @@ __device__ void pf_bulk_ds(const PfArgs& a, double* smem) {
       if (!pf_wait_item(a, cur)) return;
       pf_fetch(a, cur, R);
     }
+    // the next item's flags, probed now (one look, no wait) so that the
+    // acquire's round trip overlaps the layout of this item's operands
+    const bool more = g + nbulk < total;
+    int okn = 0;
+    if (more) {
+      pf_item(a, g + nbulk, kk, nxt);
+      okn = threadIdx.x < nxt.nf ? ld_acquire(nxt.flag(threadIdx.x)) >= nxt.target(threadIdx.x) : 1;
+    }
 #pragma unroll
     for (int m = 0; m < 4; m++) {  // S: tile (I,k) and L_kk row-major; U: the product's operands
       const int idx = threadIdx.x + 256 * m, r = idx & 31, c = idx >> 5;
@@ -1186,26 +1189,19 @@ __device__ void pf_bulk_ds(const PfArgs& a, double* smem) {
       }
     }
     if (cur.solve && threadIdx.x < NB) rp[threadIdx.x] = ds_from(R.r);
-    __syncthreads();
-    have = false;
-    if (g + nbulk < total) {
-      pf_item(a, g + nbulk, kk, nxt);
-      if (pf_ready(nxt)) {
-        pf_fetch(a, nxt, R);  // in flight while this item is computed
-        have = true;
-      }
-    }
+    have = __syncthreads_and(okn) != 0;  // false when there is no next item
+    if (have) pf_fetch(a, nxt, R);       // in flight while this item is computed
     if (cur.solve) {
-      if (w < 4) {
-        const int r = 8 * w + (lane & 7), gq = lane >> 3;
-        Dsf v[8];
+      {
+        const int r = 4 * w + (lane & 3), gq = lane >> 2;
+        Dsf v[4];
 #pragma unroll
-        for (int q = 0; q < 8; q++) v[q] = P[r][gq + 4 * q];
-        trsm_rows_ds<false>(Q, rp, v, lane & 7, [](int) {});
+        for (int q = 0; q < 4; q++) v[q] = P[r][gq + 8 * q];
+        trsm_rows_ds<false>(Q, rp, v);
         const long gr = 32 * cur.I + r;
 #pragma unroll
-        for (int q = 0; q < 8; q++) {
-          const long gc = 32 * cur.k + gq + 4 * q;
+        for (int q = 0; q < 4; q++) {
+          const long gc = 32 * cur.k + gq + 8 * q;
           if (gr < a.n && gr - gc <= a.bw) a.B[gc * a.bw + gr] = ds_to(v[q]);
         }
       }

@@ -108,6 +108,26 @@ def test_oc_update(case):
     assert ch == pytest.approx(expect, rel=1e-6)
 
 
+def test_oc_update_nonpositive_dv(case):
+    """The OC bisection with some dv zero or negative: the first phase's
+    binary search needs every dv > 0, so these inputs take the sequential
+    steps; the result still matches the oracle's bisection, and a second
+    update with all dv > 0 (the search) matches it too."""
+    from oracle import Oracle
+    g, ctx, torch = case
+    orc = Oracle(*ctx.shape, ctx.nl)
+    x, dc = g["oc_x"], g["oc_dc"]
+    for dv in (np.where(np.arange(g["oc_dv"].size) % 7 == 0, 0.0, g["oc_dv"]),
+               np.where(np.arange(g["oc_dv"].size) % 11 == 3, -g["oc_dv"], g["oc_dv"]),
+               g["oc_dv"] * 1.5):
+        ctx.upload("x", x)
+        ctx.upload("dv", dv)
+        ctx.upload("dc", dc)
+        ctx.oc_update(float(g["oc_g"]))
+        want = orc.oc_update(x, dv, dc, float(g["oc_g"]))
+        assert relerr(ctx.download("xnew"), want) < 1e-12
+
+
 def test_coarse_direct_solve(case):
     """The GPU band Cholesky against the oracle's on the same coarsest operator."""
     from oracle import Oracle

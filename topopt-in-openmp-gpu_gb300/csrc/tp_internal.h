@@ -63,6 +63,9 @@ enum Scalar {
   S_IT,     // (column 0) iteration counter of the captured CG loop
   S_G,      // (column 0) constraint value g = vol - volfrac of the OC bisection
   S_RL,     // (column 0) 1/sqrt(lmid) of the next bisection step, formed once per step
+  S_BLO,    // (column 0) the bisection's first phase, searched: steps below BLO keep gt <= 0,
+  S_BHI,    //            step BHI has gt > 0 (or BHI = cap + 1); S_TMP1 the step probed
+  S_DVBAD,  // (column 0) nonzero when some dv is not positive: the first phase runs step by step
   S_COUNT
 };
 

@@ -326,6 +326,11 @@ void volume_partials(tp_ctx* c, const double* xphys, int* nblocks) {
 }
 
 // ----------------------------------------------------------------------------
+// The bisection takes at most kOcCap steps (then oc_bisect reports that it
+// did not finish); a step after the cap, or after the interval is narrow
+// enough, returns at once.
+constexpr int kOcCap = 240;
+
 // OC: xnew = max(0, max(x - move, min(1, min(x + move, x*sqrt(-dc/(dv*lmid))))))
 // with the reference's MAX/MIN macros (a > b ? a : b), move = 0.2.
 __device__ __forceinline__ double oc_xnew(double x, double dc, double dv, double lmid) {
@@ -365,13 +370,14 @@ __device__ __forceinline__ double oc_clamp(double lo, double hi, double v) {
 }
 __global__ void oc_prep_kernel(long n, const double* __restrict__ x, const double* __restrict__ dc,
                                const double* __restrict__ dv, double* __restrict__ B, double* __restrict__ lo,
-                               double* __restrict__ hi) {
+                               double* __restrict__ hi, double* __restrict__ scal) {
   const long e = blockIdx.x * 256L + threadIdx.x;
   if (e >= n) return;
-  const double move = 0.2, xe = x[e];
-  B[e] = xe * sqrt(-dc[e] / dv[e]);
+  const double move = 0.2, xe = x[e], dve = dv[e];
+  B[e] = xe * sqrt(-dc[e] / dve);
   lo[e] = fmax(0.0, xe - move);
   hi[e] = fmin(1.0, xe + move);
+  if (!(dve > 0.0)) scal[S_DVBAD] = 1.0;  // the first phase's search needs every dv > 0
 }
 
 // one bisection step: partial sums of dv*(xnew - x) at lmid = (l1 + l2)/2;
@@ -380,7 +386,7 @@ __global__ void oc_step_kernel(long n, const double* __restrict__ x, const doubl
                                const double* __restrict__ dv, const double* __restrict__ B,
                                const double* __restrict__ lo, const double* __restrict__ hi,
                                double* __restrict__ scal, double* __restrict__ partials) {
-  if (scal[S_OCDONE] != 0.0) return;
+  if (scal[S_OCDONE] != 0.0 || scal[S_TMP0] >= (double)kOcCap) return;
   const double lmid = 0.5 * (scal[S_L2] + scal[S_L1]);
   // 1/sqrt(lmid), formed once per step by the kernel that set l1 and l2 (FP64
   // division and square root are slow enough here to matter once per thread)
@@ -396,19 +402,21 @@ __global__ void oc_step_kernel(long n, const double* __restrict__ x, const doubl
 }
 
 // gt = sum + g (g in scal[S_G]); l1 or l2 <- lmid; done when (l2-l1)/(l1+l2) <= 1e-6
-__global__ void oc_finish_kernel(const double* __restrict__ partials, int nb, double* __restrict__ scal) {
-  if (scal[S_OCDONE] != 0.0) return;
-  const double g = scal[S_G];
+__device__ __forceinline__ double oc_gt(const double* __restrict__ partials, int nb, const double* scal) {
   __shared__ double sh[256];
   const int per = (nb + 255) / 256;
   const int b0 = threadIdx.x * per;
   double s = 0.0;
   for (int i = b0; i < b0 + per && i < nb; i++) s += partials[i];
-  const double t = fold256(s, false, sh);
+  return fold256(s, false, sh) + scal[S_G];
+}
+
+__global__ void oc_finish_kernel(const double* __restrict__ partials, int nb, double* __restrict__ scal) {
+  if (scal[S_OCDONE] != 0.0 || scal[S_TMP0] >= (double)kOcCap) return;
+  const double gt = oc_gt(partials, nb, scal);
   if (threadIdx.x == 0) {
     const double l1 = scal[S_L1], l2 = scal[S_L2];
     const double lmid = 0.5 * (l2 + l1);
-    const double gt = t + g;
     double nl1 = l1, nl2 = l2;
     if (gt > 0)
       nl1 = lmid;
@@ -422,6 +430,99 @@ __global__ void oc_finish_kernel(const double* __restrict__ partials, int nb, do
     scal[S_RL] = 1.0 / sqrt(0.5 * (nl2 + nl1));
     scal[S_TMP0] += 1.0;  // steps taken
   }
+}
+
+// The bisection's first phase, searched. From l1 = 0, l2 = 1e9 the bisection
+// halves l2 (step n tries lmid = 1e9 2^-n exactly: l2 + 0 and the halving do
+// not round) while gt(lmid) <= 0, and sets l1 at the first step n* with
+// gt > 0. With every dv > 0, gt as evaluated is a non-increasing function of
+// lmid: each xnew is a non-decreasing function of 1/sqrt(lmid) (rounding is
+// monotone, and a NaN term is NaN at every lmid), and the sum adds monotone
+// terms in a fixed order. So n* is found by a binary search over n in
+// ceil(log2(cap + 1)) probes of the same step kernel, each run with the l1,
+// l2 and 1/sqrt(lmid) that sequential step n would have, and the state after
+// step n* is set as the sequential steps leave it: the same decisions, the
+// same bits, in 8 passes over the elements instead of n* (~40 at
+// 256x128x128). A probe after the search has ended returns at once.
+constexpr int kOcProbes = 8;  // 2^8 > kOcCap + 1
+static_assert((1 << kOcProbes) > kOcCap + 1, "probes cover the first phase");
+
+__device__ __forceinline__ double oc_l2_before(int n) { return ldexp(1e9, -(n - 1)); }  // l2 before step n
+
+__global__ void oc_search_init_kernel(double* scal) {
+  // a dv that is not positive leaves the first phase to the sequential steps
+  scal[S_BLO] = 1.0;
+  scal[S_BHI] = scal[S_DVBAD] != 0.0 ? 1.0 : (double)(kOcCap + 1);
+}
+
+__global__ void oc_probe_set_kernel(double* scal) {
+  const int lo = (int)scal[S_BLO], hi = (int)scal[S_BHI];
+  if (lo >= hi) {
+    scal[S_OCDONE] = 1.0;  // the probe's step and finish return at once
+    return;
+  }
+  const int mid = (lo + hi) / 2;
+  const double l2 = oc_l2_before(mid);
+  scal[S_L1] = 0.0;
+  scal[S_L2] = l2;
+  scal[S_RL] = 1.0 / sqrt(0.5 * (l2 + 0.0));
+  scal[S_OCDONE] = 0.0;
+  scal[S_TMP0] = 0.0;
+  scal[S_TMP1] = (double)mid;
+}
+
+__global__ void oc_probe_finish_kernel(const double* __restrict__ partials, int nb, double* __restrict__ scal) {
+  if (scal[S_OCDONE] != 0.0) return;
+  const double gt = oc_gt(partials, nb, scal);
+  if (threadIdx.x == 0) {
+    const int mid = (int)scal[S_TMP1];
+    if (gt > 0)
+      scal[S_BHI] = (double)mid;
+    else
+      scal[S_BLO] = (double)(mid + 1);
+  }
+}
+
+// the state the sequential steps 1 .. n* leave (or, with no n* within the
+// cap, steps 1 .. cap); with the search skipped, the state before step 1
+__global__ void oc_search_done_kernel(double* scal) {
+  if (scal[S_DVBAD] != 0.0) {
+    scal[S_L1] = 0.0;
+    scal[S_L2] = 1e9;
+    scal[S_OCDONE] = ((1e9 - 0.0) / (0.0 + 1e9) > 1e-6) ? 0.0 : 1.0;
+    scal[S_TMP0] = 0.0;
+    scal[S_LMID] = 0.0;
+    scal[S_RL] = 1.0 / sqrt(0.5 * (1e9 + 0.0));
+    return;
+  }
+  const int n = (int)scal[S_BLO];  // == hi
+  double nl1, nl2;
+  if (n > kOcCap) {  // cap halvings, no root bracketed
+    nl1 = 0.0;
+    nl2 = oc_l2_before(kOcCap + 1);
+    scal[S_TMP0] = (double)kOcCap;
+  } else {
+    nl1 = oc_l2_before(n + 1);  // lmid of step n
+    nl2 = oc_l2_before(n);
+    scal[S_TMP0] = (double)n;
+  }
+  scal[S_LMID] = n > kOcCap ? nl2 : nl1;
+  scal[S_L1] = nl1;
+  scal[S_L2] = nl2;
+  scal[S_OCDONE] = ((nl2 - nl1) / (nl1 + nl2) > 1e-6) ? 0.0 : 1.0;
+  scal[S_RL] = 1.0 / sqrt(0.5 * (nl2 + nl1));
+}
+
+// the search, enqueued: 3 + 2 kOcProbes small launches and kOcProbes passes
+static void oc_search_enqueue(tp_ctx* c, long ne, int nb, const double* x, const double* dc, const double* dv,
+                              const double* B, const double* lo, const double* hi) {
+  oc_search_init_kernel<<<1, 1, 0, c->s>>>(c->d_scal);
+  for (int q = 0; q < kOcProbes; q++) {
+    oc_probe_set_kernel<<<1, 1, 0, c->s>>>(c->d_scal);
+    oc_step_kernel<<<nb, 256, 0, c->s>>>(ne, x, dc, dv, B, lo, hi, c->d_scal, c->d_red);
+    oc_probe_finish_kernel<<<1, 256, 0, c->s>>>(c->d_red, nb, c->d_scal);
+  }
+  oc_search_done_kernel<<<1, 1, 0, c->s>>>(c->d_scal);
 }
 
 // final pass at the last lmid: xnew, max |x - xnew| partials, x <- xnew
@@ -457,6 +558,7 @@ __global__ void oc_cond_kernel(const double* scal, cudaGraphConditionalHandle h,
 }
 
 __global__ void oc_init_kernel(double* scal) {
+  scal[S_DVBAD] = 0.0;
   scal[S_L1] = 0.0;
   scal[S_L2] = 1e9;
   scal[S_OCDONE] = ((1e9 - 0.0) / (0.0 + 1e9) > 1e-6) ? 0.0 : 1.0;
@@ -492,23 +594,23 @@ int oc_bisect(tp_ctx* c, long ne, double* x, double* xnew, const double* dc, con
   }
   if (c->d_ocb && ne <= c->ocb_n) {
     double* b = c->d_ocb;
-    oc_prep_kernel<<<grid_for(ne, 256), 256, 0, c->s>>>(ne, x, dc, dv, b, b + ne, b + 2 * ne);
+    oc_prep_kernel<<<grid_for(ne, 256), 256, 0, c->s>>>(ne, x, dc, dv, b, b + ne, b + 2 * ne, c->d_scal);
     B = b;
     lo = b + ne;
     hi = b + 2 * ne;
+    oc_search_enqueue(c, ne, nb, x, dc, dv, B, lo, hi);
   }
-  const int kBatch = 24, kMaxSteps = 240;
-  int taken = 0;
+  const int kBatch = 24;
   for (;;) {
     for (int q = 0; q < kBatch; q++) {
       oc_step_kernel<<<nb, 256, 0, c->s>>>(ne, x, dc, dv, B, lo, hi, c->d_scal, c->d_red);
       oc_finish_kernel<<<1, 256, 0, c->s>>>(c->d_red, nb, c->d_scal);
     }
-    taken += kBatch;
-    cudaMemcpyAsync(c->h_scal + S_OCDONE, c->d_scal + S_OCDONE, sizeof(double), cudaMemcpyDeviceToHost, c->s);
+    // S_OCDONE and S_TMP0 (steps taken) are adjacent
+    cudaMemcpyAsync(c->h_scal + S_OCDONE, c->d_scal + S_OCDONE, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->s);
     cudaStreamSynchronize(c->s);
     if (c->h_scal[S_OCDONE] != 0.0) break;
-    if (taken >= kMaxSteps) return -1;
+    if (c->h_scal[S_TMP0] >= (double)kOcCap) return -1;
   }
   oc_apply_kernel<<<nb, 256, 0, c->s>>>(ne, x, xnew, dc, dv, c->d_scal, c->d_red, commit ? 1 : 0);
   finish_sum(c, nb, S_CHANGE, 1);
@@ -532,7 +634,7 @@ void constraint_from_volume(tp_ctx* c) {
 // the interval is narrow enough return at once) and the condition kernel.
 // It takes the same steps as oc_bisect, with no host check between them; the
 // cap is the same 240 steps.
-constexpr int kOcBody = 8, kOcMaxSteps = 240;
+constexpr int kOcBody = 8;
 
 void oc_graph_free(tp_ctx* c) {
   if (c->oc_exec) cudaGraphExecDestroy(c->oc_exec);
@@ -565,7 +667,7 @@ static bool oc_graph_build(tp_ctx* c) {
                                              c->d_red);
         oc_finish_kernel<<<1, 256, 0, c->s>>>(c->d_red, nb, c->d_scal);
       }
-      oc_cond_kernel<<<1, 1, 0, c->s>>>(c->d_scal, h, kOcMaxSteps);
+      oc_cond_kernel<<<1, 1, 0, c->s>>>(c->d_scal, h, kOcCap);
       cudaGraph_t out = nullptr;
       ok = cudaStreamEndCapture(c->s, &out) == cudaSuccess;
     }
@@ -587,7 +689,9 @@ bool oc_update_graph(tp_ctx* c) {
   const int nb = blocks_for(ne);
   double* b = c->d_ocb;
   oc_init_kernel<<<1, 1, 0, c->s>>>(c->d_scal);
-  oc_prep_kernel<<<grid_for(ne, 256), 256, 0, c->s>>>(ne, c->d_x, c->d_dc, c->d_dv, b, b + ne, b + 2 * ne);
+  oc_prep_kernel<<<grid_for(ne, 256), 256, 0, c->s>>>(ne, c->d_x, c->d_dc, c->d_dv, b, b + ne, b + 2 * ne,
+                                                      c->d_scal);
+  oc_search_enqueue(c, ne, nb, c->d_x, c->d_dc, c->d_dv, b, b + ne, b + 2 * ne);
   cudaGraphLaunch(c->oc_exec, c->s);
   oc_apply_kernel<<<nb, 256, 0, c->s>>>(ne, c->d_x, c->d_xnew, c->d_dc, c->d_dv, c->d_scal, c->d_red, 1);
   finish_sum(c, nb, S_CHANGE, 1);

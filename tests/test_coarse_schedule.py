@@ -225,7 +225,7 @@ def ps_row_of(b, rl, G):
 @pytest.mark.parametrize("grid", list(GRIDS), ids=list(GRIDS))
 def test_coarse_solve_phases(grid):
     n, bw = GRIDS[grid]
-    nbs = min(512, (n + 31) // 32 * 32)
+    nbs = min(min(768, max(512, 4 * NSM // 32 * 32)), (n + 31) // 32 * 32)  # coarse_alloc: 4 rows per SM
     nblk = (n + nbs - 1) // nbs
     R = 1
     while R < 8 and (nbs + R - 1) // R > NSM:

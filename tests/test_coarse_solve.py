@@ -1,6 +1,7 @@
 """The coarsest-level direct solve on grids whose coarsest level spans many
-512-row blocks, one of them with a half bandwidth wider than a block (the
-forward sweep then reads the solution of the two previous blocks).
+solve blocks (608 rows on 152 SMs: 4 per SM), one of them with a half
+bandwidth wider than a block (the forward sweep then reads the solution of
+the two previous blocks).
 
 The single cooperative launch (both triangular sweeps, grid barriers between
 the block steps) is checked against the two-launch block solve, against the
@@ -17,7 +18,7 @@ import topopt_gb300 as tp
 pytestmark = pytest.mark.gpu
 
 # (shape, levels): coarsest 16x8x8 elements (n = 4131, half bandwidth 275,
-# 9 blocks) and 16x16x16 elements (n = 14739, half bandwidth 923, 29 blocks)
+# 7 blocks of 608) and 16x16x16 elements (n = 14739, half bandwidth 923, 25)
 CASES = [((64, 32, 32), 3), ((64, 64, 64), 3)]
 
 

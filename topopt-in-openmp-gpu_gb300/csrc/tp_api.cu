@@ -261,11 +261,13 @@ static tp_status assemble(tp_ctx* c) {
   return assemble_status(c, *c->h_info);
 }
 
-// PCG set-up: r = b - K u, |b|^2 per column, converged marks cleared
+// PCG set-up: r = b - K u, |b|^2 per column, converged marks cleared; the
+// mixed form's first V-cycle input (float) r
 void pcg_prologue(tp_ctx* c, const double* b, const double* u, int nr) {
   const long n = c->L[0].ndof;
   int nb = 0;
   fine_resid<double>(c, c->d_E, b, u, c->d_r, nr);
+  if (mixed(c)) cast_d2f(c, n * nr, c->d_r, c->mgf_r[0]);
   dot_partials(c, n, b, b, &nb, nr);
   finish_sum(c, nb, S_BNORM2, 0, nr);
   cg_reset(c, nr);
@@ -273,18 +275,31 @@ void pcg_prologue(tp_ctx* c, const double* b, const double* u, int nr) {
 
 // One PCG iteration over nr columns. iter >= 0 is the host's iteration
 // index; iter = -1 takes it from the device counter (the captured loop).
+// The mixed form's V-cycle reads r as the float copy that the prologue and
+// the last r update wrote, and the dot and the p update read its float
+// output directly (widened exactly), so neither cast pass runs here.
 void pcg_iteration(tp_ctx* c, double* u, int iter, int nr) {
   const long n = c->L[0].ndof;
   double *r = c->d_r, *z = c->d_z, *p = c->d_p, *q = c->d_q;
   int nb = 0;
-  precondition(c, r, z, nr);
-  dot_partials(c, n, r, z, &nb, nr);
-  finish_sum(c, nb, S_RHO, 0, nr);
-  if (iter != 0) cg_scalars(c, 0, nr);
-  cg_pupdate(c, n, z, p, iter < 0 ? -1 : (iter == 0), nr);
+  const int first = iter < 0 ? -1 : (iter == 0);
+  if (mixed(c)) {
+    MG<float> m = mg_float(c);
+    vcycle<float>(c, m, 0, nr);
+    dot_partials(c, n, r, (const float*)m.z[0], &nb, nr);
+    finish_sum(c, nb, S_RHO, 0, nr);
+    if (iter != 0) cg_scalars(c, 0, nr);
+    cg_pupdate(c, n, (const float*)m.z[0], p, first, nr);
+  } else {
+    precondition(c, r, z, nr);
+    dot_partials(c, n, r, (const double*)z, &nb, nr);
+    finish_sum(c, nb, S_RHO, 0, nr);
+    if (iter != 0) cg_scalars(c, 0, nr);
+    cg_pupdate(c, n, (const double*)z, p, first, nr);
+  }
   finish_sum(c, fine_apply_dot<double>(c, c->d_E, p, q, nr), S_DPR, 0, nr);
   cg_scalars(c, 1, nr);
-  cg_xr_update(c, n, u, r, p, q, &nb, nr);
+  cg_xr_update(c, n, u, r, p, q, &nb, nr, mixed(c) ? c->mgf_r[0] : nullptr);
   finish_sum(c, nb, S_RNORM2, 0, nr);
   cg_scalars(c, 2, nr, c->p.cgtol, iter);
 }

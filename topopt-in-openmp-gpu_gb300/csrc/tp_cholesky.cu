@@ -38,7 +38,8 @@
 namespace tp {
 
 constexpr int NB = 32;    // factor panel width
-constexpr int NBS = 512;  // solve block size (largest)
+constexpr int NBS = 512;      // solve block size: at least this, or 4 rows per SM (608 on 152 SMs)
+constexpr int kNbsMax = 768;  // the block inverses' staged rows fit the shared memory
 constexpr long kBarrierSpin = 1L << 22;  // polls of a flag or barrier counter in global memory (about a second)
 
 __host__ __device__ __forceinline__ long lmax(long a, long b) { return a > b ? a : b; }
@@ -121,7 +122,15 @@ void coarse_alloc(tp_ctx* c) {
   if (C.bw > C.n - 1) C.bw = std::max(1L, C.n - 1);
   C.band_elems = (size_t)C.n * (C.bw + 1) + 1;
   dev_malloc(&C.band, C.band_elems * sizeof(double));
-  C.nbs = (int)std::min((long)NBS, ((C.n + 31) / 32) * 32);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&C.nsm, cudaDevAttrMultiProcessorCount, dev);
+  // Solve blocks of 4 rows per SM: the single-launch solve's plan then gives
+  // every SM a CTA of 4 rows in each phase (512-row blocks left 24 of 152 SMs
+  // idle), and fewer blocks mean fewer phases (186 instead of 222 at
+  // 256x128x128), for 19% more block-inverse work in the factorisation.
+  const long nbs_sm = std::min((long)kNbsMax, std::max((long)NBS, (4L * C.nsm) / 32 * 32));
+  C.nbs = (int)std::min(nbs_sm, ((C.n + 31) / 32) * 32);
   C.nblk = (int)((C.n + C.nbs - 1) / C.nbs);
   const size_t dsz = (size_t)C.nblk * C.nbs * C.nbs;
   const size_t lsz = (size_t)C.nblk * C.nbs * C.bw;
@@ -138,9 +147,6 @@ void coarse_alloc(tp_ctx* c) {
   int lo = 0, hi = 0;
   cudaDeviceGetStreamPriorityRange(&lo, &hi);
   C.prio_high = hi;
-  int dev = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&C.nsm, cudaDevAttrMultiProcessorCount, dev);
   cudaEventCreateWithFlags(&C.ev_panel, cudaEventDisableTiming);
   cudaEventCreateWithFlags(&C.ev_rest, cudaEventDisableTiming);
   c->mem_bytes += (long)(C.band_elems + 2 * dsz + lsz + C.n * 18) * 8;

@@ -308,7 +308,8 @@ template <typename T> void prolong_set(tp_ctx* c, int l, const T* coarse, T* fin
 
 // vectors
 template <typename T> void vscale(tp_ctx* c, long n, const T* a, const T* b, T* out, T omega, int nr = 1);  // out = omega*a*b
-void dot_partials(tp_ctx* c, long n, const double* a, const double* b, int* nblocks, int nr = 1);
+template <typename TB>
+void dot_partials(tp_ctx* c, long n, const double* a, const TB* b, int* nblocks, int nr = 1);
 #ifdef __CUDACC__
 // The 256 values of a block (one per thread) folded in a fixed tree --
 // pairs (i, i + 128), then (i, i + 64), (i, i + 32), then a warp's shuffles
@@ -341,8 +342,10 @@ __device__ __forceinline__ double fold256(double v, bool is_max, double* sh) {
 void finish_sum(tp_ctx* c, int nblocks, int slot, int op, int nr = 1);  // column r: partials -> d_scal[r*S_COUNT + slot]
 void cast_d2f(tp_ctx* c, long n, const double* a, float* b);
 void cast_f2d(tp_ctx* c, long n, const float* a, double* b);
-void cg_pupdate(tp_ctx* c, long n, const double* z, double* p, int first, int nr = 1);
-void cg_xr_update(tp_ctx* c, long n, double* u, double* r, const double* p, const double* q, int* nblocks, int nr = 1);
+template <typename TZ>
+void cg_pupdate(tp_ctx* c, long n, const TZ* z, double* p, int first, int nr = 1);
+void cg_xr_update(tp_ctx* c, long n, double* u, double* r, const double* p, const double* q, int* nblocks, int nr = 1,
+                  float* rf = nullptr);
 void cg_scalars(tp_ctx* c, int what, int nr = 1, double tol = 0.0, int iter = 0);
 void cg_reset(tp_ctx* c, int nr);
 

@@ -47,23 +47,29 @@ static int dot_blocks(long n) {
   return nb;
 }
 
-// grid-stride dot per column with a fixed number of blocks -> partials[r * gridDim.x + block]
-__global__ void dot_kernel(long n, const double* __restrict__ a, const double* __restrict__ b,
+// grid-stride dot per column with a fixed number of blocks -> partials[r * gridDim.x + block];
+// b may be FP32 (the mixed V-cycle's output, widened exactly)
+template <typename TB>
+__global__ void dot_kernel(long n, const double* __restrict__ a, const TB* __restrict__ b,
                            double* __restrict__ partials) {
   const long off = (long)blockIdx.y * n;
   double s = 0.0;
-  for (long i = blockIdx.x * 256L + threadIdx.x; i < n; i += (long)gridDim.x * 256) s += a[off + i] * b[off + i];
+  for (long i = blockIdx.x * 256L + threadIdx.x; i < n; i += (long)gridDim.x * 256)
+    s += a[off + i] * (double)b[off + i];
   s = block_sum256(s);
   if (threadIdx.x == 0) partials[(long)blockIdx.y * gridDim.x + blockIdx.x] = s;
 }
 
-void dot_partials(tp_ctx* c, long n, const double* a, const double* b, int* nblocks, int nr) {
+template <typename TB>
+void dot_partials(tp_ctx* c, long n, const double* a, const TB* b, int* nblocks, int nr) {
   ProfScope ps(c, P_VECTOR);
   const int nb = dot_blocks(n);
-  dot_kernel<<<dim3(nb, nr), 256, 0, c->s>>>(n, a, b, c->d_red);
+  dot_kernel<TB><<<dim3(nb, nr), 256, 0, c->s>>>(n, a, b, c->d_red);
   TP_CHECK_LAUNCH(c, "dot");
   *nblocks = nb;
 }
+template void dot_partials<double>(tp_ctx*, long, const double*, const double*, int*, int);
+template void dot_partials<float>(tp_ctx*, long, const double*, const float*, int*, int);
 
 // op 0: sum; op 1: max. Column r (blockIdx.x) folds partials[r*nb .. r*nb + nb)
 // into out[r * S_COUNT].
@@ -120,26 +126,33 @@ template void vscale<double>(tp_ctx*, long, const double*, const double*, double
 template void vscale<float>(tp_ctx*, long, const float*, const float*, float*, float, int);
 
 // p = z (first iteration) or p = beta*p + z, beta of the column from the
-// device; first = -1: the first iteration is the device counter's zero
-__global__ void pupdate_kernel(long n, const double* __restrict__ z, double* __restrict__ p,
+// device; first = -1: the first iteration is the device counter's zero. z
+// may be FP32 (the mixed V-cycle's output, widened exactly).
+template <typename TZ>
+__global__ void pupdate_kernel(long n, const TZ* __restrict__ z, double* __restrict__ p,
                                const double* __restrict__ scal, int first) {
   const long i = blockIdx.x * 256L + threadIdx.x;
   if (i >= n) return;
   const long o = (long)blockIdx.y * n;  // column
   if (first < 0) first = scal[S_IT] == 0.0;
+  const double zi = (double)z[o + i];
   if (first)
-    p[o + i] = z[o + i];
+    p[o + i] = zi;
   else
-    p[o + i] = scal[blockIdx.y * S_COUNT + S_BETA] * p[o + i] + z[o + i];
+    p[o + i] = scal[blockIdx.y * S_COUNT + S_BETA] * p[o + i] + zi;
 }
-void cg_pupdate(tp_ctx* c, long n, const double* z, double* p, int first, int nr) {
+template <typename TZ>
+void cg_pupdate(tp_ctx* c, long n, const TZ* z, double* p, int first, int nr) {
   ProfScope ps(c, P_VECTOR);
-  pupdate_kernel<<<dim3(grid_for(n, 256), nr), 256, 0, c->s>>>(n, z, p, c->d_scal, first);
+  pupdate_kernel<TZ><<<dim3(grid_for(n, 256), nr), 256, 0, c->s>>>(n, z, p, c->d_scal, first);
   TP_CHECK_LAUNCH(c, "cg_pupdate");
 }
+template void cg_pupdate<double>(tp_ctx*, long, const double*, double*, int, int);
+template void cg_pupdate<float>(tp_ctx*, long, const float*, double*, int, int);
 
-// u += alpha p ; r -= alpha q ; partials of <r, r>, per column
-__global__ void xr_kernel(long n, double* __restrict__ u, double* __restrict__ r,
+// u += alpha p ; r -= alpha q ; partials of <r, r>, per column; with rf, also
+// rf = (float) r, the next mixed V-cycle's input (the cast it would start with)
+__global__ void xr_kernel(long n, double* __restrict__ u, double* __restrict__ r, float* __restrict__ rf,
                           const double* __restrict__ p, const double* __restrict__ q,
                           const double* __restrict__ scal, double* __restrict__ partials) {
   const long off = (long)blockIdx.y * n;
@@ -149,15 +162,17 @@ __global__ void xr_kernel(long n, double* __restrict__ u, double* __restrict__ r
     u[i] += alpha * p[i];
     const double ri = r[i] - alpha * q[i];
     r[i] = ri;
+    if (rf) rf[i] = (float)ri;
     s += ri * ri;
   }
   s = block_sum256(s);
   if (threadIdx.x == 0) partials[(long)blockIdx.y * gridDim.x + blockIdx.x] = s;
 }
-void cg_xr_update(tp_ctx* c, long n, double* u, double* r, const double* p, const double* q, int* nblocks, int nr) {
+void cg_xr_update(tp_ctx* c, long n, double* u, double* r, const double* p, const double* q, int* nblocks, int nr,
+                  float* rf) {
   ProfScope ps(c, P_VECTOR);
   const int nb = dot_blocks(n);
-  xr_kernel<<<dim3(nb, nr), 256, 0, c->s>>>(n, u, r, p, q, c->d_scal, c->d_red);
+  xr_kernel<<<dim3(nb, nr), 256, 0, c->s>>>(n, u, r, rf, p, q, c->d_scal, c->d_red);
   TP_CHECK_LAUNCH(c, "cg_xr_update");
   *nblocks = nb;
 }

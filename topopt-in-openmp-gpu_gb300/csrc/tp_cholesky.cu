@@ -1249,11 +1249,15 @@ __global__ void __launch_bounds__(256) pf_kernel(PfArgs a) {
   }
 }
 
-// Inverse of each diagonal NBSxNBS block of L, one CTA per (block, 32-column
+// Inverse of each diagonal nbs x nbs block of L, one CTA per (block, 32-column
 // chunk): the chunk's columns X of L_bb^{-1} are found by blocked forward
 // substitution over 32-row chunks R,
 //   acc = E_R - sum_{S<R} L_RS X_S,    X_R = L_RR^{-1} acc (substitution),
 // with X kept in shared memory. Writes D (row-major) and D^T (row-major).
+// The tiles L_RS of a row chunk are loaded into registers one tile ahead, so
+// a tile's product does not wait on its load. blockIdx.x is the block and
+// blockIdx.y the chunk: CTAs go out chunk by chunk, the heaviest (chunk 0,
+// nR(nR-1)/2 tile products) first, so the last wave holds the lightest.
 constexpr int kDinvThreads = 256;
 
 template <typename V>
@@ -1264,7 +1268,7 @@ __global__ void __launch_bounds__(kDinvThreads)
   V* X = reinterpret_cast<V*>(smem_d);  // nbs x 33
   V* Lt = X + (long)nbs * 33;           // 32 x 33
   V* Acc = Lt + 32 * 33;                // the chunk's 32 reciprocal pivots
-  const int blk = blockIdx.y, cc = blockIdx.x, tid = threadIdx.x;
+  const int blk = blockIdx.x, cc = blockIdx.y, tid = threadIdx.x;
   const long b0 = (long)blk * nbs;
   const int s = (int)lmin((long)nbs, n - b0);
   const int j0 = cc * 32;
@@ -1276,13 +1280,25 @@ __global__ void __launch_bounds__(kDinvThreads)
     V acc[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) acc[q] = V((R == cc && a == q0 + q) ? 1.0f : 0.0f);
-    for (int S = cc; S < R; S++) {
-      for (int idx = tid; idx < 1024; idx += kDinvThreads) {
-        const int ra = idx & 31, cs = idx >> 5;
+    // tile L_RS, element idx = tid + 256 m at (ra, cs) = (idx & 31, idx >> 5)
+    auto load_tile = [&](int S, double* v) {
+#pragma unroll
+      for (int m = 0; m < 4; m++) {
+        const int idx = tid + kDinvThreads * m, ra = idx & 31, cs = idx >> 5;
         const long r = b0 + R * 32 + ra, col = b0 + S * 32 + cs;
-        Lt[ra * 33 + cs] = ds_in<V>((R * 32 + ra < s) ? bget(B, bw, r, col) : 0.0);
+        v[m] = (R * 32 + ra < s) ? bget(B, bw, r, col) : 0.0;
+      }
+    };
+    double nxt[4];
+    if (cc < R) load_tile(cc, nxt);
+    for (int S = cc; S < R; S++) {
+#pragma unroll
+      for (int m = 0; m < 4; m++) {
+        const int idx = tid + kDinvThreads * m;
+        Lt[(idx & 31) * 33 + (idx >> 5)] = ds_in<V>(nxt[m]);
       }
       __syncthreads();
+      if (S + 1 < R) load_tile(S + 1, nxt);  // in flight during this tile's product
 #pragma unroll 4
       for (int t = 0; t < 32; t++) {
         const V l = Lt[a * 33 + t];
@@ -1476,7 +1492,7 @@ static void coarse_factor_launches(tp_ctx* c, size_t dinv_smem) {
     pf_launch(c);
   else
     step_launches(c);
-  (C.ds ? dinv_kernel<Dsf> : dinv_kernel<double>)<<<dim3(C.nbs / 32, C.nblk), kDinvThreads, dinv_smem, c->s>>>(
+  (C.ds ? dinv_kernel<Dsf> : dinv_kernel<double>)<<<dim3(C.nblk, C.nbs / 32), kDinvThreads, dinv_smem, c->s>>>(
       C.band, C.bw, C.n, C.nbs, C.dinv, C.dinvT);
   lrow_kernel<<<dim3((unsigned)((C.bw + 31) / 32), C.nbs / 32, C.nblk), dim3(32, 8), 0, c->s>>>(C.band, C.bw, C.n,
                                                                                                C.nbs, C.lrow);

@@ -95,6 +95,10 @@ long tp_ndof(const tp_ctx* c, int level);   /* 3 * nodes of level */
 long tp_nelem(const tp_ctx* c);             /* fine elements */
 long tp_device_bytes(const tp_ctx* c);      /* device memory the context holds */
 double* tp_field_ptr(tp_ctx* c, tp_field f); /* device pointer to a context field */
+/* The caller has written field f through tp_field_ptr (with its own copies,
+ * finished before this call): what tp_upload would do after its copy. For
+ * TP_FIELD_XPHYS the assembled operators are marked stale. */
+tp_status tp_field_written(tp_ctx* c, tp_field f);
 
 /* Host <-> device copies of context fields (count = elements of the field). */
 tp_status tp_upload(tp_ctx* c, tp_field f, const double* host, long count);

@@ -592,16 +592,22 @@ static long field_count(const tp_ctx* c, tp_field f) {
   return tp_nelem(c);
 }
 
+tp_status tp_field_written(tp_ctx* c, tp_field f) {
+  if (!c || !tp_field_ptr(c, f)) return TP_ERR_ARG;
+  if (f == TP_FIELD_XPHYS) {
+    c->assembled = false;
+    for (int l = 0; l < TP_MAXL; l++) c->st_sub_valid[l] = false;
+  }
+  return TP_OK;
+}
+
 tp_status tp_upload(tp_ctx* c, tp_field f, const double* host, long count) {
   if (!c || !host || count != field_count(c, f)) return TP_ERR_ARG;
   double* d = tp_field_ptr(c, f);
   if (!d) return TP_ERR_ARG;
   if (!cuda_ok(c, cudaMemcpyAsync(d, host, sizeof(double) * count, cudaMemcpyHostToDevice, c->s), "upload"))
     return TP_ERR_CUDA;
-  if (f == TP_FIELD_XPHYS) {
-    c->assembled = false;
-    for (int l = 0; l < TP_MAXL; l++) c->st_sub_valid[l] = false;
-  }
+  tp_field_written(c, f);
   return sync_check(c);
 }
 

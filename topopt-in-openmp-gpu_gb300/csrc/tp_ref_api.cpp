@@ -9,11 +9,13 @@
 #include <cuda_runtime.h>
 #include <omp.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <stdexcept>
 #include <mutex>
 #include <utility>
 #include <tuple>
@@ -284,10 +286,181 @@ HVec down(const double* d, size_t n) {
   return h;
 }
 
+// -- pipelined transfers -------------------------------------------------------
+// A transfer of an array of lines (len doubles each, line l at l * len in the
+// canonical layout) in chunks of whole lines through two page-locked buffers,
+// on a stream of its own: the host converts chunk j + 1 (its lines shared out
+// over the host threads) while chunk j is on the link, so conversion and copy
+// overlap instead of adding up. Each call returns after its last chunk has
+// landed (uploads) or been converted (downloads), so the device buffer is
+// ready for the context's stream and the host array for the caller.
+struct Pipe {
+  static constexpr long kChunk = 1L << 20;  // doubles per buffer
+  double* buf[2] = {nullptr, nullptr};
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaStream_t st = nullptr;
+  std::mutex mu;
+  bool ready() {
+    if (st) return true;
+    for (int b = 0; b < 2; b++) {
+      buf[b] = static_cast<double*>(pinned_cache().get(kChunk * sizeof(double)));
+      if (cudaEventCreateWithFlags(&ev[b], cudaEventDisableTiming) != cudaSuccess) return false;
+    }
+    return cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
+  }
+};
+Pipe& pipe() {
+  static Pipe* p = new Pipe();  // kept until exit, like the staging cache
+  return *p;
+}
+
+// fill(l, dst): canonical line l into dst[0 .. len); n: the array's doubles
+// (the last line may be short)
+template <typename Fill>
+void up_lines(double* d, long n, long len, Fill fill) {
+  Pipe& P = pipe();
+  std::lock_guard<std::mutex> lock(P.mu);
+  if (!P.ready()) throw std::runtime_error("pipelined transfer: no stream");
+  const long nlines = (n + len - 1) / len, per = std::max(1L, Pipe::kChunk / len);
+  long j = 0;
+  for (long l0 = 0; l0 < nlines; l0 += per, j++) {
+    const long l1 = std::min(nlines, l0 + per);
+    const int b = (int)(j & 1);
+    if (j >= 2) cudaEventSynchronize(P.ev[b]);  // the copy that last read this buffer
+    double* dst = P.buf[b];
+#pragma omp parallel for schedule(static)
+    for (long l = l0; l < l1; l++) fill(l, dst + (l - l0) * len);
+    const long lo = l0 * len, hi = std::min(n, l1 * len);
+    cudaMemcpyAsync(d + lo, dst, (hi - lo) * sizeof(double), cudaMemcpyHostToDevice, P.st);
+    cudaEventRecord(P.ev[b], P.st);
+  }
+  cudaStreamSynchronize(P.st);
+  g_h2d += n * (long)sizeof(double);
+}
+
+// drain(l, src): canonical line l from src[0 .. len) into the caller's array
+template <typename Drain>
+void down_lines(const double* d, long n, long len, Drain drain) {
+  Pipe& P = pipe();
+  std::lock_guard<std::mutex> lock(P.mu);
+  if (!P.ready()) throw std::runtime_error("pipelined transfer: no stream");
+  const long nlines = (n + len - 1) / len, per = std::max(1L, Pipe::kChunk / len);
+  auto issue = [&](long j) {
+    const long l0 = j * per, l1 = std::min(nlines, l0 + per);
+    const long lo = l0 * len, hi = std::min(n, l1 * len);
+    cudaMemcpyAsync(P.buf[j & 1], d + lo, (hi - lo) * sizeof(double), cudaMemcpyDeviceToHost, P.st);
+    cudaEventRecord(P.ev[j & 1], P.st);
+  };
+  const long nchunks = (nlines + per - 1) / per;
+  if (nchunks > 0) issue(0);
+  for (long j = 0; j < nchunks; j++) {
+    if (j + 1 < nchunks) issue(j + 1);  // its buffer was drained at step j - 1
+    cudaEventSynchronize(P.ev[j & 1]);
+    const long l0 = j * per, l1 = std::min(nlines, l0 + per);
+    const double* src = P.buf[j & 1];
+#pragma omp parallel for schedule(static)
+    for (long l = l0; l < l1; l++) drain(l, src + (l - l0) * len);
+  }
+  g_d2h += n * (long)sizeof(double);
+}
+
+// The padded host layouts hold the canonical lines (len values) as a regular
+// box: line (i, k) at base + i si + k sk, si a multiple of sk. Double arrays
+// cross in one strided copy between the caller's array and the device (the
+// copy engines read pageable memory over the host link at ~85-185 GB/s on
+// this part, several times a host-side conversion into staging; the halo is
+// neither read nor written); float arrays (the float flavour) take the
+// pipelined conversion above.
+bool copy_box(double* dev, double* host, long len, long nk, long ni, long sk, long si, bool up) {
+  cudaMemcpy3DParms p = {};
+  const cudaPitchedPtr hp = make_cudaPitchedPtr(host, sk * sizeof(double), sk, si / sk);
+  const cudaPitchedPtr dp = make_cudaPitchedPtr(dev, len * sizeof(double), len, nk);
+  p.srcPtr = up ? hp : dp;
+  p.dstPtr = up ? dp : hp;
+  p.extent = make_cudaExtent(len * sizeof(double), nk, ni);
+  p.kind = up ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+  if (cudaMemcpy3D(&p) != cudaSuccess) return false;
+  (up ? g_h2d : g_d2h) += len * nk * ni * (long)sizeof(double);
+  return true;
+}
+
+// the line shapes of the three layouts: a level's nodal vector (a y line of
+// nodes, 3 (ey + 1) values, per (x, z)), the fine elements (a y line of ey per
+// (x, z)), and a plain array of n values (lines of kPlain)
+constexpr long kPlain = 4096;
+template <typename T>
+void up_nodes(double* d, const Dims& dm, const T* v) {
+  const long len = 3L * (dm.ey + 1), nz = dm.ez + 1;
+  if constexpr (sizeof(T) == sizeof(double)) {
+    if (copy_box(d, (double*)(v + 3 * pnode(dm, 0, 0, 0)), len, nz, dm.ex + 1, 3L * dm.wy, 3L * dm.wy * dm.wz, true))
+      return;
+    cudaGetLastError();
+  }
+  up_lines(d, len * (dm.ex + 1) * nz, len, [&](long l, double* dst) {
+    line_copy(dst, v + 3 * pnode(dm, (int)(l / nz), (int)(l % nz), 0), len);
+  });
+}
+template <typename T>
+void down_nodes(const double* d, const Dims& dm, T* v) {
+  const long len = 3L * (dm.ey + 1), nz = dm.ez + 1;
+  if constexpr (sizeof(T) == sizeof(double)) {
+    if (copy_box((double*)d, (double*)(v + 3 * pnode(dm, 0, 0, 0)), len, nz, dm.ex + 1, 3L * dm.wy,
+                 3L * dm.wy * dm.wz, false))
+      return;
+    cudaGetLastError();
+  }
+  down_lines(d, len * (dm.ex + 1) * nz, len, [&](long l, const double* src) {
+    line_copy_out(v + 3 * pnode(dm, (int)(l / nz), (int)(l % nz), 0), src, len);
+  });
+}
+void up_elems(double* d, const gridContext& gc, const DTYPE* x) {
+  const long ey = gc.nely, ez = gc.nelz, wy = gc.wrapy - 1, wz = gc.wrapz - 1;
+  if constexpr (sizeof(DTYPE) == sizeof(double)) {
+    if (copy_box(d, (double*)(x + wy * wz + wy + 1), ey, ez, gc.nelx, wy, wy * wz, true)) return;
+    cudaGetLastError();
+  }
+  up_lines(d, (long)gc.nelx * ez * ey, ey, [&](long l, double* dst) {
+    line_copy(dst, x + (l / ez + 1) * wy * wz + (l % ez + 1) * wy + 1, ey);
+  });
+}
+void down_elems(const double* d, const gridContext& gc, DTYPE* x) {
+  const long ey = gc.nely, ez = gc.nelz, wy = gc.wrapy - 1, wz = gc.wrapz - 1;
+  if constexpr (sizeof(DTYPE) == sizeof(double)) {
+    if (copy_box((double*)d, (double*)(x + wy * wz + wy + 1), ey, ez, gc.nelx, wy, wy * wz, false)) return;
+    cudaGetLastError();
+  }
+  down_lines(d, (long)gc.nelx * ez * ey, ey, [&](long l, const double* src) {
+    line_copy_out(x + (l / ez + 1) * wy * wz + (l % ez + 1) * wy + 1, src, ey);
+  });
+}
+template <typename T>
+void up_plain(double* d, const T* x, long n) {
+  if constexpr (sizeof(T) == sizeof(double)) {
+    if (cudaMemcpy(d, x, n * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess) {
+      g_h2d += n * (long)sizeof(double);
+      return;
+    }
+    cudaGetLastError();
+  }
+  up_lines(d, n, kPlain, [&](long l, double* dst) { line_copy(dst, x + l * kPlain, std::min(kPlain, n - l * kPlain)); });
+}
+template <typename T>
+void down_plain(const double* d, T* x, long n) {
+  if constexpr (sizeof(T) == sizeof(double)) {
+    if (cudaMemcpy(x, d, n * sizeof(double), cudaMemcpyDeviceToHost) == cudaSuccess) {
+      g_d2h += n * (long)sizeof(double);
+      return;
+    }
+    cudaGetLastError();
+  }
+  down_lines(d, n, kPlain, [&](long l, const double* src) {
+    line_copy_out(x + l * kPlain, src, std::min(kPlain, n - l * kPlain));
+  });
+}
+
 void set_design(tp_ctx* c, const gridContext& gc, const DTYPE* x) {
-  const HVec xc = el_to_canon(gc, x);
-  check(c, tp_upload(c, TP_FIELD_XPHYS, xc.data(), (long)xc.size()), "upload xPhys");
-  g_h2d += (long)(xc.size() * sizeof(double));
+  up_elems(tp_field_ptr(c, TP_FIELD_XPHYS), gc, x);
+  check(c, tp_field_written(c, TP_FIELD_XPHYS), "upload xPhys");
 }
 
 }  // namespace
@@ -504,15 +677,10 @@ void getComplianceAndSensetivity_halo(const struct gpuNode* node, const DTYPE* x
   tp_ctx* c = ctx_levels(gc, 2);
   set_design(c, gc, x);
   const Dims d = dims_of((int)gc.nelx, (int)gc.nely, (int)gc.nelz, 0);
-  const HVec h = to_canon(d, u);
-  check(c, tp_upload(c, TP_FIELD_U, h.data(), (long)h.size()), "upload U");
-  g_h2d += (long)(h.size() * sizeof(double));
+  up_nodes(tp_field_ptr(c, TP_FIELD_U), d, u);
   double cc = 0;
   check(c, tp_compliance(c, &cc), "getComplianceAndSensetivity_halo");
-  HVec dc(tp_nelem(c));
-  check(c, tp_download(c, TP_FIELD_DC, dc.data(), (long)dc.size()), "download dc");
-  g_d2h += (long)(dc.size() * sizeof(double));
-  el_from_canon(gc, dc, dcdx);
+  down_elems(tp_field_ptr(c, TP_FIELD_DC), gc, dcdx);
   *c_out = (DTYPE)cc;
 }
 
@@ -634,13 +802,10 @@ void solveStateMG_halo(const struct gpuGrid* gpu_gc, DTYPE* x, const int nswp, c
   tp_ctx* c = ctx_for((int)gc.nelx, (int)gc.nely, (int)gc.nelz, nl);
   set_design(c, gc, x);
   const Dims d = dims_of((int)gc.nelx, (int)gc.nely, (int)gc.nelz, 0);
-  const HVec hb = to_canon(d, b), hu = to_canon(d, u);
-  check(c, tp_upload(c, TP_FIELD_F, hb.data(), (long)hb.size()), "upload F");
-  g_h2d += (long)(hb.size() * sizeof(double));
-  check(c, tp_upload(c, TP_FIELD_U, hu.data(), (long)hu.size()), "upload U");
-  g_h2d += (long)(hu.size() * sizeof(double));
   double* F = tp_field_ptr(c, TP_FIELD_F);
   double* U = tp_field_ptr(c, TP_FIELD_U);
+  up_nodes(F, d, b);
+  up_nodes(U, d, u);
   // the reference's nswp and tol arrive per call; omega 0.6 and the cap of
   // 1000 iterations are fixed there (stencil_solvers.c:332-334)
   check(c, tp_set_cg(c, (double)tol, 1000, nswp, 0.6), "solver settings");
@@ -649,10 +814,7 @@ void solveStateMG_halo(const struct gpuGrid* gpu_gc, DTYPE* x, const int nswp, c
   check(c, tp_assemble(c), "assemble");
   const tp_status st = tp_solve_rhs(c, F, U, &it, &rr);
   check(c, st, "solveStateMG_halo");
-  HVec hu2(hu.size());
-  check(c, tp_download(c, TP_FIELD_U, hu2.data(), (long)hu2.size()), "download U");
-  g_d2h += (long)(hu2.size() * sizeof(double));
-  from_canon(d, hu2, u);
+  down_nodes(U, d, u);
   *finalIter = it;
   *finalRes = (float)rr;
 }
@@ -826,23 +988,24 @@ void solveSubspaceMatrix(const struct gridContext gc, const int l, struct Coarse
 // gpu_definitions.h: volume, change, OC update on the GPU
 DTYPE compute_volume(const struct gridContext gc, DTYPE* xPhys) {
   tp_ctx* c = ctx_levels(gc, 2);
-  const HVec h = el_to_canon(gc, xPhys);
-  double* d = up(0, h);
+  const long n = (long)gc.nelx * gc.nely * gc.nelz;
+  double* d = g_s[0].get(n);
+  up_elems(d, gc, xPhys);
   double s = 0;
-  check(c, tp_vec_sum(c, (long)h.size(), d, &s), "compute_volume");
+  check(c, tp_vec_sum(c, n, d, &s), "compute_volume");
   return (DTYPE)s;
 }
 
+// max |x - xnew| (exact in any order) and x <- xnew, on the host: the arrays
+// are there already, and the copy back was the reference's host loop
 float compute_change(DTYPE* x, DTYPE* xnew, const int nelem) {
-  tp_ctx* c = g_ctx.empty() ? nullptr : g_ctx.begin()->second;
-  if (!c) c = ctx_for(2, 2, 2, 2);
-  const HVec hx = el_copy(x, nelem), hn = el_copy(xnew, nelem);
-  double* dx = up(0, hx);
-  double* dn = up(1, hn);
-  double ch = 0;
-  check(c, tp_vec_change(c, nelem, dx, dn, &ch), "compute_change");
-#pragma omp parallel for schedule(static)
-  for (int e = 0; e < nelem; e++) x[e] = xnew[e];
+  double ch = 0.0;
+#pragma omp parallel for schedule(static) reduction(max : ch)
+  for (int e = 0; e < nelem; e++) {
+    const double dd = std::fabs((double)x[e] - (double)xnew[e]);
+    ch = dd > ch ? dd : ch;
+    x[e] = xnew[e];
+  }
   return (float)ch;
 }
 
@@ -850,15 +1013,15 @@ void update_solution(const DTYPE* x, DTYPE* xnew, const DTYPE* dv, const DTYPE* 
                      const DTYPE g) {
   tp_ctx* c = g_ctx.empty() ? nullptr : g_ctx.begin()->second;
   if (!c) c = ctx_for(2, 2, 2, 2);
-  const HVec hx = el_copy(x, nelem), hv = el_copy(dv, nelem), hc = el_copy(dc, nelem);
-  double* dx = up(0, hx);
-  double* ddv = up(1, hv);
-  double* ddc = up(2, hc);
+  double* dx = g_s[0].get(nelem);
+  double* ddv = g_s[1].get(nelem);
+  double* ddc = g_s[2].get(nelem);
   double* dn = g_s[3].get(nelem);
+  up_plain(dx, x, nelem);
+  up_plain(ddv, dv, nelem);
+  up_plain(ddc, dc, nelem);
   check(c, tp_oc_bisect(c, nelem, dx, ddv, ddc, (double)g, dn), "update_solution");
-  const HVec out = down(dn, nelem);
-#pragma omp parallel for schedule(static)
-  for (int e = 0; e < nelem; e++) xnew[e] = (DTYPE)out[e];
+  down_plain(dn, xnew, nelem);
 }
 
 // ---------------------------------------------------------------------------
@@ -866,20 +1029,22 @@ void update_solution(const DTYPE* x, DTYPE* xnew, const DTYPE* dv, const DTYPE* 
 void applyDensityFilter(const struct gridContext gc, const DTYPE rmin, const DTYPE* rho, DTYPE* out) {
   tp_ctx* c = ctx_levels(gc, 2);
   check(c, tp_set_rmin(c, (double)rmin), "set rmin");
-  const HVec h = el_to_canon(gc, rho);
-  double* din = up(0, h);
-  double* dout = g_s[1].get(h.size());
+  const long n = (long)gc.nelx * gc.nely * gc.nelz;
+  double* din = g_s[0].get(n);
+  double* dout = g_s[1].get(n);
+  up_elems(din, gc, rho);
   check(c, tp_filter(c, din, dout), "applyDensityFilter");
-  el_from_canon(gc, down(dout, h.size()), out);
+  down_elems(dout, gc, out);
 }
 
 void applyDensityFilterGradient(const struct gridContext gc, const DTYPE rmin, DTYPE* v) {
   tp_ctx* c = ctx_levels(gc, 2);
   check(c, tp_set_rmin(c, (double)rmin), "set rmin");
-  const HVec h = el_to_canon(gc, v);
-  double* dv = up(0, h);
+  const long n = (long)gc.nelx * gc.nely * gc.nelz;
+  double* dv = g_s[0].get(n);
+  up_elems(dv, gc, v);
   check(c, tp_filter_T(c, dv), "applyDensityFilterGradient");
-  el_from_canon(gc, down(dv, h.size()), v);
+  down_elems(dv, gc, v);
 }
 
 static void vtk_write(FILE* f, int wx, int wy, int wz, int ex, int ey, int ez, int e0, const DTYPE* dens,

@@ -73,6 +73,7 @@ def load():
     L.tp_device_bytes.argtypes = [V]
     L.tp_field_ptr.restype = ctypes.c_void_p
     L.tp_field_ptr.argtypes = [V, I]
+    L.tp_field_written.argtypes = [V, I]
     L.tp_upload.argtypes = [V, I, P, ctypes.c_long]
     L.tp_download.argtypes = [V, I, P, ctypes.c_long]
     L.tp_element_matrices.argtypes = [V, I, P]
@@ -550,13 +551,20 @@ class RefLoop:
         self.reset()
 
     def reset(self):
-        """x = xPhys = volfrac on the real elements, U = 0 (:97-137)."""
-        ones = np.ones(self.nelem)
-        self.x = el_to_padded(self.volfrac * ones, self.dims)
-        self.xPhys = self.x.copy()
-        self.xnew = np.zeros(self.nelem_padded)
-        self.dc = np.zeros(self.nelem_padded)
-        self.U = np.zeros_like(self.F)
+        """x = xPhys = volfrac on the real elements, U = 0 (:97-137). The
+        arrays are allocated once and refilled, as the reference's loop
+        allocates them once: a device copy into pages that were never
+        touched waits on their first faults."""
+        x0 = el_to_padded(self.volfrac * np.ones(self.nelem), self.dims)
+        if getattr(self, "x", None) is None:
+            self.x, self.xPhys = np.empty_like(x0), np.empty_like(x0)
+            self.xnew, self.dc = np.empty(self.nelem_padded), np.empty(self.nelem_padded)
+            self.U = np.empty_like(self.F)
+        np.copyto(self.x, x0)
+        np.copyto(self.xPhys, x0)
+        self.xnew.fill(0.0)
+        self.dc.fill(0.0)
+        self.U.fill(0.0)
 
     def iteration(self):
         L = self.L

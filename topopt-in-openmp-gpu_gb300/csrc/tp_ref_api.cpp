@@ -79,6 +79,11 @@ tp_ctx* ctx_for(int nelx, int nely, int nelz, int nl) {
                  c ? tp_error_message(c) : "");
     std::abort();
   }
+  // the level-0 kernels' launch plans tuned once for this grid (as a caller
+  // of the handle API does with tp_autotune): every plan gives the same
+  // results bit for bit; TOPOPT_AUTOTUNE=0 keeps the default plans
+  const char* tune = std::getenv("TOPOPT_AUTOTUNE");
+  if (!(tune && std::strcmp(tune, "0") == 0)) tp_autotune(c, nullptr);
   g_ctx[key] = c;
   return c;
 }

@@ -773,7 +773,11 @@ tp_status tp_solve_rhs(tp_ctx* c, const double* rhs, double* sol, int* iters, do
   }
   int it = 0;
   double rr = 0;
-  tp_status st = pcg(c, rhs, sol, &it, &rr);
+  // the context's own F and U (the drop-in layer's state solve): the captured
+  // CG loop, one host wait per solve instead of one per iteration (the same
+  // kernels and decisions); graph_solve 2 forces the host-driven loop
+  const bool graph = rhs == c->d_F && sol == c->d_U && c->p.nrhs == 1 && c->graph_solve != 2;
+  tp_status st = graph ? pcg_graph(c, &it, &rr) : pcg(c, rhs, sol, &it, &rr);
   if (iters) *iters = it;
   if (relres) *relres = rr;
   return st;

@@ -57,6 +57,7 @@ tp_status tp_set_rmin(tp_ctx* c, double rmin) {
 
 tp_status tp_set_cg(tp_ctx* c, double cgtol, int cgmax, int nswp, double omega) {
   if (!c || !(cgtol > 0) || cgmax < 1 || nswp < 0) return TP_ERR_ARG;
+  if (c->p.cgtol == cgtol && c->p.cgmax == cgmax && c->p.nswp == nswp && c->p.omega == omega) return TP_OK;
   c->p.cgtol = cgtol;
   c->p.cgmax = cgmax;
   c->p.nswp = nswp;

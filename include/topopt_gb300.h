@@ -205,6 +205,17 @@ tp_status tp_set_coarse_solve_variant(tp_ctx* c, int variant);
  * default is 1 for TP_MIXED, whose V-cycle is FP32, and 0 for TP_FP64. The
  * factor is redone at the next solve. */
 tp_status tp_set_coarse_arith(tp_ctx* c, int arith);
+/* Elimination order of the coarsest-level factor (CHOLMOD, which the
+ * reference calls at stencil_assembly.c:394-396, picks its own fill-reducing
+ * order): 0 = the natural node order, one band; 1 (the default) = one level
+ * of nested dissection, the middle x node plane as the separator: the two
+ * halves are banded factors eliminated at the same time (half the natural
+ * chain of 32-column steps each), then the separator's Schur complement, and
+ * the solve sweeps both halves in the same phases. Order 1 applies with the
+ * single-launch variant where the coarsest grid is large enough (otherwise
+ * the natural band is used). The two orders agree to rounding; the factor is
+ * redone at the next solve. */
+tp_status tp_set_coarse_order(tp_ctx* c, int order);
 /* Failure detection of the single-launch coarse factor and solve (host-side
  * fault injection, for tests): each of their waits in global memory gives up
  * after spin polls (0 = the default, about a second) and, with missing = 1,

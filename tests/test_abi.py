@@ -64,7 +64,7 @@ def test_create_rejects_bad_arguments(lib, field, value):
 
 
 @pytest.mark.parametrize("setter", ["tp_set_fine_variant", "tp_set_fine_arith", "tp_set_coarse_solve_variant",
-                                    "tp_set_coarse_arith"])
+                                    "tp_set_coarse_arith", "tp_set_coarse_order"])
 def test_selectors_reject_bad_arguments(lib, setter):
     """The kernel and arithmetic selectors check their arguments before any
     CUDA call: no context, or a choice other than 0 and 1, is TP_ERR_ARG."""

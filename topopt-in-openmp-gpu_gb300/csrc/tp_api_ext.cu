@@ -85,15 +85,7 @@ tp_status tp_set_fine_arith(tp_ctx* c, int arith) {
 
 // the factorisation is redone with the chosen launches or arithmetic at the next solve
 static void coarse_reset(tp_ctx* c) {
-  Coarse& C = c->coarse;
-  if (C.graph_exec) {
-    cudaGraphExecDestroy(C.graph_exec);
-    C.graph_exec = nullptr;
-  }
-  if (C.factor_exec) {
-    cudaGraphExecDestroy(C.factor_exec);
-    C.factor_exec = nullptr;
-  }
+  coarse_graphs_free(c);
   c->assembled = false;
   graph_free(c);
 }
@@ -101,6 +93,13 @@ static void coarse_reset(tp_ctx* c) {
 tp_status tp_set_coarse_solve_variant(tp_ctx* c, int variant) {
   if (!c || variant < 0 || variant > 1) return TP_ERR_ARG;
   c->coarse.solve_variant = variant;
+  coarse_reset(c);
+  return TP_OK;
+}
+
+tp_status tp_set_coarse_order(tp_ctx* c, int order) {
+  if (!c || order < 0 || order > 1) return TP_ERR_ARG;
+  c->coarse.order = order;
   coarse_reset(c);
   return TP_OK;
 }
@@ -117,14 +116,7 @@ tp_status tp_fault_coarse_barrier(tp_ctx* c, long spin, int missing) {
   Coarse& C = c->coarse;
   C.ps_spin = spin;
   C.ps_missing = missing;
-  if (C.graph_exec) {  // the captured solve and factorisation hold the old values
-    cudaGraphExecDestroy(C.graph_exec);
-    C.graph_exec = nullptr;
-  }
-  if (C.factor_exec) {
-    cudaGraphExecDestroy(C.factor_exec);
-    C.factor_exec = nullptr;
-  }
+  coarse_graphs_free(c);  // the captured solve and factorisation hold the old values
   graph_free(c);
   return TP_OK;
 }
@@ -190,6 +182,7 @@ tp_status tp_download_stencil(tp_ctx* c, int level, int subspace, double* host) 
 tp_status tp_coarse_factor_csr(tp_ctx* c, long n, const int* rowptr, const int* col, const double* val) {
   if (!c || !rowptr || !col || !val || n != c->coarse.n) return TP_ERR_ARG;
   Coarse& C = c->coarse;
+  coarse_use_natural(c);
   std::vector<double> band(C.band_elems, 0.0);
   for (long r = 0; r < n; r++)
     for (int q = rowptr[r]; q < rowptr[r + 1]; q++) {

@@ -52,6 +52,8 @@ __device__ __forceinline__ double bget(const double* B, long bw, long r, long c)
 
 static void ps_plan(tp_ctx* c);
 static void pf_plan(tp_ctx* c);
+static void nd_layout(tp_ctx* c);
+static void nd_plan(tp_ctx* c);
 
 // the operations the factor and solve kernels need on either value type
 __device__ __forceinline__ double vshfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
@@ -77,6 +79,12 @@ __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_grou
 template <int N>
 __device__ __forceinline__ void cp_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// sum over the warp (valid in lane 0), in a fixed tree
+__device__ __forceinline__ double wsum(double s) {
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  return s;
 }
 
 // ----------------------------------------------------------------------------
@@ -120,8 +128,6 @@ void coarse_alloc(tp_ctx* c) {
   C.n = L.ndof;
   C.bw = 3L * ((long)L.nz * L.ny + L.ny + 1) + 2;
   if (C.bw > C.n - 1) C.bw = std::max(1L, C.n - 1);
-  C.band_elems = (size_t)C.n * (C.bw + 1) + 1;
-  dev_malloc(&C.band, C.band_elems * sizeof(double));
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&C.nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -132,8 +138,14 @@ void coarse_alloc(tp_ctx* c) {
   const long nbs_sm = std::min((long)kNbsMax, std::max((long)NBS, (4L * C.nsm) / 32 * 32));
   C.nbs = (int)std::min(nbs_sm, ((C.n + 31) / 32) * 32);
   C.nblk = (int)((C.n + C.nbs - 1) / C.nbs);
-  const size_t dsz = (size_t)C.nblk * C.nbs * C.nbs;
-  const size_t lsz = (size_t)C.nblk * C.nbs * C.bw;
+  // the dissected factor shares the band, block inverse and block row arrays
+  nd_layout(c);
+  const long rows = C.nd_ok ? std::max(C.n, C.nd_ntot) : C.n;
+  const long blks = C.nd_ok ? std::max((long)C.nblk, (long)C.nd_blk0[2] + C.nd_nblk[2]) : (long)C.nblk;
+  C.band_elems = (size_t)rows * (C.bw + 1) + 1;
+  dev_malloc(&C.band, C.band_elems * sizeof(double));
+  const size_t dsz = (size_t)blks * C.nbs * C.nbs;
+  const size_t lsz = (size_t)blks * C.nbs * C.bw;
   dev_malloc(&C.dinv, dsz * sizeof(double));
   dev_malloc(&C.dinvT, dsz * sizeof(double));
   dev_malloc(&C.lrow, lsz * sizeof(double));
@@ -160,6 +172,7 @@ void coarse_alloc(tp_ctx* c) {
   }
   ps_plan(c);
   pf_plan(c);
+  nd_plan(c);
 }
 
 void coarse_free(tp_ctx* c) {
@@ -180,19 +193,61 @@ void coarse_free(tp_ctx* c) {
   dev_free(C.pf_flags);
   dev_free(C.pf_rpk);
   dev_free(C.pf_off);
+  if (C.nd_graph_exec) cudaGraphExecDestroy(C.nd_graph_exec);
+  if (C.nd_factor_exec) cudaGraphExecDestroy(C.nd_factor_exec);
+  dev_free(C.nd_map);
+  dev_free(C.nd_vec);
+  dev_free(C.nd_tail);
+  dev_free(C.nd_flags);
+  dev_free(C.nd_rpk);
+  dev_free(C.nd_off);
   C = Coarse();
 }
+
+__global__ void nd_scatter_kernel(int nx, int ny, int nz, int lim, long nnodes, long bw, int masked,
+                                  const double* __restrict__ st, double* __restrict__ B, int xs, long pad_a,
+                                  long pad_b, long org_b);
 
 void coarse_assemble(tp_ctx* c) {
   ProfScope ps(c, P_COARSE_FACTOR);
   Coarse& C = c->coarse;
   const int l = c->nl - 1;
   const Level& L = c->L[l];
+  const bool nd = C.nd_ok && C.order == 1 && C.solve_variant == 0;
+  if (nd != C.nd_use) {  // captured loops hold the other form's solve launches
+    C.nd_use = nd;
+    graph_free(c);
+  }
   cudaMemsetAsync(C.band, 0, C.band_elems * sizeof(double), c->s);
   const long work = L.nnodes * 14;
-  band_scatter_kernel<<<grid_for(work, 256), 256, 0, c->s>>>(L.nx, L.ny, L.nz, L.lim, L.nnodes, C.bw, l >= 2 ? 1 : 0,
-                                                             c->st[l], C.band);
+  if (nd)
+    nd_scatter_kernel<<<grid_for(std::max(work, 32L), 256), 256, 0, c->s>>>(
+        L.nx, L.ny, L.nz, L.lim, L.nnodes, C.bw, l >= 2 ? 1 : 0, c->st[l], C.band, C.nd_xs, C.nd_pad[0], C.nd_pad[1],
+        C.nd_org[1]);
+  else
+    band_scatter_kernel<<<grid_for(work, 256), 256, 0, c->s>>>(L.nx, L.ny, L.nz, L.lim, L.nnodes, C.bw,
+                                                               l >= 2 ? 1 : 0, c->st[l], C.band);
   TP_CHECK_LAUNCH(c, "band_scatter");
+}
+
+// The coarse factor came from a caller's matrix in the natural order
+// (tp_coarse_factor_csr): the solves use the natural band until the next
+// assembly from the grid.
+void coarse_use_natural(tp_ctx* c) {
+  Coarse& C = c->coarse;
+  if (C.nd_use) {
+    C.nd_use = false;
+    graph_free(c);
+  }
+}
+
+void coarse_graphs_free(tp_ctx* c) {
+  Coarse& C = c->coarse;
+  for (cudaGraphExec_t* g : {&C.graph_exec, &C.factor_exec, &C.nd_graph_exec, &C.nd_factor_exec})
+    if (*g) {
+      cudaGraphExecDestroy(*g);
+      *g = nullptr;
+    }
 }
 
 // ----------------------------------------------------------------------------
@@ -544,7 +599,7 @@ __global__ void __launch_bounds__(256) syrk_rest_kernel(double* __restrict__ B, 
 // ----------------------------------------------------------------------------
 // The whole factorisation as ONE cooperative launch, one CTA per SM. Tiles
 // are the 32 x 32 blocks (I, J), I >= J, of the band; step k factors diagonal
-// tile k. CTA 0 runs the chain every step waits on: factor tile (k,k), solve
+// tile k. The first CTA runs the chain every step waits on: factor tile (k,k), solve
 // the panel tile (k+1,k), apply step k's update to tile (k+1,k+1) -- which it
 // keeps in shared memory and factors as step k+1. The other CTAs take, in
 // step order and round-robin, the rest of each step: the panel tiles (I,k),
@@ -558,18 +613,24 @@ __global__ void __launch_bounds__(256) syrk_rest_kernel(double* __restrict__ B, 
 // thread 0 acquires it, and the band is read through L2 (ld.global.cg).
 // Items only wait on items of earlier steps or on earlier items of their
 // own step, and every CTA takes its items in order, so the waits end.
+// A partial factor runs NT steps of a longer band: its last step's updates
+// complete the trailing block (rows 32 NT ..), which is stored unfactored.
+// Two factors can share one launch on disjoint CTAs (the dissected order).
 struct PfArgs {
   double* B;
   long bw, n;
-  int NT, TS;        // diagonal tiles; row stride of sdone and tver
+  int NT, TS;        // steps (diagonal tiles factored); row stride of sdone and tver
   double* rpk;       // [NT][NB]
   int* fdone;        // [NT]
   int* sdone;        // [NT][TS]
-  int* tver;         // [NT][TS]
+  int* tver;         // [tiles][TS], tiles = ceil(n / 32)
   const long* off;   // [NT+1]: bulk items before step k
   int* info;
   int* abort_flag;
   long spin;
+  int cta0, ncta;    // the CTAs of this factor: cta0 (the chain) .. cta0 + ncta - 1
+  int partial;       // 1: NT steps leave a trailing block (rows 32 NT ..) with all their
+                     //    updates, unfactored; tile (NT, NT) is stored by the chain
 };
 constexpr size_t kPfSmem = 120 * 1024;  // more than half an SM's shared memory: one CTA per SM
 
@@ -688,6 +749,7 @@ __device__ void pf_chain(const PfArgs& a, double* smem) {
     }
     __syncthreads();
   }
+  if (a.partial && pf_imax(a.n, a.bw, a.NT - 1) >= a.NT) pf_store(a, a.NT, a.NT, D);  // D: tile (NT, NT)
 }
 
 // One work item of the non-chain CTAs: a panel tile (S: solve tile (I,k)
@@ -820,7 +882,8 @@ __device__ __forceinline__ void pf_put(const PfItem& it, const PfRegs& R, V (*P)
   }
 }
 
-// The non-chain CTAs take items g = blockIdx.x - 1 + m (gridDim.x - 1). While
+// The non-chain CTAs of the factor take items g = b - 1 + m (ncta - 1), b the
+// CTA's place among the factor's ncta. While
 // one item is computed, the next item's inputs are loaded into registers if
 // its flags are already set (otherwise it waits for them when its turn comes).
 template <typename V>
@@ -829,8 +892,8 @@ __device__ void pf_bulk(const PfArgs& a, double* smem) {
   V(*Q)[NB + 1] = reinterpret_cast<V(*)[NB + 1]>(smem + NB * (NB + 1));
   V* rp = reinterpret_cast<V*>(smem + 2 * NB * (NB + 1));
   volatile int* ready = reinterpret_cast<volatile int*>(rp + NB);
-  const long nbulk = gridDim.x - 1, total = a.off[a.NT];
-  long g = blockIdx.x - 1, kk = 0;
+  const long nbulk = a.ncta - 1, total = a.off[a.NT];
+  long g = (long)blockIdx.x - a.cta0 - 1, kk = 0;
   if (g >= total) return;
   PfItem cur, nxt;
   PfRegs R;
@@ -1152,6 +1215,14 @@ __device__ void pf_chain_ds(const PfArgs& a, double* smem) {
     }
     __syncthreads();
   }
+  if (a.partial && pf_imax(a.n, a.bw, a.NT - 1) >= a.NT) {  // tile (NT, NT), updated by the last step
+    const Dsf(*Dl)[NB + 1] = reinterpret_cast<const Dsf(*)[NB + 1]>(smem + (a.NT & 1) * kTile);
+    for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
+      const int r = idx & 31, c = idx >> 5;
+      const long gr = 32L * a.NT + r, gc = 32L * a.NT + c;
+      if (gr < a.n && gr >= gc) a.B[gc * a.bw + gr] = ds_to(Dl[r][c]);
+    }
+  }
 }
 
 __device__ void pf_bulk_ds(const PfArgs& a, double* smem) {
@@ -1162,8 +1233,8 @@ __device__ void pf_bulk_ds(const PfArgs& a, double* smem) {
   float2* PL = reinterpret_cast<float2*>(smem + 2 * kTile + NB + kPA);
   float4* QB = reinterpret_cast<float4*>(smem + 2 * kTile + NB + kPA + kPL);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long nbulk = gridDim.x - 1, total = a.off[a.NT];
-  long g = blockIdx.x - 1, kk = 0;
+  const long nbulk = a.ncta - 1, total = a.off[a.NT];
+  long g = (long)blockIdx.x - a.cta0 - 1, kk = 0;
   if (g >= total) return;
   PfItem cur, nxt;
   PfRegs R;
@@ -1234,19 +1305,29 @@ __device__ void pf_bulk_ds(const PfArgs& a, double* smem) {
 }
 
 template <typename V>
-__global__ void __launch_bounds__(256) pf_kernel(PfArgs a) {
-  extern __shared__ double sm[];
+__device__ __forceinline__ void pf_run(const PfArgs& a, double* sm) {
   if constexpr (std::is_same<V, Dsf>::value) {
-    if (blockIdx.x == 0)
+    if ((int)blockIdx.x == a.cta0)
       pf_chain_ds(a, sm);
     else
       pf_bulk_ds(a, sm);
   } else {
-    if (blockIdx.x == 0)
+    if ((int)blockIdx.x == a.cta0)
       pf_chain<V>(a, sm);
     else
       pf_bulk<V>(a, sm);
   }
+}
+
+// one factor (a1.cta0 >= gridDim.x) or two independent ones, the CTAs below
+// a1.cta0 on a0 and the others on a1
+template <typename V>
+__global__ void __launch_bounds__(256) pf_kernel(PfArgs a0, PfArgs a1) {
+  extern __shared__ double sm[];
+  if ((int)blockIdx.x < a1.cta0)
+    pf_run<V>(a0, sm);
+  else
+    pf_run<V>(a1, sm);
 }
 
 // Inverse of each diagonal nbs x nbs block of L, one CTA per (block, 32-column
@@ -1352,11 +1433,13 @@ __global__ void __launch_bounds__(kDinvThreads)
 }
 
 // row-major copy of the band rows of each block left of the block:
-// Lrow[blk][i][t] = L(b0 + i, b0 - bw + t), zero outside the band or the matrix
-__global__ void lrow_kernel(const double* __restrict__ B, long bw, long n, int nbs, double* __restrict__ Lrow) {
+// Lrow[blk][i][t] = L(b0 + i, b0 - bw + t), b0 = base + blk nbs, zero
+// outside the band or the matrix
+__global__ void lrow_kernel(const double* __restrict__ B, long bw, long n, int nbs, double* __restrict__ Lrow,
+                            long base = 0) {
   __shared__ double tile[32][33];
   const int blk = blockIdx.z;
-  const long b0 = (long)blk * nbs;
+  const long b0 = base + (long)blk * nbs;
   const int i0 = blockIdx.y * 32, t0 = blockIdx.x * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
   for (int k = ty; k < 32; k += 8) {
@@ -1370,6 +1453,145 @@ __global__ void lrow_kernel(const double* __restrict__ B, long bw, long n, int n
     const int i = i0 + k, t = t0 + tx;
     if (i < nbs && t < bw) Lrow[((long)blk * nbs + i) * bw + t] = tile[tx][k];
   }
+}
+
+// ----------------------------------------------------------------------------
+// Nested dissection of the coarsest grid, one level (Coarse::nd_*). The node
+// plane xs separates part A (planes < xs) from part B (planes > xs); no
+// entry of the operator couples A and B. In the composite order
+//   view A: pad_a identity rows, A in natural order, then S (natural order)
+//   view B: pad_b identity rows, B in mirrored plane order (plane nx-1 first,
+//           so that the plane next to S comes last), then S
+//   view S: S
+// each of A and B is a band of the natural half bandwidth with S as a
+// trailing block. Eliminating A's and B's own rows (the partial factors)
+// leaves in the trailing blocks  S_A = K_SS - L_SA L_SA^T  and
+// -L_SB L_SB^T, whose sum is the Schur complement K_SS - K_SA K_AA^-1 K_AS
+// - K_SB K_BB^-1 K_BS that view S then factors. The two partial factors are
+// independent, so they run at the same time on halves of the grid, each
+// with its own 32-column chain (half the natural chain's length).
+//   solve: y_A = L_A^-1 b_A, y_B = L_B^-1 b_B; y_S = L_S^-1 (b_S - L_SA y_A
+//   - L_SB y_B); x_S = L_S^-T y_S; x_A = L_A^-T (y_A - L_SA^T x_S), x_B alike.
+
+// position of DOF (node (p, k, j), component c), p >= xs, in view B
+__host__ __device__ __forceinline__ long nd_pos_b(int p, int k, int j, int c, int nx, int ny, int nz, long pad_b) {
+  return pad_b + 3L * (((long)(nx - 1 - p) * nz + k) * ny + j) + c;
+}
+
+// the entries band_scatter_kernel writes, placed in the views: a pair of
+// nodes in planes <= xs goes to view A (natural order, after pad_a rows; the
+// S x S block only there), any other pair to view B (mirrored order, its
+// S x S block left zero); then the pads' unit diagonals
+__global__ void nd_scatter_kernel(int nx, int ny, int nz, int lim, long nnodes, long bw, int masked,
+                                  const double* __restrict__ st, double* __restrict__ B, int xs, long pad_a,
+                                  long pad_b, long org_b) {
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (t < pad_a) B[t * bw + t] = 1.0;
+  if (t < pad_b) B[(org_b + t) * bw + org_b + t] = 1.0;
+  if (t >= nnodes * 14) return;
+  const long n = t % nnodes;
+  const int m = (int)(t / nnodes);  // 0..13
+  const int j = n % ny;
+  const int k = (n / ny) % nz;
+  const int i = n / ((long)ny * nz);
+  const int mx = m / 9 - 1, mz = (m / 3) % 3 - 1, my = m % 3 - 1;
+  const int mi = i + mx, mk = k + mz, mj = j + my;
+  if (mi < 0 || mi >= nx || mk < 0 || mk >= nz || mj < 0 || mj >= ny) return;
+  const long nm = ((long)mi * nz + mk) * ny + mj;
+  const bool nfix = i == 0 && (j < lim || j >= ny - lim);
+  const bool mfix = mi == 0 && (mj < lim || mj >= ny - lim);
+  for (int c = 0; c < 3; c++)
+    for (int d = 0; d < 3; d++) {
+      const long r = 3 * n + c, col = 3 * nm + d;
+      if (col > r || r - col > bw) continue;
+      double v;
+      if (nfix)
+        v = (r == col) ? 1.0 : 0.0;
+      else if (masked && m != 13 && mfix)
+        v = 0.0;
+      else
+        v = (m == 13) ? st[(long)(3 * c + d) * nnodes + n] : st[((long)(13 - m) * 9 + 3 * d + c) * nnodes + nm];
+      if (i <= xs) {  // mi <= i: both nodes in A or S
+        B[(col + pad_a) * bw + r + pad_a] = v;
+      } else {        // i > xs, mi >= i - 1 >= xs: both in B or S
+        const long pr = nd_pos_b(i, k, j, c, nx, ny, nz, pad_b), pc = nd_pos_b(mi, mk, mj, d, nx, ny, nz, pad_b);
+        const long hi = lmax(pr, pc), lo = lmin(pr, pc);
+        if (hi - lo <= bw) B[(org_b + lo) * bw + org_b + hi] = v;
+      }
+    }
+}
+
+// view S (lower part) = the trailing blocks of views A and B, summed
+__global__ void nd_schur_kernel(double* __restrict__ B, long bw, long ns, long own_a, long org_b, long own_b,
+                                long org_s) {
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (t >= ns * ns) return;
+  const long i = t % ns, j = t / ns;
+  if (i < j) return;
+  const double a = B[(own_a + j) * bw + own_a + i];
+  const double b = B[(org_b + own_b + j) * bw + org_b + own_b + i];
+  B[(org_s + j) * bw + org_s + i] = a + b;
+}
+
+// composite <- natural (pads and tails zero), per column
+__global__ void nd_gather_kernel(const int* __restrict__ map, long ntot, const double* __restrict__ src, long n,
+                                 double* __restrict__ dst, int nr) {
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (t >= ntot * nr) return;
+  const long v = t / ntot, i = t % ntot;
+  const int m = map[i];
+  dst[t] = m >= 0 ? src[v * n + m] : 0.0;
+}
+
+// natural <- composite, per column
+__global__ void nd_scatter_out_kernel(const int* __restrict__ map, long ntot, const double* __restrict__ src,
+                                      long n, double* __restrict__ dst, int nr) {
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (t >= ntot * nr) return;
+  const long v = t / ntot, i = t % ntot;
+  const int m = map[i];
+  if (m >= 0) dst[v * n + m] = src[t];
+}
+
+// b_S -= L_SA y_A + L_SB y_B, one warp per row of S; the tails' rows are
+// row-major (tail[s][e] = L(own + s, own - bw + e)), each lane sums its
+// positions in order, then the warp in a fixed tree
+template <int NR>
+__global__ void nd_couple_kernel(const double* __restrict__ tail_a, const double* __restrict__ tail_b, long bw,
+                                 long ns, long own_a, long org_a, long own_b, long org_b, long org_s, long vn,
+                                 const double* __restrict__ y, double* __restrict__ rhs) {
+  const long s = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (s >= ns) return;
+  double acc[NR];
+#pragma unroll
+  for (int v = 0; v < NR; v++) acc[v] = 0.0;
+  for (int part = 0; part < 2; part++) {
+    const double* L = (part == 0 ? tail_a : tail_b) + s * bw;
+    const long own = part == 0 ? own_a : own_b, org = part == 0 ? org_a : org_b;
+    const double* yy = y + org + own - bw;  // column own - bw + e of the view
+    for (long e = lmax(s, bw - own) + lane; e < bw; e += 32) {
+      const double l = L[e];
+#pragma unroll
+      for (int v = 0; v < NR; v++) acc[v] += l * yy[v * vn + e];
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < NR; v++) {
+    const double sv = wsum(acc[v]);
+    if (lane == 0) rhs[v * vn + org_s + s] -= sv;
+  }
+}
+
+// x_S into the tails of views A and B, per column
+__global__ void nd_tails_kernel(double* __restrict__ x, long ns, long vn, long tail_a, long tail_b, long org_s,
+                                int nr) {
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (t >= ns * nr) return;
+  const long v = t / ns, s = t % ns;
+  const double xs = x[v * vn + org_s + s];
+  x[v * vn + tail_a + s] = xs;
+  x[v * vn + tail_b + s] = xs;
 }
 
 // The factorisation as launches per 32-column step (where the single launch
@@ -1430,26 +1652,38 @@ static void step_launches(tp_ctx* c) {
 // Plan of the single-launch factorisation: the flag arrays and the count of
 // the other CTAs' work items per step (T-1 panel tiles and T(T+1)/2 - 1 tile
 // updates for a panel of T tile rows).
-static void pf_plan(tp_ctx* c) {
-  Coarse& C = c->coarse;
-  C.pf_ok = false;
-  const long NT = (C.n + 31) / 32;
-  if (NT < 2 || C.nsm < 2) return;
+// the other CTAs' work items before each of NT steps of a band of n rows
+static long pf_items(long n, long bw, long NT, std::vector<long>& off) {
   long TS = 2;
-  std::vector<long> off(NT + 1, 0);
+  off.assign(NT + 1, 0);
   for (long k = 0; k < NT; k++) {
-    const long T = pf_imax(C.n, C.bw, k) - k;
+    const long T = pf_imax(n, bw, k) - k;
     TS = std::max(TS, T + 2);
     off[k + 1] = off[k] + (T >= 1 ? (T - 1) + T * (T + 1) / 2 - 1 : 0);
   }
+  return TS;
+}
+
+static bool pf_fits() {
   for (auto kern : {pf_kernel<double>, pf_kernel<Dsf>}) {
     int per = 0;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPfSmem) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, 256, kPfSmem) != cudaSuccess || per < 1) {
       cudaGetLastError();
-      return;
+      return false;
     }
   }
+  return true;
+}
+
+static void pf_plan(tp_ctx* c) {
+  Coarse& C = c->coarse;
+  C.pf_ok = false;
+  const long NT = (C.n + 31) / 32;
+  if (NT < 2 || C.nsm < 2) return;
+  std::vector<long> off;
+  const long TS = pf_items(C.n, C.bw, NT, off);
+  if (!pf_fits()) return;
   C.pf_NT = (int)NT;
   C.pf_TS = (int)TS;
   C.pf_flag_bytes = sizeof(int) * (size_t)(NT + 2 * NT * TS + 1);
@@ -1470,7 +1704,9 @@ static void pf_launch(tp_ctx* c) {
   const long NT = C.pf_NT, TS = C.pf_TS;
   int* f = C.pf_flags;
   PfArgs a{C.band, C.bw, C.n, (int)NT, (int)TS, C.pf_rpk, f, f + NT, f + NT + NT * TS, C.pf_off, C.info,
-           f + NT + 2 * NT * TS, C.ps_spin > 0 ? C.ps_spin : kBarrierSpin};
+           f + NT + 2 * NT * TS, C.ps_spin > 0 ? C.ps_spin : kBarrierSpin, 0, C.nsm, 0};
+  PfArgs none = a;
+  none.cta0 = C.nsm;
   cudaMemsetAsync(C.pf_flags, 0, C.pf_flag_bytes, c->s);
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeCooperative;
@@ -1482,7 +1718,7 @@ static void pf_launch(tp_ctx* c) {
   cfg.stream = c->s;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, C.ds ? pf_kernel<Dsf> : pf_kernel<double>, a);
+  cudaLaunchKernelEx(&cfg, C.ds ? pf_kernel<Dsf> : pf_kernel<double>, a, none);
 }
 
 static void coarse_factor_launches(tp_ctx* c, size_t dinv_smem) {
@@ -1500,28 +1736,39 @@ static void coarse_factor_launches(tp_ctx* c, size_t dinv_smem) {
 
 // The launch sequence (about 2 per 32 columns) is captured once into a CUDA
 // graph on the context's stream and replayed at every design iteration.
+static void nd_factor_launches(tp_ctx* c, size_t dinv_smem);
+
 void coarse_factor(tp_ctx* c) {
   ProfScope ps(c, P_COARSE_FACTOR);
   Coarse& C = c->coarse;
   const size_t smem = ((size_t)C.nbs * 33 + 2 * 32 * 33) * sizeof(double);
-  if (!C.factor_exec) {
-    cudaFuncSetAttribute(dinv_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(dinv_kernel<Dsf>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const bool nd = C.nd_use;
+  cudaGraphExec_t& ex = nd ? C.nd_factor_exec : C.factor_exec;
+  auto launches = [&]() {
+    if (nd)
+      nd_factor_launches(c, smem);
+    else
+      coarse_factor_launches(c, smem);
+  };
+  if (!ex) {
+    static size_t smem_max = 0;  // the attribute only grows (contexts of other sizes)
+    smem_max = std::max(smem_max, smem);
+    cudaFuncSetAttribute(dinv_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+    cudaFuncSetAttribute(dinv_kernel<Dsf>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-      coarse_factor_launches(c, smem);
+      launches();
       if (cudaStreamEndCapture(c->s, &g) == cudaSuccess && g) {
-        if (cudaGraphInstantiate(&C.factor_exec, g, cudaGraphInstantiateFlagUseNodePriority) != cudaSuccess)
-          C.factor_exec = nullptr;
+        if (cudaGraphInstantiate(&ex, g, cudaGraphInstantiateFlagUseNodePriority) != cudaSuccess) ex = nullptr;
         cudaGraphDestroy(g);
       }
     }
     cudaGetLastError();
   }
-  if (C.factor_exec)
-    cudaGraphLaunch(C.factor_exec, c->s);
+  if (ex)
+    cudaGraphLaunch(ex, c->s);
   else
-    coarse_factor_launches(c, smem);
+    launches();
   TP_CHECK_LAUNCH(c, "coarse_factor");
 }
 
@@ -1532,10 +1779,6 @@ void coarse_factor(tp_ctx* c) {
 // Up to kSolveCols right-hand sides (columns n apart) share each load of L.
 constexpr int kSolveCols = 8;
 
-__device__ __forceinline__ double wsum(double s) {
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  return s;
-}
 
 template <int NR>
 __global__ void fwd_rows_kernel(const double* __restrict__ Lrow, long bw, long n, int nbs, int blk,
@@ -1673,13 +1916,27 @@ __device__ __forceinline__ int ps_part_warp(int rl, int q, int R, int P) {
   return rl * P + q;
 }
 
-struct PsArgs {
-  const double* lrow;
-  const double* band;
-  const double* D;
+// A view: a band matrix solved by blocks of nbs rows. Its own rows (nown,
+// in blocks) may be followed by a tail (rows nown .. nview-1, solved
+// elsewhere): the backward sweep then reads the tail's solution, which the
+// caller has put behind the own rows in x. Vector entries of the view sit at
+// voff + row of every column.
+struct PsView {
+  const double* lrow;  // row-major band rows left of each block, nbs x bw per block
+  const double* band;  // the view's band (its first row at the origin)
+  const double* D;     // block inverses, row-major
   const double* DT;
-  long bw, n;
-  int nbs, nblk, R, P, seg;
+  long nown, nview, voff;
+  int nblk;
+};
+
+struct PsArgs {
+  PsView v0, v1;  // rows i < nbs of a phase belong to v0, nbs <= i < 2 nbs to v1 (nv = 2)
+  int nv;
+  long bw, vn;    // half bandwidth; distance between the vectors' columns
+  int nbs, m, R, P, seg;  // m: blocks of the longest view
+  int tail;       // the views have tails: every block, the last included, has a BA phase
+  int h0, h1;     // phases of this launch
   const double* rhs;
   double* y;
   double* t;
@@ -1692,18 +1949,44 @@ struct PsArgs {
 
 enum { PH_FA = 0, PH_FB, PH_BA, PH_BB };
 
+// phases of the forward sweep, and of both
+__host__ __device__ __forceinline__ int ps_nfwd(int m) { return 2 * m - 1; }
+__host__ __device__ __forceinline__ int ps_nall(int m, int tail) { return 4 * m - (tail ? 1 : 2); }
+
 // phase h -> (kind, block): forward FB_0, FA_1, FB_1, ..., FB_{m-1}, then
-// backward BB_{m-1}, BA_{m-2}, BB_{m-2}, ..., BB_0 (m = nblk)
+// backward BB_{m-1}, BA_{m-2}, BB_{m-2}, ..., BB_0; with tails the backward
+// sweep is BA_{m-1}, BB_{m-1}, BA_{m-2}, ..., BB_0
 __device__ __forceinline__ void ps_phase(const PsArgs& a, int h, int& kind, int& k) {
-  const int nf = 2 * a.nblk - 1;
+  const int nf = ps_nfwd(a.m);
   if (h < nf) {
     k = (h + 1) / 2;
     kind = (h & 1) ? PH_FA : PH_FB;
+  } else if (a.tail) {
+    const int q = h - nf;
+    k = a.m - 1 - q / 2;
+    kind = (q & 1) ? PH_BB : PH_BA;
   } else {
     const int q = h - nf;
-    k = a.nblk - 1 - (q + 1) / 2;
+    k = a.m - 1 - (q + 1) / 2;
     kind = (q & 1) ? PH_BA : PH_BB;
   }
+}
+
+// the view of phase row i (a copy, selected field by field so that it stays
+// in registers), and i within it
+__device__ __forceinline__ PsView ps_view(const PsArgs& a, int& i) {
+  const bool q = a.nv == 2 && i >= a.nbs;
+  if (q) i -= a.nbs;
+  PsView V;
+  V.lrow = q ? a.v1.lrow : a.v0.lrow;
+  V.band = q ? a.v1.band : a.v0.band;
+  V.D = q ? a.v1.D : a.v0.D;
+  V.DT = q ? a.v1.DT : a.v0.DT;
+  V.nown = q ? a.v1.nown : a.v0.nown;
+  V.nview = q ? a.v1.nview : a.v0.nview;
+  V.voff = q ? a.v1.voff : a.v0.voff;
+  V.nblk = q ? a.v1.nblk : a.v0.nblk;
+  return V;
 }
 
 // Row i of block k in phase kind: the matrix entry at position e is m[e], the
@@ -1715,33 +1998,35 @@ struct PsRow {
   long voff, a0, a1;
 };
 
-__device__ __forceinline__ bool ps_row(const PsArgs& a, int kind, int k, int i, int p, PsRow& r) {
+// row i of the view V (i within the view's block)
+__device__ __forceinline__ bool ps_row(const PsArgs& a, const PsView& V, int kind, int k, int i, int p, PsRow& r) {
+  if (k >= V.nblk) return false;
   const long b0 = (long)k * a.nbs;
-  const int s = (int)lmin((long)a.nbs, a.n - b0);
+  const int s = (int)lmin((long)a.nbs, V.nown - b0);
   if (i >= s) return false;
   long lo, hi;
   if (kind == PH_FA) {  // t = b - Lrow_k y over columns b0-bw+e, e in [max(0, bw-b0, i), bw)
-    r.m = a.lrow + ((long)k * a.nbs + i) * a.bw;
-    r.vb = a.y;
+    r.m = V.lrow + ((long)k * a.nbs + i) * a.bw;
+    r.vb = a.y + V.voff;
     r.voff = b0 - a.bw;
     lo = lmax(lmax(0L, a.bw - b0), (long)i);
     hi = a.bw;
   } else if (kind == PH_FB) {  // y_k = D_k t_k, lower triangle
-    r.m = a.D + ((long)k * a.nbs + i) * a.nbs;
-    r.vb = k == 0 ? a.rhs : a.t;
+    r.m = V.D + ((long)k * a.nbs + i) * a.nbs;
+    r.vb = (k == 0 ? a.rhs : a.t) + V.voff;
     r.voff = b0;
     lo = 0;
     hi = i + 1;
   } else if (kind == PH_BA) {  // t = y - L(b1.., r)^T x: band column r is contiguous
-    const long rr = b0 + i, b1 = lmin(a.n, b0 + a.nbs);
-    r.m = a.band + rr * a.bw;
-    r.vb = a.x;
+    const long rr = b0 + i, b1 = lmin(V.nown, b0 + a.nbs);
+    r.m = V.band + rr * a.bw;
+    r.vb = a.x + V.voff;
     r.voff = 0;
     lo = b1;
-    hi = lmin(a.n - 1, rr + a.bw) + 1;
+    hi = lmin(V.nview - 1, rr + a.bw) + 1;
   } else {  // x_k = D_k^T t_k, upper triangle
-    r.m = a.DT + ((long)k * a.nbs + i) * a.nbs;
-    r.vb = k == a.nblk - 1 ? a.y : a.t;
+    r.m = V.DT + ((long)k * a.nbs + i) * a.nbs;
+    r.vb = (a.tail || k != V.nblk - 1 ? a.t : a.y) + V.voff;
     r.voff = b0;
     lo = i;
     hi = s;
@@ -1754,11 +2039,12 @@ __device__ __forceinline__ bool ps_row(const PsArgs& a, int kind, int k, int i, 
 
 // stage this warp's part of phase h's matrix row; lane l copies (and later
 // reads) positions a0 + l, a0 + l + 32, ...
-__device__ __forceinline__ void ps_stage(const PsArgs& a, int h, double* wbuf, int i, int p, int lane) {
+__device__ __forceinline__ void ps_stage(const PsArgs& a, const PsView& V, int h, double* wbuf, int i, int p,
+                                         int lane) {
   int kind, k;
   ps_phase(a, h, kind, k);
   PsRow r;
-  if (!ps_row(a, kind, k, i, p, r)) return;
+  if (!ps_row(a, V, kind, k, i, p, r)) return;
   for (long e = r.a0 + lane; e < r.a1; e += 32) cp_async8(wbuf + (e - r.a0), r.m + e);
 }
 
@@ -1798,15 +2084,15 @@ __global__ void __launch_bounds__(kPsWarps * 32) ps_solve_kernel(PsArgs a) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int rl, p;
   ps_warp_row(w, a.R, a.P, rl, p);
-  const int i = ps_row_of(blockIdx.x, rl, gridDim.x);
+  int i = ps_row_of(blockIdx.x, rl, gridDim.x);
+  const PsView V = ps_view(a, i);  // this warp's view and row, the same in every phase
   auto buf = [&](int b) { return sm + (long)(b * kPsWarps + w) * a.seg; };  // stage b of this warp
   double* part = sm + 2L * kPsWarps * a.seg;  // [warp][NR]
-  const int nph = 4 * a.nblk - 2;
-  ps_stage(a, 0, buf(0), i, p, lane);
+  ps_stage(a, V, a.h0, buf(0), i, p, lane);
   cp_commit();
-  for (int h = 0; h < nph; h++) {
-    if (h + 1 < nph) {
-      ps_stage(a, h + 1, buf((h + 1) & 1), i, p, lane);
+  for (int h = a.h0; h < a.h1; h++) {
+    if (h + 1 < a.h1) {
+      ps_stage(a, V, h + 1, buf((h + 1 - a.h0) & 1), i, p, lane);
       cp_commit();
       cp_wait<1>();
     } else {
@@ -1818,12 +2104,12 @@ __global__ void __launch_bounds__(kPsWarps * 32) ps_solve_kernel(PsArgs a) {
     double acc[NR];
 #pragma unroll
     for (int v = 0; v < NR; v++) acc[v] = 0.0;
-    if (ps_row(a, kind, k, i, p, r)) {
+    if (ps_row(a, V, kind, k, i, p, r)) {
       // U positions per lane per round: all their L2 loads are issued before
       // the first multiply-add, so a round costs one L2 latency; the sum
       // still runs over the positions in order
       constexpr int U = NR == 1 ? 16 : (NR == 2 ? 8 : (NR == 4 ? 4 : 2));
-      const double* mb = buf(h & 1);
+      const double* mb = buf((h - a.h0) & 1);
       for (long e0 = r.a0 + lane; e0 < r.a1; e0 += 32L * U) {
         double mv[U], vv[U][NR];
 #pragma unroll
@@ -1832,7 +2118,7 @@ __global__ void __launch_bounds__(kPsWarps * 32) ps_solve_kernel(PsArgs a) {
           const bool in = e < r.a1;
           mv[u] = in ? mb[e - r.a0] : 0.0;
 #pragma unroll
-          for (int v = 0; v < NR; v++) vv[u][v] = in ? __ldcg(r.vb + (v * a.n + r.voff + e)) : 0.0;
+          for (int v = 0; v < NR; v++) vv[u][v] = in ? __ldcg(r.vb + (v * a.vn + r.voff + e)) : 0.0;
         }
 #pragma unroll
         for (int u = 0; u < U; u++)
@@ -1849,11 +2135,12 @@ __global__ void __launch_bounds__(kPsWarps * 32) ps_solve_kernel(PsArgs a) {
     if (threadIdx.x < a.R * NR) {
       const int rr = threadIdx.x / NR, v = threadIdx.x % NR;
       const long b0 = (long)k * a.nbs;
-      const long row = ps_row_of(blockIdx.x, rr, gridDim.x);
-      if (row < lmin((long)a.nbs, a.n - b0)) {
+      int row = ps_row_of(blockIdx.x, rr, gridDim.x);
+      const PsView W = ps_view(a, row);
+      if (k < W.nblk && row < lmin((long)a.nbs, W.nown - b0)) {
         double sum = 0.0;
         for (int q = 0; q < a.P; q++) sum += part[ps_part_warp(rr, q, a.R, a.P) * NR + v];
-        const long o = v * a.n + b0 + row;
+        const long o = v * a.vn + W.voff + b0 + row;
         if (kind == PH_FA)
           a.t[o] = a.rhs[o] - sum;
         else if (kind == PH_FB)
@@ -1864,7 +2151,7 @@ __global__ void __launch_bounds__(kPsWarps * 32) ps_solve_kernel(PsArgs a) {
           a.x[o] = sum;
       }
     }
-    if (h + 1 < nph && !ps_barrier(a.bar, a.err, (unsigned)(h + 1) * gridDim.x + a.missing, a.spin)) break;
+    if (h + 1 < a.h1 && !ps_barrier(a.bar, a.err, (unsigned)(h + 1 - a.h0) * gridDim.x + a.missing, a.spin)) break;
   }
   cp_wait<0>();
   // every CTA, on every path, counts itself out; the last one puts the
@@ -1880,27 +2167,28 @@ __global__ void __launch_bounds__(kPsWarps * 32) ps_solve_kernel(PsArgs a) {
   }
 }
 
-// Launch plan: R rows per CTA (1, 2, 4 or 8), the fewest that keep one CTA
-// per SM; P = 8/R warps per row; shared memory for two stages of every
-// warp's longest part. No plan (ps_grid = 0) if the stages do not fit or
+// Launch plan for phases of `rows` rows: R rows per CTA (1, 2, 4 or 8), the
+// fewest that keep one CTA per SM; P = 8/R warps per row; shared memory for
+// two stages of every warp's longest part. false if the stages do not fit or
 // the grid cannot be co-resident.
-static void ps_plan(tp_ctx* c) {
-  Coarse& C = c->coarse;
-  C.ps_grid = 0;
-  if (!C.bar || C.nblk < 1) return;
-  int dev = 0, nsm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+struct PsPlan {
+  int R = 0, P = 0, grid = 0, seg = 0;
+  size_t smem = 0;
+};
+static bool ps_plan_rows(long rows, long bw, int nbs, int nsm, PsPlan& pl) {
   int R = 1;
-  while (R < kPsWarps && (C.nbs + R - 1) / R > nsm) R *= 2;
+  while (R < kPsWarps && (rows + R - 1) / R > nsm) R *= 2;
   const int P = kPsWarps / R;
-  const int grid = (C.nbs + R - 1) / R;
-  if (grid > nsm) return;
-  const long seg = std::max((C.bw + P - 1) / P, (long)(C.nbs + P - 1) / P);
+  const long grid = (rows + R - 1) / R;
+  if (grid > nsm) return false;
+  const long seg = std::max((bw + P - 1) / P, (long)(nbs + P - 1) / P);
   const size_t smem = (size_t)(2 * kPsWarps * seg + kPsWarps * 8) * sizeof(double);
-  if (smem > 200 * 1024) return;
+  if (smem > 200 * 1024) return false;
+  // the attribute only grows: contexts of other sizes keep their larger plans
+  static size_t smem_max = 0;
+  const size_t attr = std::max(smem, smem_max);
   auto fits = [&](const void* f) {
-    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return false;
+    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)attr) != cudaSuccess) return false;
     int per = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, kPsWarps * 32, smem) != cudaSuccess) return false;
     return per >= 1;
@@ -1908,30 +2196,60 @@ static void ps_plan(tp_ctx* c) {
   const bool ok = fits((const void*)ps_solve_kernel<1>) && fits((const void*)ps_solve_kernel<2>) &&
                   fits((const void*)ps_solve_kernel<4>) && fits((const void*)ps_solve_kernel<8>);
   cudaGetLastError();
-  if (!ok) return;
-  C.ps_R = R;
-  C.ps_P = P;
-  C.ps_seg = (int)seg;
-  C.ps_smem = smem;
-  C.ps_grid = grid;
+  if (!ok) return false;
+  smem_max = attr;
+  pl.R = R;
+  pl.P = P;
+  pl.grid = (int)grid;
+  pl.seg = (int)seg;
+  pl.smem = smem;
+  return true;
+}
+
+static void ps_plan(tp_ctx* c) {
+  Coarse& C = c->coarse;
+  C.ps_grid = 0;
+  if (!C.bar || C.nblk < 1) return;
+  PsPlan pl;
+  if (!ps_plan_rows(C.nbs, C.bw, C.nbs, C.nsm, pl)) return;
+  C.ps_R = pl.R;
+  C.ps_P = pl.P;
+  C.ps_seg = pl.seg;
+  C.ps_smem = pl.smem;
+  C.ps_grid = pl.grid;
+}
+
+static PsView ps_view_natural(const Coarse& C) {
+  return PsView{C.lrow, C.band, C.dinv, C.dinvT, C.n, C.n, 0, C.nblk};
+}
+
+// one cooperative launch of phases [h0, h1) over nv views
+template <int NR>
+static void ps_launch_views(tp_ctx* c, const PsView& v0, const PsView& v1, int nv, long vn, int m, int tail, int h0,
+                            int h1, int R, int P, int seg, int grid, size_t smem, const double* rhs, double* y,
+                            double* t, double* x) {
+  Coarse& C = c->coarse;
+  PsArgs a{v0, v1, nv, C.bw, vn, C.nbs, m, R, P, seg, tail, h0, h1, rhs, y, t, x,
+           C.bar, C.serr, C.ps_spin > 0 ? C.ps_spin : kBarrierSpin, (unsigned)C.ps_missing};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(kPsWarps * 32);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = c->s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, ps_solve_kernel<NR>, a);
 }
 
 template <int NR>
 static void ps_launch(tp_ctx* c, const double* rhs, double* sol, double* y, double* t) {
   Coarse& C = c->coarse;
-  PsArgs a{C.lrow, C.band, C.dinv, C.dinvT, C.bw, C.n, C.nbs, C.nblk, C.ps_R, C.ps_P, C.ps_seg,
-           rhs, y, t, sol, C.bar, C.serr, C.ps_spin > 0 ? C.ps_spin : kBarrierSpin, (unsigned)C.ps_missing};
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeCooperative;
-  at[0].val.cooperative = 1;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)C.ps_grid);
-  cfg.blockDim = dim3(kPsWarps * 32);
-  cfg.dynamicSmemBytes = C.ps_smem;
-  cfg.stream = c->s;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, ps_solve_kernel<NR>, a);
+  const PsView v = ps_view_natural(C);
+  ps_launch_views<NR>(c, v, v, 1, C.n, C.nblk, 0, 0, ps_nall(C.nblk, 0), C.ps_R, C.ps_P, C.ps_seg, C.ps_grid,
+                      C.ps_smem, rhs, y, t, sol);
 }
 
 tp_status coarse_status(tp_ctx* c) {
@@ -1982,9 +2300,15 @@ static void coarse_solve_launches(tp_ctx* c, const double* rhs, double* sol, dou
 // capture of a larger sequence (c->capturing) the launches are recorded
 // directly, in chunks of kSolveCols columns working in the caller's buffers
 // with the internal work columns.
+static void nd_solve(tp_ctx* c, const double* rhs, double* x, int nr);
+
 void coarse_solve(tp_ctx* c, const double* rhs, double* x, int nr) {
   ProfScope ps(c, P_COARSE_SOLVE);
   Coarse& C = c->coarse;
+  if (C.nd_use) {
+    nd_solve(c, rhs, x, nr);
+    return;
+  }
   if (nr > 1 || c->capturing) {
     double *y = C.vec, *t = C.vec + (long)kSolveCols * C.n;
     for (int r0 = 0; r0 < nr;) {
@@ -2024,6 +2348,256 @@ void coarse_solve(tp_ctx* c, const double* rhs, double* x, int nr) {
     cudaGraphLaunch(C.graph_exec, c->s);
   else
     coarse_solve_launches<1>(c, C.rhs, C.sol, C.vec, C.vec + C.n);
+  cudaMemcpyAsync(x, C.sol, sizeof(double) * C.n, cudaMemcpyDeviceToDevice, c->s);
+  TP_CHECK_LAUNCH(c, "coarse_solve");
+}
+
+
+// ----------------------------------------------------------------------------
+// The dissected factor and solve: layout, plans and launch sequences.
+
+static void nd_layout(tp_ctx* c) {
+  Coarse& C = c->coarse;
+  C.nd_ok = false;
+  const Level& L = c->L[c->nl - 1];
+  const int xs = (L.nx - 1) / 2;
+  if (xs < 1 || L.nx - 1 - xs < 1) return;
+  const long plane = 3L * L.ny * L.nz;
+  const long na = plane * xs, nb = plane * (L.nx - 1 - xs);
+  C.nd_xs = xs;
+  C.nd_ns = plane;
+  C.nd_pad[0] = (32 - na % 32) % 32;
+  C.nd_pad[1] = (32 - nb % 32) % 32;
+  C.nd_own[0] = C.nd_pad[0] + na;
+  C.nd_own[1] = C.nd_pad[1] + nb;
+  C.nd_own[2] = plane;
+  C.nd_org[0] = 0;
+  C.nd_org[1] = C.nd_own[0] + plane;
+  C.nd_org[2] = C.nd_org[1] + C.nd_own[1] + plane;
+  C.nd_ntot = C.nd_org[2] + plane;
+  int b0 = 0;
+  for (int v = 0; v < 3; v++) {
+    C.nd_blk0[v] = b0;
+    C.nd_nblk[v] = (int)((C.nd_own[v] + C.nbs - 1) / C.nbs);
+    b0 += C.nd_nblk[v];
+  }
+  // two steps per partial factor and two tiles of S at least; the natural
+  // half bandwidth (it holds the mirrored couplings and S x S); both halves
+  // of the grid with several CTAs
+  const long bw_nat = 3L * ((long)L.nz * L.ny + L.ny + 1) + 2;
+  if (C.nd_own[0] / 32 < 2 || C.nd_own[1] / 32 < 2 || plane < 64 || C.bw != bw_nat || plane - 1 > C.bw ||
+      C.nsm < 8 || C.nd_ntot >= (1L << 31))
+    return;
+  C.nd_ok = true;
+}
+
+static void nd_plan(tp_ctx* c) {
+  Coarse& C = c->coarse;
+  if (!C.nd_ok) return;
+  C.nd_ok = false;
+  if (!C.pf_ok || C.ps_grid <= 0 || !pf_fits()) return;
+  PsPlan p2;
+  if (!ps_plan_rows(2L * C.nbs, C.bw, C.nbs, C.nsm, p2)) return;
+  const Level& L = c->L[c->nl - 1];
+  const long ns = C.nd_ns;
+  std::vector<long> offs[3];
+  long nflags = 0, nrpk = 0, noff = 0;
+  for (int v = 0; v < 3; v++) {
+    const long nview = v < 2 ? C.nd_own[v] + ns : ns;
+    const long NT = v < 2 ? C.nd_own[v] / 32 : (ns + 31) / 32;
+    const long TS = pf_items(nview, C.bw, NT, offs[v]);
+    C.nd_NT[v] = (int)NT;
+    C.nd_TS[v] = (int)TS;
+    C.nd_fo[v] = nflags;
+    // tver has a row per tile of the view: the partial factors update the
+    // tiles of the trailing block too (rows NT .. tiles-1)
+    const long tiles = (nview + 31) / 32;
+    nflags += NT + NT * TS + tiles * TS;
+    C.nd_ro[v] = nrpk;
+    nrpk += NT;
+    C.nd_io[v] = noff;
+    noff += NT + 1;
+  }
+  nflags += 1;  // the abort flag of all three factors
+  C.nd_flag_bytes = sizeof(int) * (size_t)nflags;
+  // the CTAs of the concurrent partial factors, in proportion to their rows
+  const double fa = (double)C.nd_own[0] / (double)(C.nd_own[0] + C.nd_own[1]);
+  C.nd_split = (int)std::min((long)C.nsm - 2, std::max(2L, std::lround(fa * C.nsm)));
+  // composite row -> natural row
+  std::vector<int> map(C.nd_ntot, -1);
+  for (long r = C.nd_pad[0]; r < C.nd_own[0]; r++) map[r] = (int)(r - C.nd_pad[0]);
+  for (int p = C.nd_xs + 1; p < L.nx; p++)
+    for (int k = 0; k < L.nz; k++)
+      for (int j = 0; j < L.ny; j++)
+        for (int q = 0; q < 3; q++)
+          map[C.nd_org[1] + nd_pos_b(p, k, j, q, L.nx, L.ny, L.nz, C.nd_pad[1])] =
+              (int)(3L * (((long)p * L.nz + k) * L.ny + j) + q);
+  for (long r = 0; r < ns; r++) map[C.nd_org[2] + r] = (int)(C.nd_xs * ns + r);
+  std::vector<long> off_all;
+  for (int v = 0; v < 3; v++) off_all.insert(off_all.end(), offs[v].begin(), offs[v].end());
+  if (dev_malloc(&C.nd_map, sizeof(int) * C.nd_ntot) != cudaSuccess ||
+      dev_malloc(&C.nd_vec, sizeof(double) * 32 * C.nd_ntot) != cudaSuccess ||
+      dev_malloc(&C.nd_tail, sizeof(double) * 2 * ns * C.bw) != cudaSuccess ||
+      dev_malloc(&C.nd_flags, C.nd_flag_bytes) != cudaSuccess ||
+      dev_malloc(&C.nd_rpk, sizeof(double) * nrpk * NB) != cudaSuccess ||
+      dev_malloc(&C.nd_off, sizeof(long) * noff) != cudaSuccess) {
+    cudaGetLastError();
+    C.alloc_failed = true;
+    return;
+  }
+  cudaMemcpy(C.nd_map, map.data(), sizeof(int) * C.nd_ntot, cudaMemcpyHostToDevice);
+  cudaMemcpy(C.nd_off, off_all.data(), sizeof(long) * noff, cudaMemcpyHostToDevice);
+  c->mem_bytes += (long)(4 * C.nd_ntot + 8 * 32 * C.nd_ntot + 16 * ns * C.bw + (long)C.nd_flag_bytes +
+                         8 * nrpk * NB + 8 * noff);
+  C.ps2_R = p2.R;
+  C.ps2_P = p2.P;
+  C.ps2_seg = p2.seg;
+  C.ps2_grid = p2.grid;
+  C.ps2_smem = p2.smem;
+  C.nd_ok = true;
+}
+
+static PfArgs nd_args(const Coarse& C, int v, int cta0, int ncta) {
+  int* f = C.nd_flags + C.nd_fo[v];
+  const long NT = C.nd_NT[v], TS = C.nd_TS[v];
+  return PfArgs{C.band + C.nd_org[v] * (C.bw + 1),
+                C.bw,
+                v < 2 ? C.nd_own[v] + C.nd_ns : C.nd_ns,
+                (int)NT,
+                (int)TS,
+                C.nd_rpk + C.nd_ro[v] * NB,
+                f,
+                f + NT,
+                f + NT + NT * TS,
+                C.nd_off + C.nd_io[v],
+                C.info,
+                C.nd_flags + C.nd_flag_bytes / sizeof(int) - 1,
+                C.ps_spin > 0 ? C.ps_spin : kBarrierSpin,
+                cta0,
+                ncta,
+                v < 2 ? 1 : 0};
+}
+
+static void nd_pf_launch(tp_ctx* c, const PfArgs& a0, const PfArgs& a1) {
+  Coarse& C = c->coarse;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)C.nsm);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = kPfSmem;
+  cfg.stream = c->s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, C.ds ? pf_kernel<Dsf> : pf_kernel<double>, a0, a1);
+}
+
+// partial factors of A and B (one launch), S = the sum of their trailing
+// blocks, S's factor, then the block inverses and block rows of each view
+// and the tails' rows
+static void nd_factor_launches(tp_ctx* c, size_t dinv_smem) {
+  Coarse& C = c->coarse;
+  const long ns = C.nd_ns, bw = C.bw;
+  cudaMemsetAsync(C.info, 0, sizeof(int), c->s);
+  cudaMemsetAsync(C.nd_flags, 0, C.nd_flag_bytes, c->s);
+  nd_pf_launch(c, nd_args(C, 0, 0, C.nd_split), nd_args(C, 1, C.nd_split, C.nsm - C.nd_split));
+  nd_schur_kernel<<<grid_for(ns * ns, 256), 256, 0, c->s>>>(C.band, bw, ns, C.nd_own[0], C.nd_org[1], C.nd_own[1],
+                                                           C.nd_org[2]);
+  PfArgs s = nd_args(C, 2, 0, C.nsm), none = s;
+  none.cta0 = C.nsm;
+  nd_pf_launch(c, s, none);
+  for (int v = 0; v < 3; v++) {
+    const double* Bv = C.band + C.nd_org[v] * (bw + 1);
+    (C.ds ? dinv_kernel<Dsf> : dinv_kernel<double>)<<<dim3(C.nd_nblk[v], C.nbs / 32), kDinvThreads, dinv_smem,
+                                                      c->s>>>(Bv, bw, C.nd_own[v], C.nbs,
+                                                              C.dinv + (size_t)C.nd_blk0[v] * C.nbs * C.nbs,
+                                                              C.dinvT + (size_t)C.nd_blk0[v] * C.nbs * C.nbs);
+    lrow_kernel<<<dim3((unsigned)((bw + 31) / 32), C.nbs / 32, C.nd_nblk[v]), dim3(32, 8), 0, c->s>>>(
+        Bv, bw, C.nd_own[v], C.nbs, C.lrow + (size_t)C.nd_blk0[v] * C.nbs * bw);
+  }
+  for (int v = 0; v < 2; v++)
+    lrow_kernel<<<dim3((unsigned)((bw + 31) / 32), (unsigned)((ns + 31) / 32), 1), dim3(32, 8), 0, c->s>>>(
+        C.band + C.nd_org[v] * (bw + 1), bw, C.nd_own[v] + ns, (int)ns, C.nd_tail + v * ns * bw, C.nd_own[v]);
+}
+
+static PsView nd_view(const Coarse& C, int v) {
+  const size_t b0 = (size_t)C.nd_blk0[v];
+  return PsView{C.lrow + b0 * C.nbs * C.bw,
+                C.band + C.nd_org[v] * (C.bw + 1),
+                C.dinv + b0 * C.nbs * C.nbs,
+                C.dinvT + b0 * C.nbs * C.nbs,
+                C.nd_own[v],
+                v < 2 ? C.nd_own[v] + C.nd_ns : C.nd_ns,
+                C.nd_org[v],
+                C.nd_nblk[v]};
+}
+
+// one solve of NR columns (n apart) from rhs into x: forward sweeps of A
+// and B (one launch, both views in every phase), b_S -= L_SA y_A + L_SB y_B,
+// S forward and backward, x_S into the tails, backward sweeps of A and B
+template <int NR>
+static void nd_solve_launches(tp_ctx* c, const double* rhs, double* x) {
+  Coarse& C = c->coarse;
+  const long vn = C.nd_ntot, ns = C.nd_ns;
+  double *rb = C.nd_vec, *y = rb + 8 * vn, *t = y + 8 * vn, *xc = t + 8 * vn;
+  nd_gather_kernel<<<grid_for(vn * NR, 256), 256, 0, c->s>>>(C.nd_map, vn, rhs, C.n, rb, NR);
+  const PsView va = nd_view(C, 0), vb = nd_view(C, 1), vs = nd_view(C, 2);
+  const int m = std::max(C.nd_nblk[0], C.nd_nblk[1]);
+  ps_launch_views<NR>(c, va, vb, 2, vn, m, 1, 0, ps_nfwd(m), C.ps2_R, C.ps2_P, C.ps2_seg, C.ps2_grid, C.ps2_smem, rb,
+                      y, t, xc);
+  nd_couple_kernel<NR><<<grid_for(ns * 32, 256), 256, 0, c->s>>>(C.nd_tail, C.nd_tail + ns * C.bw, C.bw, ns,
+                                                                 C.nd_own[0], C.nd_org[0], C.nd_own[1], C.nd_org[1],
+                                                                 C.nd_org[2], vn, y, rb);
+  ps_launch_views<NR>(c, vs, vs, 1, vn, C.nd_nblk[2], 0, 0, ps_nall(C.nd_nblk[2], 0), C.ps_R, C.ps_P, C.ps_seg,
+                      C.ps_grid, C.ps_smem, rb, y, t, xc);
+  nd_tails_kernel<<<grid_for(ns * NR, 256), 256, 0, c->s>>>(xc, ns, vn, C.nd_org[0] + C.nd_own[0],
+                                                           C.nd_org[1] + C.nd_own[1], C.nd_org[2], NR);
+  ps_launch_views<NR>(c, va, vb, 2, vn, m, 1, ps_nfwd(m), ps_nall(m, 1), C.ps2_R, C.ps2_P, C.ps2_seg, C.ps2_grid,
+                      C.ps2_smem, rb, y, t, xc);
+  nd_scatter_out_kernel<<<grid_for(vn * NR, 256), 256, 0, c->s>>>(C.nd_map, vn, xc, C.n, x, NR);
+}
+
+static void nd_solve(tp_ctx* c, const double* rhs, double* x, int nr) {
+  Coarse& C = c->coarse;
+  if (nr > 1 || c->capturing) {
+    for (int r0 = 0; r0 < nr;) {
+      const double* b = rhs + (long)r0 * C.n;
+      double* xx = x + (long)r0 * C.n;
+      const int left = nr - r0;
+      if (left >= 8) {
+        nd_solve_launches<8>(c, b, xx);
+        r0 += 8;
+      } else if (left >= 4) {
+        nd_solve_launches<4>(c, b, xx);
+        r0 += 4;
+      } else if (left >= 2) {
+        nd_solve_launches<2>(c, b, xx);
+        r0 += 2;
+      } else {
+        nd_solve_launches<1>(c, b, xx);
+        r0 += 1;
+      }
+    }
+    TP_CHECK_LAUNCH(c, "coarse_solve");
+    return;
+  }
+  cudaMemcpyAsync(C.rhs, rhs, sizeof(double) * C.n, cudaMemcpyDeviceToDevice, c->s);
+  if (!C.nd_graph_exec) {
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      nd_solve_launches<1>(c, C.rhs, C.sol);
+      if (cudaStreamEndCapture(c->s, &g) == cudaSuccess && g) {
+        if (cudaGraphInstantiate(&C.nd_graph_exec, g, 0) != cudaSuccess) C.nd_graph_exec = nullptr;
+        cudaGraphDestroy(g);
+      }
+    }
+    cudaGetLastError();
+  }
+  if (C.nd_graph_exec)
+    cudaGraphLaunch(C.nd_graph_exec, c->s);
+  else
+    nd_solve_launches<1>(c, C.rhs, C.sol);
   cudaMemcpyAsync(x, C.sol, sizeof(double) * C.n, cudaMemcpyDeviceToDevice, c->s);
   TP_CHECK_LAUNCH(c, "coarse_solve");
 }

@@ -110,6 +110,38 @@ struct Coarse {
   size_t pf_flag_bytes = 0;
   double* pf_rpk = nullptr;     // [NT][32] reciprocal pivots per diagonal tile
   long* pf_off = nullptr;       // [NT+1] work items of the other CTAs before each step
+  // One level of nested dissection (x planes): the node plane xs is the
+  // separator S; part A (planes < xs, natural order) and part B (planes > xs,
+  // in mirrored plane order) are each a band with S as a trailing block,
+  // factored at the same time by halves of the grid up to S; S's Schur
+  // complement (the sum of the two trailing blocks) is then factored alone.
+  // Composite rows: view A [pad_a, A, S tail], view B [pad_b, B, S tail],
+  // view S; the band, block inverses and block rows share the arrays above.
+  int order = 1;                // requested: 0 natural band, 1 dissected where its plan applies
+  bool nd_ok = false;           // the dissected plan applies (sizes, launch plans)
+  bool nd_use = false;          // the current factor is the dissected one
+  int nd_xs = 0;                // separator plane
+  long nd_ns = 0;               // separator rows
+  long nd_own[3] = {0, 0, 0};   // rows in solve blocks per view (pad + part; S: ns)
+  long nd_org[3] = {0, 0, 0};   // first composite row of each view
+  long nd_pad[2] = {0, 0};      // identity rows ahead of A and B (own rows a multiple of 32)
+  int nd_nblk[3] = {0, 0, 0};   // solve blocks per view
+  int nd_blk0[3] = {0, 0, 0};   // first block of each view in dinv / lrow
+  long nd_ntot = 0;             // composite rows
+  int* nd_map = nullptr;        // [ntot] composite row -> natural row, -1 for pads and tails
+  double* nd_vec = nullptr;     // composite work columns: rhs, y, t, x, 8 columns each
+  double* nd_tail = nullptr;    // [2][ns][bw] rows of the A and B tails left of S, row-major
+  int nd_NT[3] = {0, 0, 0}, nd_TS[3] = {0, 0, 0};  // factor steps and flag row stride per view
+  int* nd_flags = nullptr;      // per view: fdone, sdone, tver; then the shared abort flag
+  size_t nd_flag_bytes = 0;
+  long nd_fo[3] = {0, 0, 0};    // offsets of each view's flags in nd_flags
+  double* nd_rpk = nullptr;     // per view [NT][32]
+  long* nd_off = nullptr;       // per view [NT+1] work items
+  long nd_ro[3] = {0, 0, 0}, nd_io[3] = {0, 0, 0};  // offsets into nd_rpk (tiles) and nd_off
+  int nd_split = 0;             // CTAs of the A group in the concurrent factor
+  int ps2_grid = 0, ps2_R = 0, ps2_P = 0, ps2_seg = 0;  // solve plan of two views per phase
+  size_t ps2_smem = 0;
+  cudaGraphExec_t nd_graph_exec = nullptr, nd_factor_exec = nullptr;
 };
 
 // Launch plan of the element-centric level-0 kernel (tp_kernels_fine_ec.cu):
@@ -354,6 +386,8 @@ void coarse_alloc(tp_ctx* c);
 void coarse_free(tp_ctx* c);
 void coarse_assemble(tp_ctx* c);  // from the FP64 stencil of level nl-1
 void coarse_factor(tp_ctx* c);
+void coarse_use_natural(tp_ctx* c);  // a caller's natural-order factor follows (tp_coarse_factor_csr)
+void coarse_graphs_free(tp_ctx* c);  // the captured factor and solve sequences
 void coarse_solve(tp_ctx* c, const double* rhs, double* x, int nr = 1);  // nr columns of ndof(nl-1)
 // TP_ERR_TIMEOUT (with the message set) if a single-launch solve gave up at a
 // grid barrier; synchronises the context's stream

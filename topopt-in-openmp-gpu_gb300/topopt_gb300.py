@@ -101,6 +101,7 @@ def load():
     L.tp_set_fine_arith.argtypes = [V, I]
     L.tp_set_coarse_arith.argtypes = [V, I]
     L.tp_set_coarse_solve_variant.argtypes = [V, I]
+    L.tp_set_coarse_order.argtypes = [V, I]
     L.tp_fault_coarse_barrier.argtypes = [V, ctypes.c_long, I]
     L.tp_autotune.argtypes = [V, P]
     L.tp_multiload.argtypes = [I, I, I, I, I, ctypes.c_ulonglong, P]
@@ -254,6 +255,10 @@ class TopOpt:
     def set_coarse_solve_variant(self, variant):
         """0: coarse triangular sweeps in one cooperative launch; 1: two launches per block step."""
         self._check(self.L.tp_set_coarse_solve_variant(self.ctx, variant))
+
+    def set_coarse_order(self, order):
+        """Coarsest-level elimination order: 0 natural band; 1 nested dissection (default)."""
+        self._check(self.L.tp_set_coarse_order(self.ctx, order))
 
     def fault_coarse_barrier(self, spin, missing):
         """Failure-detection hook: barrier waits give up after spin polls; missing=1 makes them run out."""

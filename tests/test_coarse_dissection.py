@@ -17,7 +17,8 @@ default), checked on the CPU (no GPU needed).
    blocks narrower than the band.
 2. The partial factors' schedule: pf_kernel runs NT = own / 32 steps of a
    view's band, on its share of the CTAs (nd_split). Replayed as in
-   test_coarse_schedule.py for the views of the grids the library is used on:
+   test_coarse_schedule.py for the views of the grids the library is used on
+   (two CTAs per SM, split between the views in proportion to their rows):
    every flag index stays inside its array (tver has a row per tile of the
    view, the trailing block's tiles included), every tile of the trailing
    block receives every step's update once and in order (the last one of
@@ -350,6 +351,7 @@ def test_partial_factor_schedule(grid, ds):
     own, ns, bw = Ly["own"], Ly["ns"], Ly["bw"]
     if own[0] // 32 < 2 or own[1] // 32 < 2 or ns < 64:
         pytest.skip("the natural band is used on this grid")
-    split = min(NSM - 2, max(2, round(own[0] / (own[0] + own[1]) * NSM)))  # nd_split
-    for v, ncta in ((0, split), (1, NSM - split)):
+    grid = 2 * NSM  # nd_grid: two CTAs per SM
+    split = min(grid - 2, max(2, round(own[0] / (own[0] + own[1]) * grid)))  # nd_split
+    for v, ncta in ((0, split), (1, grid - split)):
         replay_partial(own[v] + ns, bw, own[v] // 32, ncta - 1, ds)

@@ -597,7 +597,8 @@ __global__ void __launch_bounds__(256) syrk_rest_kernel(double* __restrict__ B, 
 }
 
 // ----------------------------------------------------------------------------
-// The whole factorisation as ONE cooperative launch, one CTA per SM. Tiles
+// The whole factorisation as ONE cooperative launch (one CTA per SM; two for
+// the dissected order's launches, kPfSmem2). Tiles
 // are the 32 x 32 blocks (I, J), I >= J, of the band; step k factors diagonal
 // tile k. The first CTA runs the chain every step waits on: factor tile (k,k), solve
 // the panel tile (k+1,k), apply step k's update to tile (k+1,k+1) -- which it
@@ -632,7 +633,17 @@ struct PfArgs {
   int partial;       // 1: NT steps leave a trailing block (rows 32 NT ..) with all their
                      //    updates, unfactored; tile (NT, NT) is stored by the chain
 };
-constexpr size_t kPfSmem = 120 * 1024;  // more than half an SM's shared memory: one CTA per SM
+// Shared memory of a factor CTA. The natural band's launch reserves more
+// than half an SM's, so that each SM runs one CTA and its one chain has an SM
+// to itself. The dissected order's two partial factors have chains of half
+// the length and are bound by the other CTAs' tile items instead: their
+// launch reserves what the double-single chain's buffers need, so two CTAs
+// share an SM (the registers, 128 x 256 each, allow two) and one CTA's item
+// overlaps the other's loads and waits (at 256x128x128: 20.5 -> 17.1 ms per
+// assembly; the natural band with two CTAs per SM: 21.0 ms).
+constexpr size_t kPfSmem = 120 * 1024;
+constexpr size_t kPfSmem2 = 68 * 1024;
+constexpr int kPfPerSm2 = 2;
 
 // last tile row of step k's panel (k itself: no panel)
 __host__ __device__ __forceinline__ long pf_imax(long n, long bw, long k) {
@@ -1126,6 +1137,7 @@ __device__ __forceinline__ void trsm_rows_ds(const Dsf (*Lm)[NB + 1], const Dsf*
 // smem offsets (in doubles) of the chain's and the other CTAs' buffers
 constexpr int kTile = NB * (NB + 1);  // a 32 x 33 tile of pairs
 constexpr int kPA = 2 * NB * NB, kPL = NB * NB;  // PA, PL; then QB (NB * NB doubles)
+static_assert((4 * kTile + NB + kPA + kPL + NB * NB) * sizeof(double) <= kPfSmem2, "chain buffers");
 
 // The chain CTA, step k: warps 0-3 factor tile (k,k), store it and release
 // fdone[k]; meanwhile warps 4-7 wait for and load the panel tile (k+1,k) and
@@ -1664,14 +1676,19 @@ static long pf_items(long n, long bw, long NT, std::vector<long>& off) {
   return TS;
 }
 
-static bool pf_fits() {
+// whether the factor launch fits with kPfSmem (one CTA per SM), and how
+// many CTAs per SM (up to two) it holds with kPfSmem2
+static bool pf_fits(int* per2) {
+  *per2 = kPfPerSm2;
   for (auto kern : {pf_kernel<double>, pf_kernel<Dsf>}) {
-    int per = 0;
+    int per = 0, p2 = 0;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPfSmem) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, 256, kPfSmem) != cudaSuccess || per < 1) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, 256, kPfSmem) != cudaSuccess || per < 1 ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p2, kern, 256, kPfSmem2) != cudaSuccess || p2 < 1) {
       cudaGetLastError();
       return false;
     }
+    *per2 = std::min(*per2, p2);
   }
   return true;
 }
@@ -1683,7 +1700,10 @@ static void pf_plan(tp_ctx* c) {
   if (NT < 2 || C.nsm < 2) return;
   std::vector<long> off;
   const long TS = pf_items(C.n, C.bw, NT, off);
-  if (!pf_fits()) return;
+  int per2 = 0;
+  if (!pf_fits(&per2)) return;
+  C.pf_grid = C.nsm;
+  C.nd_grid = per2 * C.nsm;
   C.pf_NT = (int)NT;
   C.pf_TS = (int)TS;
   C.pf_flag_bytes = sizeof(int) * (size_t)(NT + 2 * NT * TS + 1);
@@ -1704,15 +1724,15 @@ static void pf_launch(tp_ctx* c) {
   const long NT = C.pf_NT, TS = C.pf_TS;
   int* f = C.pf_flags;
   PfArgs a{C.band, C.bw, C.n, (int)NT, (int)TS, C.pf_rpk, f, f + NT, f + NT + NT * TS, C.pf_off, C.info,
-           f + NT + 2 * NT * TS, C.ps_spin > 0 ? C.ps_spin : kBarrierSpin, 0, C.nsm, 0};
+           f + NT + 2 * NT * TS, C.ps_spin > 0 ? C.ps_spin : kBarrierSpin, 0, C.pf_grid, 0};
   PfArgs none = a;
-  none.cta0 = C.nsm;
+  none.cta0 = C.pf_grid;
   cudaMemsetAsync(C.pf_flags, 0, C.pf_flag_bytes, c->s);
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeCooperative;
   at[0].val.cooperative = 1;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)C.nsm);
+  cfg.gridDim = dim3((unsigned)C.pf_grid);
   cfg.blockDim = dim3(256);
   cfg.dynamicSmemBytes = kPfSmem;
   cfg.stream = c->s;
@@ -2395,7 +2415,7 @@ static void nd_plan(tp_ctx* c) {
   Coarse& C = c->coarse;
   if (!C.nd_ok) return;
   C.nd_ok = false;
-  if (!C.pf_ok || C.ps_grid <= 0 || !pf_fits()) return;
+  if (!C.pf_ok || C.ps_grid <= 0) return;
   PsPlan p2;
   if (!ps_plan_rows(2L * C.nbs, C.bw, C.nbs, C.nsm, p2)) return;
   const Level& L = c->L[c->nl - 1];
@@ -2422,7 +2442,7 @@ static void nd_plan(tp_ctx* c) {
   C.nd_flag_bytes = sizeof(int) * (size_t)nflags;
   // the CTAs of the concurrent partial factors, in proportion to their rows
   const double fa = (double)C.nd_own[0] / (double)(C.nd_own[0] + C.nd_own[1]);
-  C.nd_split = (int)std::min((long)C.nsm - 2, std::max(2L, std::lround(fa * C.nsm)));
+  C.nd_split = (int)std::min((long)C.nd_grid - 2, std::max(2L, std::lround(fa * C.nd_grid)));
   // composite row -> natural row
   std::vector<int> map(C.nd_ntot, -1);
   for (long r = C.nd_pad[0]; r < C.nd_own[0]; r++) map[r] = (int)(r - C.nd_pad[0]);
@@ -2484,9 +2504,9 @@ static void nd_pf_launch(tp_ctx* c, const PfArgs& a0, const PfArgs& a1) {
   at[0].id = cudaLaunchAttributeCooperative;
   at[0].val.cooperative = 1;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)C.nsm);
+  cfg.gridDim = dim3((unsigned)C.nd_grid);
   cfg.blockDim = dim3(256);
-  cfg.dynamicSmemBytes = kPfSmem;
+  cfg.dynamicSmemBytes = kPfSmem2;
   cfg.stream = c->s;
   cfg.attrs = at;
   cfg.numAttrs = 1;
@@ -2501,11 +2521,11 @@ static void nd_factor_launches(tp_ctx* c, size_t dinv_smem) {
   const long ns = C.nd_ns, bw = C.bw;
   cudaMemsetAsync(C.info, 0, sizeof(int), c->s);
   cudaMemsetAsync(C.nd_flags, 0, C.nd_flag_bytes, c->s);
-  nd_pf_launch(c, nd_args(C, 0, 0, C.nd_split), nd_args(C, 1, C.nd_split, C.nsm - C.nd_split));
+  nd_pf_launch(c, nd_args(C, 0, 0, C.nd_split), nd_args(C, 1, C.nd_split, C.nd_grid - C.nd_split));
   nd_schur_kernel<<<grid_for(ns * ns, 256), 256, 0, c->s>>>(C.band, bw, ns, C.nd_own[0], C.nd_org[1], C.nd_own[1],
                                                            C.nd_org[2]);
-  PfArgs s = nd_args(C, 2, 0, C.nsm), none = s;
-  none.cta0 = C.nsm;
+  PfArgs s = nd_args(C, 2, 0, C.nd_grid), none = s;
+  none.cta0 = C.nd_grid;
   nd_pf_launch(c, s, none);
   for (int v = 0; v < 3; v++) {
     const double* Bv = C.band + C.nd_org[v] * (bw + 1);

@@ -105,6 +105,7 @@ struct Coarse {
   int ds = 0;                   // single-launch factor and block inverses in double-single arithmetic
   // single-launch factor (one cooperative kernel for all 32-column steps)
   bool pf_ok = false;
+  int pf_grid = 0;              // its CTAs (one per SM)
   int pf_NT = 0, pf_TS = 0;     // diagonal tiles; row stride of its flag arrays
   int* pf_flags = nullptr;      // fdone [NT], sdone [NT][TS], tver [NT][TS], abort [1]
   size_t pf_flag_bytes = 0;
@@ -138,6 +139,7 @@ struct Coarse {
   double* nd_rpk = nullptr;     // per view [NT][32]
   long* nd_off = nullptr;       // per view [NT+1] work items
   long nd_ro[3] = {0, 0, 0}, nd_io[3] = {0, 0, 0};  // offsets into nd_rpk (tiles) and nd_off
+  int nd_grid = 0;              // CTAs of the dissected factor's launches (two per SM)
   int nd_split = 0;             // CTAs of the A group in the concurrent factor
   int ps2_grid = 0, ps2_R = 0, ps2_P = 0, ps2_seg = 0;  // solve plan of two views per phase
   size_t ps2_smem = 0;

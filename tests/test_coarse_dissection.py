@@ -18,7 +18,8 @@ default), checked on the CPU (no GPU needed).
 2. The partial factors' schedule: pf_kernel runs NT = own / 32 steps of a
    view's band, on its share of the CTAs (nd_split). Replayed as in
    test_coarse_schedule.py for the views of the grids the library is used on
-   (two CTAs per SM, split between the views in proportion to their rows):
+   (three CTAs per SM in double-single, two in FP64, split between the
+   views in proportion to their rows):
    every flag index stays inside its array (tver has a row per tile of the
    view, the trailing block's tiles included), every tile of the trailing
    block receives every step's update once and in order (the last one of
@@ -351,7 +352,7 @@ def test_partial_factor_schedule(grid, ds):
     own, ns, bw = Ly["own"], Ly["ns"], Ly["bw"]
     if own[0] // 32 < 2 or own[1] // 32 < 2 or ns < 64:
         pytest.skip("the natural band is used on this grid")
-    grid = 2 * NSM  # nd_grid: two CTAs per SM
+    grid = (3 if ds else 2) * NSM  # nd_grid: three CTAs per SM in double-single, two in FP64
     split = min(grid - 2, max(2, round(own[0] / (own[0] + own[1]) * grid)))  # nd_split
     for v, ncta in ((0, split), (1, grid - split)):
         replay_partial(own[v] + ns, bw, own[v] // 32, ncta - 1, ds)

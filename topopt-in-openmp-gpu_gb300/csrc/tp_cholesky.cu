@@ -643,7 +643,14 @@ struct PfArgs {
 // assembly; the natural band with two CTAs per SM: 21.0 ms).
 constexpr size_t kPfSmem = 120 * 1024;
 constexpr size_t kPfSmem2 = 68 * 1024;
-constexpr int kPfPerSm2 = 2;
+constexpr int kPfPerSm2 = 3;
+// CTAs per SM the factor kernel's registers are sized for (pf_kernel's MB):
+// 2 gives 128 per thread; 3 gives 80 (a few spilled bytes), so that three
+// CTAs of the dissected double-single factor share an SM (16.4 -> 16.0 ms per
+// assembly at 256x128x128; the natural band's chain slows down with the cap,
+// 20.5 -> 23.2 ms, so its launch keeps 128)
+template <typename V>
+constexpr int kPfMinBlocksNd = std::is_same<V, Dsf>::value ? 3 : 2;
 
 // last tile row of step k's panel (k itself: no panel)
 __host__ __device__ __forceinline__ long pf_imax(long n, long bw, long k) {
@@ -1333,8 +1340,8 @@ __device__ __forceinline__ void pf_run(const PfArgs& a, double* sm) {
 
 // one factor (a1.cta0 >= gridDim.x) or two independent ones, the CTAs below
 // a1.cta0 on a0 and the others on a1
-template <typename V>
-__global__ void __launch_bounds__(256) pf_kernel(PfArgs a0, PfArgs a1) {
+template <typename V, int MB>
+__global__ void __launch_bounds__(256, MB) pf_kernel(PfArgs a0, PfArgs a1) {
   extern __shared__ double sm[];
   if ((int)blockIdx.x < a1.cta0)
     pf_run<V>(a0, sm);
@@ -1350,19 +1357,29 @@ __global__ void __launch_bounds__(256) pf_kernel(PfArgs a0, PfArgs a1) {
 // The tiles L_RS of a row chunk are loaded into registers one tile ahead, so
 // a tile's product does not wait on its load. blockIdx.x is the block and
 // blockIdx.y the chunk: CTAs go out chunk by chunk, the heaviest (chunk 0,
-// nR(nR-1)/2 tile products) first, so the last wave holds the lightest.
+// nR(nR-1)/2 tile products) first, so the last wave holds the lightest. The
+// blocks of up to three bands (the dissected order's views) go in one launch:
+// a launch takes as long as its heaviest CTAs, whatever its block count.
 constexpr int kDinvThreads = 256;
+
+struct DinvBands {
+  const double* B[3];  // the bands (origin at their first row)
+  long n[3];           // rows in blocks
+  int blk0[3];         // first block of each band; blocks are numbered across the bands
+};
 
 template <typename V>
 __global__ void __launch_bounds__(kDinvThreads)
-    dinv_kernel(const double* __restrict__ B, long bw, long n, int nbs, double* __restrict__ D,
-                double* __restrict__ DT) {
+    dinv_kernel(DinvBands bands, long bw, int nbs, double* __restrict__ D, double* __restrict__ DT) {
   extern __shared__ double smem_d[];
   V* X = reinterpret_cast<V*>(smem_d);  // nbs x 33
   V* Lt = X + (long)nbs * 33;           // 32 x 33
   V* Acc = Lt + 32 * 33;                // the chunk's 32 reciprocal pivots
   const int blk = blockIdx.x, cc = blockIdx.y, tid = threadIdx.x;
-  const long b0 = (long)blk * nbs;
+  const int v = blk >= bands.blk0[2] ? 2 : (blk >= bands.blk0[1] ? 1 : 0);
+  const double* B = v == 2 ? bands.B[2] : (v == 1 ? bands.B[1] : bands.B[0]);
+  const long n = v == 2 ? bands.n[2] : (v == 1 ? bands.n[1] : bands.n[0]);
+  const long b0 = (long)(blk - (v == 2 ? bands.blk0[2] : (v == 1 ? bands.blk0[1] : 0))) * nbs;
   const int s = (int)lmin((long)nbs, n - b0);
   const int j0 = cc * 32;
   double* Db = D + (long)blk * nbs * nbs;
@@ -1566,8 +1583,10 @@ __global__ void nd_scatter_out_kernel(const int* __restrict__ map, long ntot, co
 }
 
 // b_S -= L_SA y_A + L_SB y_B, one warp per row of S; the tails' rows are
-// row-major (tail[s][e] = L(own + s, own - bw + e)), each lane sums its
-// positions in order, then the warp in a fixed tree
+// row-major (tail[s][e] = L(own + s, own - bw + e)). Each lane sums its
+// positions in order into four accumulators (position e to accumulator
+// (e / 32) % 4, so four loads are in flight), which it then adds in a fixed
+// order; then the warp in a fixed tree.
 template <int NR>
 __global__ void nd_couple_kernel(const double* __restrict__ tail_a, const double* __restrict__ tail_b, long bw,
                                  long ns, long own_a, long org_a, long own_b, long org_b, long org_s, long vn,
@@ -1575,22 +1594,31 @@ __global__ void nd_couple_kernel(const double* __restrict__ tail_a, const double
   const long s = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (s >= ns) return;
-  double acc[NR];
+  double acc[4][NR];
 #pragma unroll
-  for (int v = 0; v < NR; v++) acc[v] = 0.0;
+  for (int u = 0; u < 4; u++)
+#pragma unroll
+    for (int v = 0; v < NR; v++) acc[u][v] = 0.0;
   for (int part = 0; part < 2; part++) {
     const double* L = (part == 0 ? tail_a : tail_b) + s * bw;
     const long own = part == 0 ? own_a : own_b, org = part == 0 ? org_a : org_b;
     const double* yy = y + org + own - bw;  // column own - bw + e of the view
-    for (long e = lmax(s, bw - own) + lane; e < bw; e += 32) {
-      const double l = L[e];
+    const long e0 = lmax(s, bw - own);
+    for (long e = e0 + lane; e < bw; e += 128) {
 #pragma unroll
-      for (int v = 0; v < NR; v++) acc[v] += l * yy[v * vn + e];
+      for (int u = 0; u < 4; u++) {
+        const long eu = e + 32 * u;
+        if (eu < bw) {
+          const double l = L[eu];
+#pragma unroll
+          for (int v = 0; v < NR; v++) acc[u][v] += l * yy[v * vn + eu];
+        }
+      }
     }
   }
 #pragma unroll
   for (int v = 0; v < NR; v++) {
-    const double sv = wsum(acc[v]);
+    const double sv = wsum((acc[0][v] + acc[1][v]) + (acc[2][v] + acc[3][v]));
     if (lane == 0) rhs[v * vn + org_s + s] -= sv;
   }
 }
@@ -1678,17 +1706,25 @@ static long pf_items(long n, long bw, long NT, std::vector<long>& off) {
 
 // whether the factor launch fits with kPfSmem (one CTA per SM), and how
 // many CTAs per SM (up to two) it holds with kPfSmem2
-static bool pf_fits(int* per2) {
-  *per2 = kPfPerSm2;
-  for (auto kern : {pf_kernel<double>, pf_kernel<Dsf>}) {
-    int per = 0, p2 = 0;
+static bool pf_fits(int per2[2]) {
+  for (auto kern : {pf_kernel<double, 2>, pf_kernel<Dsf, 2>}) {
+    int per = 0;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPfSmem) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, 256, kPfSmem) != cudaSuccess || per < 1 ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, 256, kPfSmem) != cudaSuccess || per < 1) {
+      cudaGetLastError();
+      return false;
+    }
+  }
+  int q = 0;
+  for (auto kern : {pf_kernel<double, kPfMinBlocksNd<double>>, pf_kernel<Dsf, kPfMinBlocksNd<Dsf>>}) {
+    int p2 = 0;
+    // (the attribute is the larger size: the FP64 kernel serves both launches)
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPfSmem) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p2, kern, 256, kPfSmem2) != cudaSuccess || p2 < 1) {
       cudaGetLastError();
       return false;
     }
-    *per2 = std::min(*per2, p2);
+    per2[q++] = std::min(kPfPerSm2, p2);
   }
   return true;
 }
@@ -1700,10 +1736,11 @@ static void pf_plan(tp_ctx* c) {
   if (NT < 2 || C.nsm < 2) return;
   std::vector<long> off;
   const long TS = pf_items(C.n, C.bw, NT, off);
-  int per2 = 0;
-  if (!pf_fits(&per2)) return;
+  int per2[2] = {0, 0};
+  if (!pf_fits(per2)) return;
   C.pf_grid = C.nsm;
-  C.nd_grid = per2 * C.nsm;
+  C.nd_grid[0] = per2[0] * C.nsm;
+  C.nd_grid[1] = per2[1] * C.nsm;
   C.pf_NT = (int)NT;
   C.pf_TS = (int)TS;
   C.pf_flag_bytes = sizeof(int) * (size_t)(NT + 2 * NT * TS + 1);
@@ -1738,7 +1775,7 @@ static void pf_launch(tp_ctx* c) {
   cfg.stream = c->s;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, C.ds ? pf_kernel<Dsf> : pf_kernel<double>, a, none);
+  cudaLaunchKernelEx(&cfg, C.ds ? pf_kernel<Dsf, 2> : pf_kernel<double, 2>, a, none);
 }
 
 static void coarse_factor_launches(tp_ctx* c, size_t dinv_smem) {
@@ -1748,8 +1785,9 @@ static void coarse_factor_launches(tp_ctx* c, size_t dinv_smem) {
     pf_launch(c);
   else
     step_launches(c);
+  const DinvBands one{{C.band, C.band, C.band}, {C.n, C.n, C.n}, {0, C.nblk, C.nblk}};
   (C.ds ? dinv_kernel<Dsf> : dinv_kernel<double>)<<<dim3(C.nblk, C.nbs / 32), kDinvThreads, dinv_smem, c->s>>>(
-      C.band, C.bw, C.n, C.nbs, C.dinv, C.dinvT);
+      one, C.bw, C.nbs, C.dinv, C.dinvT);
   lrow_kernel<<<dim3((unsigned)((C.bw + 31) / 32), C.nbs / 32, C.nblk), dim3(32, 8), 0, c->s>>>(C.band, C.bw, C.n,
                                                                                                C.nbs, C.lrow);
 }
@@ -2188,19 +2226,20 @@ __global__ void __launch_bounds__(kPsWarps * 32) ps_solve_kernel(PsArgs a) {
 }
 
 // Launch plan for phases of `rows` rows: R rows per CTA (1, 2, 4 or 8), the
-// fewest that keep one CTA per SM; P = 8/R warps per row; shared memory for
-// two stages of every warp's longest part. false if the stages do not fit or
-// the grid cannot be co-resident.
+// fewest that keep at most per_sm CTAs per SM; P = 8/R warps per row; shared
+// memory for two stages of every warp's longest part. false if the stages do
+// not fit or the grid cannot be co-resident.
 struct PsPlan {
   int R = 0, P = 0, grid = 0, seg = 0;
   size_t smem = 0;
 };
-static bool ps_plan_rows(long rows, long bw, int nbs, int nsm, PsPlan& pl) {
+static bool ps_plan_rows(long rows, long bw, int nbs, int nsm, int per_sm, PsPlan& pl) {
   int R = 1;
-  while (R < kPsWarps && (rows + R - 1) / R > nsm) R *= 2;
+  while (R < kPsWarps && (rows + R - 1) / R > (long)per_sm * nsm) R *= 2;
   const int P = kPsWarps / R;
   const long grid = (rows + R - 1) / R;
-  if (grid > nsm) return false;
+  if (grid > (long)per_sm * nsm) return false;
+  const int need = (int)((grid + nsm - 1) / nsm);  // CTAs per SM
   const long seg = std::max((bw + P - 1) / P, (long)(nbs + P - 1) / P);
   const size_t smem = (size_t)(2 * kPsWarps * seg + kPsWarps * 8) * sizeof(double);
   if (smem > 200 * 1024) return false;
@@ -2211,7 +2250,7 @@ static bool ps_plan_rows(long rows, long bw, int nbs, int nsm, PsPlan& pl) {
     if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)attr) != cudaSuccess) return false;
     int per = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, kPsWarps * 32, smem) != cudaSuccess) return false;
-    return per >= 1;
+    return per >= need;
   };
   const bool ok = fits((const void*)ps_solve_kernel<1>) && fits((const void*)ps_solve_kernel<2>) &&
                   fits((const void*)ps_solve_kernel<4>) && fits((const void*)ps_solve_kernel<8>);
@@ -2231,7 +2270,7 @@ static void ps_plan(tp_ctx* c) {
   C.ps_grid = 0;
   if (!C.bar || C.nblk < 1) return;
   PsPlan pl;
-  if (!ps_plan_rows(C.nbs, C.bw, C.nbs, C.nsm, pl)) return;
+  if (!ps_plan_rows(C.nbs, C.bw, C.nbs, C.nsm, 1, pl)) return;
   C.ps_R = pl.R;
   C.ps_P = pl.P;
   C.ps_seg = pl.seg;
@@ -2417,7 +2456,9 @@ static void nd_plan(tp_ctx* c) {
   C.nd_ok = false;
   if (!C.pf_ok || C.ps_grid <= 0) return;
   PsPlan p2;
-  if (!ps_plan_rows(2L * C.nbs, C.bw, C.nbs, C.nsm, p2)) return;
+  // two views per phase: eight rows per CTA, one warp per row (two CTAs per
+  // SM of four rows each measured slower: 0.65 against 0.63 ms per solve)
+  if (!ps_plan_rows(2L * C.nbs, C.bw, C.nbs, C.nsm, 1, p2)) return;
   const Level& L = c->L[c->nl - 1];
   const long ns = C.nd_ns;
   std::vector<long> offs[3];
@@ -2442,7 +2483,8 @@ static void nd_plan(tp_ctx* c) {
   C.nd_flag_bytes = sizeof(int) * (size_t)nflags;
   // the CTAs of the concurrent partial factors, in proportion to their rows
   const double fa = (double)C.nd_own[0] / (double)(C.nd_own[0] + C.nd_own[1]);
-  C.nd_split = (int)std::min((long)C.nd_grid - 2, std::max(2L, std::lround(fa * C.nd_grid)));
+  for (int q = 0; q < 2; q++)
+    C.nd_split[q] = (int)std::min((long)C.nd_grid[q] - 2, std::max(2L, std::lround(fa * C.nd_grid[q])));
   // composite row -> natural row
   std::vector<int> map(C.nd_ntot, -1);
   for (long r = C.nd_pad[0]; r < C.nd_own[0]; r++) map[r] = (int)(r - C.nd_pad[0]);
@@ -2504,13 +2546,14 @@ static void nd_pf_launch(tp_ctx* c, const PfArgs& a0, const PfArgs& a1) {
   at[0].id = cudaLaunchAttributeCooperative;
   at[0].val.cooperative = 1;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)C.nd_grid);
+  cfg.gridDim = dim3((unsigned)C.nd_grid[C.ds ? 1 : 0]);
   cfg.blockDim = dim3(256);
   cfg.dynamicSmemBytes = kPfSmem2;
   cfg.stream = c->s;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, C.ds ? pf_kernel<Dsf> : pf_kernel<double>, a0, a1);
+  cudaLaunchKernelEx(&cfg, C.ds ? pf_kernel<Dsf, kPfMinBlocksNd<Dsf>> : pf_kernel<double, kPfMinBlocksNd<double>>, a0,
+                     a1);
 }
 
 // partial factors of A and B (one launch), S = the sum of their trailing
@@ -2521,21 +2564,24 @@ static void nd_factor_launches(tp_ctx* c, size_t dinv_smem) {
   const long ns = C.nd_ns, bw = C.bw;
   cudaMemsetAsync(C.info, 0, sizeof(int), c->s);
   cudaMemsetAsync(C.nd_flags, 0, C.nd_flag_bytes, c->s);
-  nd_pf_launch(c, nd_args(C, 0, 0, C.nd_split), nd_args(C, 1, C.nd_split, C.nd_grid - C.nd_split));
+  const int grid = C.nd_grid[C.ds ? 1 : 0], split = C.nd_split[C.ds ? 1 : 0];
+  nd_pf_launch(c, nd_args(C, 0, 0, split), nd_args(C, 1, split, grid - split));
   nd_schur_kernel<<<grid_for(ns * ns, 256), 256, 0, c->s>>>(C.band, bw, ns, C.nd_own[0], C.nd_org[1], C.nd_own[1],
                                                            C.nd_org[2]);
-  PfArgs s = nd_args(C, 2, 0, C.nd_grid), none = s;
-  none.cta0 = C.nd_grid;
+  PfArgs s = nd_args(C, 2, 0, grid), none = s;
+  none.cta0 = grid;
   nd_pf_launch(c, s, none);
+  DinvBands views;
   for (int v = 0; v < 3; v++) {
-    const double* Bv = C.band + C.nd_org[v] * (bw + 1);
-    (C.ds ? dinv_kernel<Dsf> : dinv_kernel<double>)<<<dim3(C.nd_nblk[v], C.nbs / 32), kDinvThreads, dinv_smem,
-                                                      c->s>>>(Bv, bw, C.nd_own[v], C.nbs,
-                                                              C.dinv + (size_t)C.nd_blk0[v] * C.nbs * C.nbs,
-                                                              C.dinvT + (size_t)C.nd_blk0[v] * C.nbs * C.nbs);
-    lrow_kernel<<<dim3((unsigned)((bw + 31) / 32), C.nbs / 32, C.nd_nblk[v]), dim3(32, 8), 0, c->s>>>(
-        Bv, bw, C.nd_own[v], C.nbs, C.lrow + (size_t)C.nd_blk0[v] * C.nbs * bw);
+    views.B[v] = C.band + C.nd_org[v] * (bw + 1);
+    views.n[v] = C.nd_own[v];
+    views.blk0[v] = C.nd_blk0[v];
   }
+  (C.ds ? dinv_kernel<Dsf> : dinv_kernel<double>)<<<dim3(C.nd_blk0[2] + C.nd_nblk[2], C.nbs / 32), kDinvThreads,
+                                                    dinv_smem, c->s>>>(views, bw, C.nbs, C.dinv, C.dinvT);
+  for (int v = 0; v < 3; v++)
+    lrow_kernel<<<dim3((unsigned)((bw + 31) / 32), C.nbs / 32, C.nd_nblk[v]), dim3(32, 8), 0, c->s>>>(
+        views.B[v], bw, C.nd_own[v], C.nbs, C.lrow + (size_t)C.nd_blk0[v] * C.nbs * bw);
   for (int v = 0; v < 2; v++)
     lrow_kernel<<<dim3((unsigned)((bw + 31) / 32), (unsigned)((ns + 31) / 32), 1), dim3(32, 8), 0, c->s>>>(
         C.band + C.nd_org[v] * (bw + 1), bw, C.nd_own[v] + ns, (int)ns, C.nd_tail + v * ns * bw, C.nd_own[v]);

@@ -139,8 +139,8 @@ struct Coarse {
   double* nd_rpk = nullptr;     // per view [NT][32]
   long* nd_off = nullptr;       // per view [NT+1] work items
   long nd_ro[3] = {0, 0, 0}, nd_io[3] = {0, 0, 0};  // offsets into nd_rpk (tiles) and nd_off
-  int nd_grid = 0;              // CTAs of the dissected factor's launches (two per SM)
-  int nd_split = 0;             // CTAs of the A group in the concurrent factor
+  int nd_grid[2] = {0, 0};      // CTAs of the dissected factor's launches, FP64 and double-single
+  int nd_split[2] = {0, 0};     // CTAs of the A group in the concurrent factor
   int ps2_grid = 0, ps2_R = 0, ps2_P = 0, ps2_seg = 0;  // solve plan of two views per phase
   size_t ps2_smem = 0;
   cudaGraphExec_t nd_graph_exec = nullptr, nd_factor_exec = nullptr;

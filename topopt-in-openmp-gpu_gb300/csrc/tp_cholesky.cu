@@ -24,11 +24,19 @@
 // is FP32, so the last bits of FP64 buy its coarse correction nothing, while
 // FP64 instructions hold the FP64 unit ~67 cycles each. Its factor kernel
 // (pf_chain_ds / pf_bulk_ds) is laid out for FP32 latency rather than FP64
-// throughput: at 256x128x128 it takes 18 ms per factorisation against 28 ms
-// for the same double-single operations in the FP64 layout (and 33 ms in
-// FP64), with the same result bit for bit; the inverses take 2.2 ms instead
-// of 5.2. The sweeps stay FP64: their phases wait on grid barriers and L2
-// reads, not on their few multiply-adds.
+// throughput: at 256x128x128 the natural band takes 15.6 ms per
+// factorisation against 28 ms for the same double-single operations in the
+// FP64 layout (and 33 ms in FP64), with the same result bit for bit. The
+// sweeps stay FP64: their phases wait on grid barriers and L2 reads, not on
+// their few multiply-adds.
+// By default the operator is eliminated in a one-level nested-dissection
+// order (the nd_* code at the end of this file): the middle x node plane
+// separates two halves whose partial band factors run in one launch, and
+// whose solve sweeps share the phases of one launch, which halves the solve's
+// chain of grid barriers (0.92 -> 0.63 ms per solve at 256x128x128); the
+// factor, bound by its tile items rather than its chain once the chains are
+// halved, runs two or three CTAs per SM (15.6 + 1.9 ms -> 11 + 0.8 ms for
+// the partial factors and the block inverses).
 #include <algorithm>
 #include <type_traits>
 

@@ -213,8 +213,10 @@ tp_status tp_set_coarse_arith(tp_ctx* c, int arith);
  * chain of 32-column steps each), then the separator's Schur complement, and
  * the solve sweeps both halves in the same phases. Order 1 applies with the
  * single-launch variant where the coarsest grid is large enough (otherwise
- * the natural band is used). The two orders agree to rounding; the factor is
- * redone at the next solve. */
+ * the natural band is used); where a solve phase of both halves does not fit
+ * the shared memory (wide bands), the halves are swept one after the other,
+ * and order 2 asks for that form everywhere. The orders agree to rounding;
+ * the factor is redone at the next solve. */
 tp_status tp_set_coarse_order(tp_ctx* c, int order);
 /* Failure detection of the single-launch coarse factor and solve (host-side
  * fault injection, for tests): each of their waits in global memory gives up

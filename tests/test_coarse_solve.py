@@ -141,7 +141,8 @@ def test_dissected_order_against_natural(cuda, shape):
     17 and 16 node planes, so halves of 8 and 8 and of 7 and 8 planes) against
     the natural band: the solutions agree to rounding but not bit for bit (so
     the dissected path ran), repeated solves agree bit for bit, and the
-    solution solves the system."""
+    solution solves the system; the form with the halves swept one after the
+    other gives the same solution to rounding."""
     torch = cuda
     ctx = tp.TopOpt(*shape, 3)
     try:
@@ -159,5 +160,11 @@ def test_dissected_order_against_natural(cuda, shape):
         assert 0 < relerr(s1, s0) < 1e-10
         back = ctx.apply(lc, _dev(torch, s1)).cpu().numpy()
         assert relerr(back, rhs) < 1e-8
+        # the same factor, the halves' sweeps one after the other (the form
+        # taken where a phase of both halves does not fit the shared memory)
+        ctx.set_coarse_order(2)
+        ctx.assemble()
+        s2 = ctx.coarse_solve(b).cpu().numpy()
+        assert relerr(s2, s1) < 1e-12
     finally:
         ctx.close()

@@ -98,7 +98,7 @@ tp_status tp_set_coarse_solve_variant(tp_ctx* c, int variant) {
 }
 
 tp_status tp_set_coarse_order(tp_ctx* c, int order) {
-  if (!c || order < 0 || order > 1) return TP_ERR_ARG;
+  if (!c || order < 0 || order > 2) return TP_ERR_ARG;
   c->coarse.order = order;
   coarse_reset(c);
   return TP_OK;

@@ -221,7 +221,7 @@ void coarse_assemble(tp_ctx* c) {
   Coarse& C = c->coarse;
   const int l = c->nl - 1;
   const Level& L = c->L[l];
-  const bool nd = C.nd_ok && C.order == 1 && C.solve_variant == 0;
+  const bool nd = C.nd_ok && C.order >= 1 && C.solve_variant == 0;
   if (nd != C.nd_use) {  // captured loops hold the other form's solve launches
     C.nd_use = nd;
     graph_free(c);
@@ -2465,8 +2465,11 @@ static void nd_plan(tp_ctx* c) {
   if (!C.pf_ok || C.ps_grid <= 0) return;
   PsPlan p2;
   // two views per phase: eight rows per CTA, one warp per row (two CTAs per
-  // SM of four rows each measured slower: 0.65 against 0.63 ms per solve)
-  if (!ps_plan_rows(2L * C.nbs, C.bw, C.nbs, C.nsm, 1, p2)) return;
+  // SM of four rows each measured slower: 0.65 against 0.63 ms per solve).
+  // Where a warp's staged row does not fit (wide bands: 1,955 at the
+  // coarsest level of 384x192x192), the halves are swept one after the
+  // other with the single-view plan (ps2_grid = 0).
+  if (!ps_plan_rows(2L * C.nbs, C.bw, C.nbs, C.nsm, 1, p2)) p2 = PsPlan();
   const Level& L = c->L[c->nl - 1];
   const long ns = C.nd_ns;
   std::vector<long> offs[3];
@@ -2618,8 +2621,19 @@ static void nd_solve_launches(tp_ctx* c, const double* rhs, double* x) {
   nd_gather_kernel<<<grid_for(vn * NR, 256), 256, 0, c->s>>>(C.nd_map, vn, rhs, C.n, rb, NR);
   const PsView va = nd_view(C, 0), vb = nd_view(C, 1), vs = nd_view(C, 2);
   const int m = std::max(C.nd_nblk[0], C.nd_nblk[1]);
-  ps_launch_views<NR>(c, va, vb, 2, vn, m, 1, 0, ps_nfwd(m), C.ps2_R, C.ps2_P, C.ps2_seg, C.ps2_grid, C.ps2_smem, rb,
-                      y, t, xc);
+  // both halves in every phase, or one half after the other
+  const bool two = C.ps2_grid > 0 && C.order != 2;
+  auto sweep = [&](bool fwd) {
+    if (two) {
+      ps_launch_views<NR>(c, va, vb, 2, vn, m, 1, fwd ? 0 : ps_nfwd(m), fwd ? ps_nfwd(m) : ps_nall(m, 1), C.ps2_R,
+                          C.ps2_P, C.ps2_seg, C.ps2_grid, C.ps2_smem, rb, y, t, xc);
+      return;
+    }
+    for (const PsView& v : {va, vb})
+      ps_launch_views<NR>(c, v, v, 1, vn, v.nblk, 1, fwd ? 0 : ps_nfwd(v.nblk), fwd ? ps_nfwd(v.nblk) : ps_nall(v.nblk, 1),
+                          C.ps_R, C.ps_P, C.ps_seg, C.ps_grid, C.ps_smem, rb, y, t, xc);
+  };
+  sweep(true);
   nd_couple_kernel<NR><<<grid_for(ns * 32, 256), 256, 0, c->s>>>(C.nd_tail, C.nd_tail + ns * C.bw, C.bw, ns,
                                                                  C.nd_own[0], C.nd_org[0], C.nd_own[1], C.nd_org[1],
                                                                  C.nd_org[2], vn, y, rb);
@@ -2627,8 +2641,7 @@ static void nd_solve_launches(tp_ctx* c, const double* rhs, double* x) {
                       C.ps_grid, C.ps_smem, rb, y, t, xc);
   nd_tails_kernel<<<grid_for(ns * NR, 256), 256, 0, c->s>>>(xc, ns, vn, C.nd_org[0] + C.nd_own[0],
                                                            C.nd_org[1] + C.nd_own[1], C.nd_org[2], NR);
-  ps_launch_views<NR>(c, va, vb, 2, vn, m, 1, ps_nfwd(m), ps_nall(m, 1), C.ps2_R, C.ps2_P, C.ps2_seg, C.ps2_grid,
-                      C.ps2_smem, rb, y, t, xc);
+  sweep(false);
   nd_scatter_out_kernel<<<grid_for(vn * NR, 256), 256, 0, c->s>>>(C.nd_map, vn, xc, C.n, x, NR);
 }
 

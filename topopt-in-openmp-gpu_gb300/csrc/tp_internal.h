@@ -118,7 +118,8 @@ struct Coarse {
   // complement (the sum of the two trailing blocks) is then factored alone.
   // Composite rows: view A [pad_a, A, S tail], view B [pad_b, B, S tail],
   // view S; the band, block inverses and block rows share the arrays above.
-  int order = 1;                // requested: 0 natural band, 1 dissected where its plan applies
+  int order = 1;                // requested: 0 natural band, 1 dissected where its plan applies,
+                                //   2 dissected with the halves' sweeps one after the other
   bool nd_ok = false;           // the dissected plan applies (sizes, launch plans)
   bool nd_use = false;          // the current factor is the dissected one
   int nd_xs = 0;                // separator plane

@@ -257,7 +257,8 @@ class TopOpt:
         self._check(self.L.tp_set_coarse_solve_variant(self.ctx, variant))
 
     def set_coarse_order(self, order):
-        """Coarsest-level elimination order: 0 natural band; 1 nested dissection (default)."""
+        """Coarsest-level elimination order: 0 natural band; 1 nested dissection (default);
+        2 nested dissection with the halves' sweeps one after the other."""
         self._check(self.L.tp_set_coarse_order(self.ctx, order))
 
     def fault_coarse_barrier(self, spin, missing):

@@ -217,13 +217,13 @@ void assemble_stencil(tp_ctx* c, int l, const T* E, const T* ke, T* st, double* 
     TP_CHECK_LAUNCH(c, "assemble_stencil");
     return;
   }
-  if (nsub >= 32) {
+  // 8 sub-cells per coarse element (level 1): one thread per node sums them
+  // in order; the lanes' shuffle reductions of the 8-lane form cost more
+  // instructions than the sums themselves
+  if (nsub >= 32)
     assemble_kernel<T, 32><<<grid_for(g.nnodes * 32, threads), threads, 0, c->s>>>(g, E, ke, st, invD);
-  } else if (nsub >= 8) {
-    assemble_kernel<T, 8><<<grid_for(g.nnodes * 8, threads), threads, 0, c->s>>>(g, E, ke, st, invD);
-  } else {
+  else
     assemble_kernel<T, 1><<<grid_for(g.nnodes, threads), threads, 0, c->s>>>(g, E, ke, st, invD);
-  }
   TP_CHECK_LAUNCH(c, "assemble_stencil");
 }
 template void assemble_stencil<double>(tp_ctx*, int, const double*, const double*, double*, double*);

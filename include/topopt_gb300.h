@@ -181,8 +181,8 @@ tp_status tp_set_fine_variant(tp_ctx* c, int variant);
  * counterpart in the reference): 0 = FP64; 1 = double-single, pairs of FP32
  * numbers with about 48 significant bits, each addition's error bounded by
  * ~2^-45 (|a| + |b|) instead of 2^-53 (|a| + |b|). The vectors stay FP64 in
- * memory. The default is 1 for TP_MIXED (its CG matvec and residual) and 0
- * for TP_FP64. Double-single has FP32's exponent range: vector entries of
+ * memory. The default is 1 for TP_MIXED (its CG matvec and residual, and the
+ * element energies of the compliance pass) and 0 for TP_FP64. Double-single has FP32's exponent range: vector entries of
  * magnitude below 2^-126 (1.2e-38) count as zero, above 2^128 as infinity
  * (which the solve then reports as TP_ERR_NONFINITE); select 0 for
  * right-hand sides scaled outside that range. */

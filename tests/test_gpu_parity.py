@@ -77,6 +77,30 @@ def test_compliance_and_sensitivity(case):
     assert relerr(s, g["dc"]) < OP_TOL
 
 
+def test_compliance_double_single(cuda):
+    """The mixed form forms the element energies of the compliance pass in
+    double-single arithmetic (about 48 bits): compliance and sensitivities
+    within 1e-11 of the reference's own FP64 values (golden fixture) and of
+    the FP64 pass on the same context (tp_set_fine_arith(0))."""
+    g = golden("kernels_32x16x16_l4.npz")
+    ctx = tp.TopOpt(32, 16, 16, 4, precision=tp.TP_MIXED)
+    try:
+        ctx.upload("xphys", g["x"])
+        ctx.upload("U", g["u_c"])
+        c_ds = ctx.compliance()
+        dc_ds = ctx.download("dc")
+        ctx.set_fine_arith(0)
+        c_64 = ctx.compliance()
+        dc_64 = ctx.download("dc")
+    finally:
+        ctx.close()
+    assert abs(c_ds - float(g["c"])) / abs(float(g["c"])) < 1e-11
+    assert relerr(dc_ds, g["dc"]) < 1e-11
+    assert abs(c_ds - c_64) / abs(c_64) < 1e-11
+    assert relerr(dc_ds, dc_64) < 1e-11
+    assert c_ds != c_64 or not np.array_equal(dc_ds, dc_64)  # a different arithmetic ran
+
+
 def test_filters(case):
     g, ctx, torch = case
     if abs(ctx.params.rmin - 1.5) > 0:

@@ -2,17 +2,21 @@
 // compliance and sensitivity (stencil_methods.c:808-862), the density filter
 // and its adjoint (stencil_optimization.c:228-395), the volume
 // (gpu_definitions.c:94-108) and the OC bisection with the change measure
-// (gpu_definitions.c:110-157). All FP64, all reductions two-pass and
-// order-fixed.
+// (gpu_definitions.c:110-157). FP64 on FP64 data, all reductions two-pass
+// and order-fixed; in the mixed form the element energies of the compliance
+// pass are formed in double-single arithmetic (the level-0 operator's), the
+// rest in FP64.
 #include <cmath>
 #include <vector>
 
+#include "tp_dsf.cuh"
 #include "tp_internal.h"
 
 namespace tp {
 
 __constant__ double c_ke0_design[576];
 __constant__ double c_kz_design[45];
+__constant__ float c_kzd_design[45][2];  // c_kz_design as double-single pairs
 static bool g_kz_design = false;
 
 void set_design_ke(const double* ke0) {
@@ -21,6 +25,12 @@ void set_design_ke(const double* ke0) {
 }
 void set_design_kz(const double* kz45) {
   cudaMemcpyToSymbol(c_kz_design, kz45, sizeof(double) * 45);
+  float d[45][2];
+  for (int i = 0; i < 45; i++) {
+    d[i][0] = (float)kz45[i];
+    d[i][1] = (float)(kz45[i] - (double)d[i][0]);
+  }
+  cudaMemcpyToSymbol(c_kzd_design, d, sizeof(d));
   g_kz_design = true;
 }
 
@@ -65,20 +75,21 @@ constexpr int kMaxBlocks = 4096;
 // (v in the reference's local node order, z[(bx*4 + by*2 + bz)*3 + c]): three
 // butterfly stages, x, y, z. The rigid-translation entries (b = 0) are not
 // formed: KZ's row and column 0..2 vanish.
-__device__ __forceinline__ void t8_transform(const double* v, double* z) {
+template <typename V>
+__device__ __forceinline__ void t8_transform(const V* v, V* z) {
   // local node of corner (dx, dy, dz): dz*4 + (dy ? (dx ? 1 : 0) : (dx ? 2 : 3))
 #pragma unroll
   for (int c = 0; c < 3; c++) {
-    double a[2][2][2];  // [dy][dz][bx]
+    V a[2][2][2];  // [dy][dz][bx]
 #pragma unroll
     for (int dy = 0; dy < 2; dy++)
 #pragma unroll
       for (int dz = 0; dz < 2; dz++) {
-        const double v0 = v[3 * (dz * 4 + (dy ? 0 : 3)) + c], v1 = v[3 * (dz * 4 + (dy ? 1 : 2)) + c];
+        const V v0 = v[3 * (dz * 4 + (dy ? 0 : 3)) + c], v1 = v[3 * (dz * 4 + (dy ? 1 : 2)) + c];
         a[dy][dz][0] = v0 + v1;
         a[dy][dz][1] = v1 - v0;
       }
-    double b[2][2][2];  // [bx][dz][by]
+    V b[2][2][2];  // [bx][dz][by]
 #pragma unroll
     for (int bx = 0; bx < 2; bx++)
 #pragma unroll
@@ -165,6 +176,45 @@ __global__ void sens_kernel(DGeom g, const double* __restrict__ x, const double*
   }
 }
 
+// The compliance pass of the mixed form: the element energy (T u)^T KZ (T u)
+// of sens_kernel<true, true> in double-single arithmetic (on this part an
+// FP64 instruction holds its sub-partition's FP64 unit ~67 cycles, so the
+// FP64 kernel is bound by that unit: about a tenth of its time), the
+// penalty terms and the sums in FP64.
+__global__ void sens_ds_kernel(DGeom g, const double* __restrict__ x, const double* __restrict__ u,
+                               double* __restrict__ out, double* __restrict__ partials, int nr, long vs) {
+  const long ne = (long)g.ex * g.ey * g.ez;
+  const double Ed = 1.0 - 1e-6;
+  double csum = 0.0;
+  for (long e = blockIdx.x * 256L + threadIdx.x; e < ne; e += (long)gridDim.x * 256) {
+    const int j = e % g.ey;
+    const int k = (e / g.ey) % g.ez;
+    const int i = e / ((long)g.ey * g.ez);
+    const double xe = x[e];
+    double d = 0.0;
+    for (int r = 0; r < nr; r++) {
+      Dsf ue[24], zu[24];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const long n = ((long)(i + dloc_dx(q)) * g.nz + (k + dloc_dz(q))) * g.ny + (j + dloc_dy(q));
+#pragma unroll
+        for (int c = 0; c < 3; c++) ue[3 * q + c] = ds_from(u[r * vs + 3 * n + c]);
+      }
+      t8_transform(ue, zu);
+      Dsf en(0.f);
+#define TP_KZ_TERM(i, rr, ss) en += Dsf(c_kzd_design[i][0], c_kzd_design[i][1]) * zu[rr] * zu[ss];
+      TP_KZ_PATTERN(TP_KZ_TERM)
+#undef TP_KZ_TERM
+      const double ed = ds_to(en);
+      csum += ed * (1e-6 + xe * xe * xe * Ed);
+      d += ed * (-3.0 * Ed * xe * xe);
+    }
+    out[e] = d;
+  }
+  const double s = bsum256(csum);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
 static int blocks_for(long n) {
   long b = (n + 255) / 256;
   if (b > kMaxBlocks) b = kMaxBlocks;
@@ -177,7 +227,9 @@ void compliance(tp_ctx* c, const double* u, double* dc, int* nblocks, int nr) {
   const DGeom g = dgeom(c);
   const long ne = (long)g.ex * g.ey * g.ez;
   const int nb = blocks_for(ne);
-  if (c->ec_ok && g_kz_design)
+  if (c->ec_ok && g_kz_design && c->fine_ds)
+    sens_ds_kernel<<<nb, 256, 0, c->s>>>(g, c->d_xphys, u, dc, c->d_red, nr, c->L[0].ndof);
+  else if (c->ec_ok && g_kz_design)
     sens_kernel<true, true><<<nb, 256, 0, c->s>>>(g, c->d_xphys, u, nullptr, dc, c->d_red, nr, c->L[0].ndof);
   else
     sens_kernel<true, false><<<nb, 256, 0, c->s>>>(g, c->d_xphys, u, nullptr, dc, c->d_red, nr, c->L[0].ndof);

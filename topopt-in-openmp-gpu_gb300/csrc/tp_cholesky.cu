@@ -2144,8 +2144,12 @@ __device__ __forceinline__ bool ps_barrier(unsigned* bar, int* err, unsigned tar
   return s_ok != 0;
 }
 
-template <int NR>
-__global__ void __launch_bounds__(kPsWarps * 32) ps_solve_kernel(PsArgs a) {
+// WIDE: 32 positions per lane per round instead of 16 (one warp per whole
+// row, P = 1: a 923-long row in one L2 round trip instead of two; 0.627 ->
+// 0.611 ms per solve of both halves at 256x128x128, the same bits; with two
+// warps per row the narrow rounds are faster, 0.92 against 1.10 ms)
+template <int NR, bool WIDE>
+__device__ __forceinline__ void ps_solve_body(const PsArgs& a) {
   extern __shared__ double sm[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int rl, p;
@@ -2174,7 +2178,7 @@ __global__ void __launch_bounds__(kPsWarps * 32) ps_solve_kernel(PsArgs a) {
       // U positions per lane per round: all their L2 loads are issued before
       // the first multiply-add, so a round costs one L2 latency; the sum
       // still runs over the positions in order
-      constexpr int U = NR == 1 ? 16 : (NR == 2 ? 8 : (NR == 4 ? 4 : 2));
+      constexpr int U = (NR == 1 ? 16 : (NR == 2 ? 8 : (NR == 4 ? 4 : 2))) * (WIDE ? 2 : 1);
       const double* mb = buf((h - a.h0) & 1);
       for (long e0 = r.a0 + lane; e0 < r.a1; e0 += 32L * U) {
         double mv[U], vv[U][NR];
@@ -2186,6 +2190,8 @@ __global__ void __launch_bounds__(kPsWarps * 32) ps_solve_kernel(PsArgs a) {
 #pragma unroll
           for (int v = 0; v < NR; v++) vv[u][v] = in ? __ldcg(r.vb + (v * a.vn + r.voff + e)) : 0.0;
         }
+        // (the compiler keeps the round's loads ahead of its multiply-adds)
+        asm volatile("" ::: "memory");
 #pragma unroll
         for (int u = 0; u < U; u++)
 #pragma unroll
@@ -2233,6 +2239,17 @@ __global__ void __launch_bounds__(kPsWarps * 32) ps_solve_kernel(PsArgs a) {
   }
 }
 
+// the narrow form keeps the compiler's register choice for 256 threads; the
+// wide one may take more (its 32 positions' loads in flight)
+template <int NR>
+__global__ void __launch_bounds__(kPsWarps * 32) ps_solve_kernel(PsArgs a) {
+  ps_solve_body<NR, false>(a);
+}
+template <int NR>
+__global__ void __launch_bounds__(kPsWarps * 32, 1) ps_solve_wide_kernel(PsArgs a) {
+  ps_solve_body<NR, true>(a);
+}
+
 // Launch plan for phases of `rows` rows: R rows per CTA (1, 2, 4 or 8), the
 // fewest that keep at most per_sm CTAs per SM; P = 8/R warps per row; shared
 // memory for two stages of every warp's longest part. false if the stages do
@@ -2261,7 +2278,9 @@ static bool ps_plan_rows(long rows, long bw, int nbs, int nsm, int per_sm, PsPla
     return per >= need;
   };
   const bool ok = fits((const void*)ps_solve_kernel<1>) && fits((const void*)ps_solve_kernel<2>) &&
-                  fits((const void*)ps_solve_kernel<4>) && fits((const void*)ps_solve_kernel<8>);
+                  fits((const void*)ps_solve_kernel<4>) && fits((const void*)ps_solve_kernel<8>) &&
+                  fits((const void*)ps_solve_wide_kernel<1>) && fits((const void*)ps_solve_wide_kernel<2>) &&
+                  fits((const void*)ps_solve_wide_kernel<4>) && fits((const void*)ps_solve_wide_kernel<8>);
   cudaGetLastError();
   if (!ok) return false;
   smem_max = attr;
@@ -2308,7 +2327,10 @@ static void ps_launch_views(tp_ctx* c, const PsView& v0, const PsView& v1, int n
   cfg.stream = c->s;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, ps_solve_kernel<NR>, a);
+  if (P == 1)
+    cudaLaunchKernelEx(&cfg, ps_solve_wide_kernel<NR>, a);
+  else
+    cudaLaunchKernelEx(&cfg, ps_solve_kernel<NR>, a);
 }
 
 template <int NR>

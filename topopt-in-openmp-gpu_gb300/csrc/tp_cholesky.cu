@@ -1590,44 +1590,42 @@ __global__ void nd_scatter_out_kernel(const int* __restrict__ map, long ntot, co
   if (m >= 0) dst[v * n + m] = src[t];
 }
 
-// b_S -= L_SA y_A + L_SB y_B, one warp per row of S; the tails' rows are
-// row-major (tail[s][e] = L(own + s, own - bw + e)). Each lane sums its
-// positions in order into four accumulators (position e to accumulator
-// (e / 32) % 4, so four loads are in flight), which it then adds in a fixed
-// order; then the warp in a fixed tree.
+// b_S -= L_SA y_A + L_SB y_B, one CTA of kCoupleThreads per row of S; the
+// tails' rows are row-major (tail[s][e] = L(own + s, own - bw + e)). Thread
+// t sums positions t, t + 128, ... of each tail in order, each warp in a
+// fixed tree, then the four warps in order.
+constexpr int kCoupleThreads = 128;
 template <int NR>
-__global__ void nd_couple_kernel(const double* __restrict__ tail_a, const double* __restrict__ tail_b, long bw,
-                                 long ns, long own_a, long org_a, long own_b, long org_b, long org_s, long vn,
-                                 const double* __restrict__ y, double* __restrict__ rhs) {
-  const long s = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (s >= ns) return;
-  double acc[4][NR];
+__global__ void __launch_bounds__(kCoupleThreads)
+    nd_couple_kernel(const double* __restrict__ tail_a, const double* __restrict__ tail_b, long bw, long ns,
+                     long own_a, long org_a, long own_b, long org_b, long org_s, long vn,
+                     const double* __restrict__ y, double* __restrict__ rhs) {
+  __shared__ double red[kCoupleThreads / 32][NR];
+  const long s = blockIdx.x;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double acc[NR];
 #pragma unroll
-  for (int u = 0; u < 4; u++)
-#pragma unroll
-    for (int v = 0; v < NR; v++) acc[u][v] = 0.0;
+  for (int v = 0; v < NR; v++) acc[v] = 0.0;
   for (int part = 0; part < 2; part++) {
     const double* L = (part == 0 ? tail_a : tail_b) + s * bw;
     const long own = part == 0 ? own_a : own_b, org = part == 0 ? org_a : org_b;
     const double* yy = y + org + own - bw;  // column own - bw + e of the view
-    const long e0 = lmax(s, bw - own);
-    for (long e = e0 + lane; e < bw; e += 128) {
+    for (long e = lmax(s, bw - own) + threadIdx.x; e < bw; e += kCoupleThreads) {
+      const double l = L[e];
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const long eu = e + 32 * u;
-        if (eu < bw) {
-          const double l = L[eu];
-#pragma unroll
-          for (int v = 0; v < NR; v++) acc[u][v] += l * yy[v * vn + eu];
-        }
-      }
+      for (int v = 0; v < NR; v++) acc[v] += l * yy[v * vn + e];
     }
   }
 #pragma unroll
   for (int v = 0; v < NR; v++) {
-    const double sv = wsum((acc[0][v] + acc[1][v]) + (acc[2][v] + acc[3][v]));
-    if (lane == 0) rhs[v * vn + org_s + s] -= sv;
+    const double sv = wsum(acc[v]);
+    if (lane == 0) red[w][v] = sv;
+  }
+  __syncthreads();
+  if (threadIdx.x < NR) {
+    double t = 0.0;
+    for (int q = 0; q < kCoupleThreads / 32; q++) t += red[q][threadIdx.x];
+    rhs[threadIdx.x * vn + org_s + s] -= t;
   }
 }
 
@@ -2656,7 +2654,7 @@ static void nd_solve_launches(tp_ctx* c, const double* rhs, double* x) {
                           C.ps_R, C.ps_P, C.ps_seg, C.ps_grid, C.ps_smem, rb, y, t, xc);
   };
   sweep(true);
-  nd_couple_kernel<NR><<<grid_for(ns * 32, 256), 256, 0, c->s>>>(C.nd_tail, C.nd_tail + ns * C.bw, C.bw, ns,
+  nd_couple_kernel<NR><<<(unsigned)ns, kCoupleThreads, 0, c->s>>>(C.nd_tail, C.nd_tail + ns * C.bw, C.bw, ns,
                                                                  C.nd_own[0], C.nd_org[0], C.nd_own[1], C.nd_org[1],
                                                                  C.nd_org[2], vn, y, rb);
   ps_launch_views<NR>(c, vs, vs, 1, vn, C.nd_nblk[2], 0, 0, ps_nall(C.nd_nblk[2], 0), C.ps_R, C.ps_P, C.ps_seg,

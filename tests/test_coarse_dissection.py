@@ -10,7 +10,9 @@ default), checked on the CPU (no GPU needed).
    tails' rows, and the solve: the forward phases of both views
    (ps_solve_kernel's FA / FB rows), nd_couple_kernel, S's forward and
    backward phases, nd_tails_kernel, the backward phases with tails (BA of
-   every block, the last included) and the gather / scatter through nd_map.
+   every block, the last included) and the gather / scatter through nd_map;
+   with both halves in every phase and with the halves swept in turn (the
+   form for bands too wide for a phase of both).
    On small grids with a random SPD operator of the coarse pattern (fixed
    rows and columns as the coarsest level has them) the composite solve
    equals a dense solve to rounding, with equal and unequal halves and with
@@ -44,7 +46,7 @@ def layout(nx, ny, nz, nbs):
     return dict(xs=xs, ns=plane, pad=pad, own=own, org=org, ntot=org[2] + plane, nblk=nblk, bw=bw)
 
 
-def composite_solve(nx, ny, nz, lim, nbs, seed):
+def composite_solve(nx, ny, nz, lim, nbs, seed, sequential=False):
     rng = np.random.default_rng(seed)
     nn, n = nx * ny * nz, 3 * nx * ny * nz
     Ly = layout(nx, ny, nz, nbs)
@@ -206,7 +208,16 @@ def composite_solve(nx, ny, nz, lim, nbs, seed):
                 arr[o] = val
 
     m = max(nblk[0], nblk[1])
-    run([0, 1], m, 1, 0, 2 * m - 1)
+
+    def sweep(fwd):  # both halves in every phase, or one after the other (wide bands)
+        if sequential:
+            for v in (0, 1):
+                mv = nblk[v]
+                run([v], mv, 1, 0 if fwd else 2 * mv - 1, 2 * mv - 1 if fwd else 4 * mv - 1)
+        else:
+            run([0, 1], m, 1, 0 if fwd else 2 * m - 1, 2 * m - 1 if fwd else 4 * m - 1)
+
+    sweep(True)
     for s in range(ns):  # nd_couple_kernel
         acc = 0.0
         for v in range(2):
@@ -216,17 +227,18 @@ def composite_solve(nx, ny, nz, lim, nbs, seed):
     run([2], nblk[2], 0, 0, 4 * nblk[2] - 2)
     for v in range(2):  # nd_tails_kernel
         x[org[v] + own[v]:org[v] + own[v] + ns] = x[org[2]:org[2] + ns]
-    run([0, 1], m, 1, 2 * m - 1, 4 * m - 1)
+    sweep(False)
     x_nat = np.zeros(n)
     x_nat[mp[mp >= 0]] = x[mp >= 0]  # nd_scatter_out_kernel
     ref = np.linalg.solve(K, b_nat)
     return np.linalg.norm(x_nat - ref) / np.linalg.norm(ref)
 
 
+@pytest.mark.parametrize("sequential", [False, True], ids=["both_halves_per_phase", "halves_in_turn"])
 @pytest.mark.parametrize("grid", [(9, 5, 5, 1, 64, 0), (8, 5, 5, 1, 96, 1), (11, 4, 6, 1, 128, 2)],
                          ids=["halves_4_4_bw_over_block", "halves_3_4", "halves_5_5"])
-def test_composite_solve_model(grid):
-    assert composite_solve(*grid) < 1e-12
+def test_composite_solve_model(grid, sequential):
+    assert composite_solve(*grid, sequential=sequential) < 1e-12
 
 
 def pf_imax(n, bw, k):

@@ -41,9 +41,9 @@ def _design(seed=0):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("nr", [3, 5, 8], ids=["cases3", "cases5", "cases8"])  # column chunks 2+1, 4+1, 8
 @pytest.mark.parametrize("prec", [tp.TP_FP64, tp.TP_MIXED], ids=["fp64", "mixed"])
-def test_batched_solve_matches_single(cuda, prec):
-    nr = 3
+def test_batched_solve_matches_single(cuda, prec, nr):
     F = tp.multiload(*SHAPE, nr, 5, seed=1)
     x = _design()
     g = tp.TopOpt(*SHAPE, NL, precision=prec, nrhs=nr)

@@ -119,6 +119,12 @@ tp_status tp_fixed_dofs(const tp_ctx* c, int level, long* out_host, long* count)
  * Jacobi diagonals, assembled stencils of levels >= 1, and the band Cholesky
  * factor of the coarsest level on FP64 storage (stencil_solvers.c:283-302). */
 tp_status tp_assemble(tp_ctx* c);
+/* The same assembly enqueued on the context's stream without waiting, so that
+ * host work (copies on streams of the caller's own) overlaps it; the next
+ * tp_assemble completes it and reports its status. A change of xPhys or of
+ * the solver's set-up in between discards it (tp_assemble then assembles
+ * again). */
+tp_status tp_assemble_async(tp_ctx* c);
 
 /* Operators on device vectors of level `level`.
  * level 0: the matrix-free hex8 stencil (stencil_methods.c:7-428);

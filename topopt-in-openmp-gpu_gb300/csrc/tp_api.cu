@@ -252,7 +252,8 @@ static tp_status assemble_status(tp_ctx* c, int info) {
 }
 
 static tp_status assemble(tp_ctx* c) {
-  assemble_enqueue(c);
+  if (!c->assemble_pending) assemble_enqueue(c);
+  c->assemble_pending = false;
   tp_status st = check(c);
   if (st != TP_OK) return st;
   cudaMemcpyAsync(c->h_info, c->coarse.info, sizeof(int), cudaMemcpyDeviceToHost, c->s);
@@ -596,6 +597,7 @@ tp_status tp_field_written(tp_ctx* c, tp_field f) {
   if (!c || !tp_field_ptr(c, f)) return TP_ERR_ARG;
   if (f == TP_FIELD_XPHYS) {
     c->assembled = false;
+    c->assemble_pending = false;
     for (int l = 0; l < TP_MAXL; l++) c->st_sub_valid[l] = false;
   }
   return TP_OK;
@@ -657,6 +659,17 @@ tp_status tp_fixed_dofs(const tp_ctx* c, int level, long* out_host, long* count)
 tp_status tp_assemble(tp_ctx* c) {
   if (!c) return TP_ERR_ARG;
   return assemble(c);
+}
+
+// The assembly enqueued without a wait: the caller's host work (copies on
+// streams of its own) overlaps it; the next tp_assemble completes it (one
+// synchronisation, the factor's status) unless xPhys or the solver's set-up
+// changed in between, which discards it.
+tp_status tp_assemble_async(tp_ctx* c) {
+  if (!c) return TP_ERR_ARG;
+  if (!c->assemble_pending) assemble_enqueue(c);
+  c->assemble_pending = true;
+  return check(c);
 }
 
 tp_status tp_apply(tp_ctx* c, int level, const double* in, double* out) {
@@ -852,6 +865,7 @@ tp_status tp_init_design(tp_ctx* c) {
   filter_adj(c, c->d_dv, c->d_xnew);
   cudaMemsetAsync(c->d_U, 0, sizeof(double) * c->L[0].ndof * c->p.nrhs, c->s);
   c->assembled = false;
+  c->assemble_pending = false;
   return sync_check(c);
 }
 
@@ -878,6 +892,7 @@ static tp_status design_iteration_host(tp_ctx* c, tp_iter_info* info) {
   }
   filter_fwd(c, c->d_x, c->d_xphys);
   c->assembled = false;
+  c->assemble_pending = false;
   cudaEventRecord(c->it_ev[1], c->s);
   cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, c->s);
   st = sync_check(c);
@@ -926,6 +941,7 @@ static tp_status design_iteration_device(tp_ctx* c, tp_iter_info* info) {
   // the factor's status first: a failed factor makes every later value moot
   st = assemble_status(c, *c->h_info);
   c->assembled = false;  // xPhys has changed
+  c->assemble_pending = false;
   if (st != TP_OK) return st;
   int it = 0;
   double rr = 0;

@@ -87,6 +87,7 @@ tp_status tp_set_fine_arith(tp_ctx* c, int arith) {
 static void coarse_reset(tp_ctx* c) {
   coarse_graphs_free(c);
   c->assembled = false;
+  c->assemble_pending = false;
   graph_free(c);
 }
 

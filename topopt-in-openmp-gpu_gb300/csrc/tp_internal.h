@@ -253,6 +253,7 @@ struct tp_ctx {
   tp::EcPlan ec_f32[4], ec_f64[4], ec_ds[4];
 
   bool assembled = false;    // operators built for the current xPhys
+  bool assemble_pending = false;  // tp_assemble_async enqueued an assembly that tp_assemble completes
   long mem_bytes = 0;
 
   // the multi-load solve: one CUDA graph per context, a while-node looping

@@ -318,6 +318,13 @@ Pipe& pipe() {
   static Pipe* p = new Pipe();  // kept until exit, like the staging cache
   return *p;
 }
+// the pipe's stream (created on first use), or null (then copies go on the
+// legacy stream)
+cudaStream_t transfer_stream() {
+  Pipe& P = pipe();
+  std::lock_guard<std::mutex> lock(P.mu);
+  return P.ready() ? P.st : nullptr;
+}
 
 // fill(l, dst): canonical line l into dst[0 .. len); n: the array's doubles
 // (the last line may be short)
@@ -375,8 +382,10 @@ void down_lines(const double* d, long n, long len, Drain drain) {
 // copy engines read pageable memory over the host link at ~85-185 GB/s on
 // this part, several times a host-side conversion into staging; the halo is
 // neither read nor written); float arrays (the float flavour) take the
-// pipelined conversion above.
-bool copy_box(double* dev, double* host, long len, long nk, long ni, long sk, long si, bool up) {
+// pipelined conversion above. With a stream s, the copy goes on s (a stream
+// that does not wait for the context's) and returns once it has landed.
+bool copy_box(double* dev, double* host, long len, long nk, long ni, long sk, long si, bool up,
+              cudaStream_t s = nullptr) {
   cudaMemcpy3DParms p = {};
   const cudaPitchedPtr hp = make_cudaPitchedPtr(host, sk * sizeof(double), sk, si / sk);
   const cudaPitchedPtr dp = make_cudaPitchedPtr(dev, len * sizeof(double), len, nk);
@@ -384,7 +393,9 @@ bool copy_box(double* dev, double* host, long len, long nk, long ni, long sk, lo
   p.dstPtr = up ? dp : hp;
   p.extent = make_cudaExtent(len * sizeof(double), nk, ni);
   p.kind = up ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
-  if (cudaMemcpy3D(&p) != cudaSuccess) return false;
+  if (s ? (cudaMemcpy3DAsync(&p, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
+        : cudaMemcpy3D(&p) != cudaSuccess)
+    return false;
   (up ? g_h2d : g_d2h) += len * nk * ni * (long)sizeof(double);
   return true;
 }
@@ -394,10 +405,11 @@ bool copy_box(double* dev, double* host, long len, long nk, long ni, long sk, lo
 // (x, z)), and a plain array of n values (lines of kPlain)
 constexpr long kPlain = 4096;
 template <typename T>
-void up_nodes(double* d, const Dims& dm, const T* v) {
+void up_nodes(double* d, const Dims& dm, const T* v, cudaStream_t s = nullptr) {
   const long len = 3L * (dm.ey + 1), nz = dm.ez + 1;
   if constexpr (sizeof(T) == sizeof(double)) {
-    if (copy_box(d, (double*)(v + 3 * pnode(dm, 0, 0, 0)), len, nz, dm.ex + 1, 3L * dm.wy, 3L * dm.wy * dm.wz, true))
+    if (copy_box(d, (double*)(v + 3 * pnode(dm, 0, 0, 0)), len, nz, dm.ex + 1, 3L * dm.wy, 3L * dm.wy * dm.wz, true,
+                 s))
       return;
     cudaGetLastError();
   }
@@ -809,11 +821,16 @@ void solveStateMG_halo(const struct gpuGrid* gpu_gc, DTYPE* x, const int nswp, c
   const Dims d = dims_of((int)gc.nelx, (int)gc.nely, (int)gc.nelz, 0);
   double* F = tp_field_ptr(c, TP_FIELD_F);
   double* U = tp_field_ptr(c, TP_FIELD_U);
-  up_nodes(F, d, b);
-  up_nodes(U, d, u);
   // the reference's nswp and tol arrive per call; omega 0.6 and the cap of
   // 1000 iterations are fixed there (stencil_solvers.c:332-334)
   check(c, tp_set_cg(c, (double)tol, 1000, nswp, 0.6), "solver settings");
+  // the operators (from xPhys alone) are assembled on the device while F and
+  // U cross the host link on the transfer stream, which does not wait for
+  // the context's
+  check(c, tp_assemble_async(c), "assemble");
+  const cudaStream_t s = transfer_stream();
+  up_nodes(F, d, b, s);
+  up_nodes(U, d, u, s);
   int it = 0;
   double rr = 0;
   check(c, tp_assemble(c), "assemble");
